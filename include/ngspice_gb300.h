@@ -1,0 +1,80 @@
+/*
+ * Engine-level C ABI of the GB300 transient engine: the operator surface
+ * underneath the sharedspice API (sharedspice.h), for callers that drive
+ * circuits directly and for the parity tests.
+ *
+ * Reference interfaces each entry point replaces:
+ *   ngsf_open     netlist -> circuit: INPpas1/INPpas2 (src/spicelib/parser/
+ *                 inppas1.c, inppas2.c), CKTsetup (src/spicelib/analysis/
+ *                 cktsetup.c:34), CKTtemp, SMPpreOrder + SMPreorder
+ *                 (src/maths/KLU/klusmp.c:1256, :753) on the first stamped
+ *                 matrix
+ *   ngsf_run      CKTdoJob -> DCtran (src/spicelib/analysis/dctran.c:67) with
+ *                 CKTload/DEVload, SMPluFac, SMPsolve, NIconvTest, CKTtrunc on
+ *                 the GPU; many circuits in one launch
+ *   ngsf_points   the accepted-point stream CKTdump -> OUTpData
+ *                 (src/spicelib/analysis/cktdump.c:33)
+ *   ngsf_capture  the stamped matrix and right-hand side of each Newton
+ *                 iteration (what NIiter hands to SMPluFac, niiter.c:156)
+ * All calls return 0 on success and a nonzero code on failure (NGSF_E_*
+ * values of the reference's sperror.h where one applies, -1 otherwise);
+ * ngsf_last_error() describes the last failure.
+ */
+#ifndef NGSPICE_GB300_H
+#define NGSPICE_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NGSF_API __attribute__((visibility("default")))
+
+typedef struct ngsf_handle ngsf_handle;
+
+/* Parse, compile, upload and pivot one circuit.  probes: space-separated
+ * equation names to record at every accepted point (NULL or "" = all).
+ * outcap: accepted points to keep.  capmax: Newton iterations whose
+ * stamped system is captured (0 = none).  Returns NULL on error. */
+NGSF_API ngsf_handle *ngsf_open(const char *netlist, const char *probes, int outcap,
+                                int capmax);
+/* Host-only compile (parse, setup, temperature; no device, no pivoting):
+ * ngsf_info / ngsf_eq_name / ngsf_pattern work on the result, ngsf_run
+ * refuses it.  Replaces the reference's INPpas1/INPpas2 + CKTsetup +
+ * CKTtemp without SMPpreOrder. */
+NGSF_API ngsf_handle *ngsf_compile(const char *netlist);
+NGSF_API void ngsf_close(ngsf_handle *h);
+NGSF_API const char *ngsf_last_error(void);
+
+/* sizes: unknowns, matrix nonzeros, state doubles, L+U nonzeros */
+NGSF_API int ngsf_info(const ngsf_handle *h, int *n, int *nnz, int *nstates, int *nlu);
+/* name of equation eq (1..n) */
+NGSF_API int ngsf_eq_name(const ngsf_handle *h, int eq, char *buf, int len);
+/* matrix pattern, CSC: colptr[n+1], rowidx[nnz] (0-based equations - 1) */
+NGSF_API int ngsf_pattern(const ngsf_handle *h, int *colptr, int *rowidx);
+/* probe list: equation numbers (1..n) of the recorded values */
+NGSF_API int ngsf_probes(const ngsf_handle *h, int *eqs, int max);
+
+/* Run .tran on count circuits in one GPU launch.  max_steps bounds the
+ * time loop of each circuit.  seconds (may be NULL) receives the device
+ * time of the launch. */
+NGSF_API int ngsf_run(ngsf_handle *const *hs, int count, long long max_steps,
+                      double *seconds);
+
+/* results: ires[NGSF_R_COUNT] (status, npoints, accepted, rejected,
+ * numIter, tranIter, timePts, ncap, opIter, badPivot), fres[2] */
+NGSF_API int ngsf_results(const ngsf_handle *h, int *ires, double *fres);
+/* accepted points: buf[np][1 + nprobe] = time, probe values; returns np */
+NGSF_API int ngsf_points(const ngsf_handle *h, double *buf, int maxpoints);
+/* captured iterations: ax[k][nnz], rhs[k][n+1], rhsold[k][n+1],
+ * meta[k][4] = time, delta, mode, order; returns the count */
+NGSF_API int ngsf_capture(ngsf_handle *h, double *ax, double *rhs, double *rhsold,
+                          double *meta, int maxcap);
+/* floating-point operations of one LU refactorization (multiply-adds) */
+NGSF_API double ngsf_lu_flops(const ngsf_handle *h);
+/* device bytes held by the circuit */
+NGSF_API long long ngsf_device_bytes(const ngsf_handle *h);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

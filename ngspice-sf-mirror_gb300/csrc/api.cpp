@@ -1,0 +1,646 @@
+/*
+ * C ABI: engine entry points (include/ngspice_gb300.h) and the
+ * sharedspice-compatible API (include/sharedspice.h).
+ *
+ * The sharedspice layer keeps the reference's observable behaviour for the
+ * transient path (src/sharedspice.c): commands are executed immediately,
+ * "bg_run" runs the analysis on a background thread and reports through
+ * BGThreadRunning, every accepted point is sent through SendData after
+ * SendInitData has described the vectors, output vectors are looked up by
+ * name with ngGet_Vec_Info, errors return 1.
+ */
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <map>
+#include <mutex>
+#include <sstream>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include "../../include/ngspice_gb300.h"
+#include "../../include/sharedspice.h"
+#include "circuit.h"
+#include "runtime.h"
+
+using namespace ngsf;
+
+struct ngsf_handle {
+    Prepared p;
+};
+
+namespace {
+thread_local std::string g_err;
+
+int fail(const std::string &msg, int code = -1)
+{
+    g_err = msg;
+    return code;
+}
+}  // namespace
+
+extern "C" {
+
+NGSF_API const char *ngsf_last_error(void) { return g_err.c_str(); }
+
+NGSF_API ngsf_handle *ngsf_open(const char *netlist, const char *probes, int outcap, int capmax)
+{
+    try {
+        auto h = std::make_unique<ngsf_handle>();
+        std::vector<std::string> pr;
+        if (probes) {
+            std::istringstream is(probes);
+            std::string t;
+            while (is >> t) {
+                for (auto &ch : t)
+                    ch = (char)tolower((unsigned char)ch);
+                pr.push_back(t);
+            }
+        }
+        prepare(h->p, netlist ? netlist : "", pr, outcap > 0 ? outcap : 1, capmax > 0 ? capmax : 0);
+        return h.release();
+    } catch (const std::exception &e) {
+        g_err = e.what();
+        return nullptr;
+    }
+}
+
+NGSF_API ngsf_handle *ngsf_compile(const char *netlist)
+{
+    try {
+        auto h = std::make_unique<ngsf_handle>();
+        h->p.ckt = parse_netlist(netlist ? netlist : "");
+        compile(*h->p.ckt, h->p.img);
+        return h.release();
+    } catch (const std::exception &e) {
+        g_err = e.what();
+        return nullptr;
+    }
+}
+
+NGSF_API void ngsf_close(ngsf_handle *h) { delete h; }
+
+NGSF_API int ngsf_info(const ngsf_handle *h, int *n, int *nnz, int *nstates, int *nlu)
+{
+    if (!h)
+        return fail("null handle");
+    if (n) *n = h->p.img.n;
+    if (nnz) *nnz = (int)h->p.img.a_ri.size();
+    if (nstates) *nstates = h->p.img.nstates;
+    if (nlu) *nlu = h->p.img.nlu;
+    return 0;
+}
+
+NGSF_API int ngsf_eq_name(const ngsf_handle *h, int eq, char *buf, int len)
+{
+    if (!h || eq < 1 || eq > h->p.img.n || !buf || len <= 0)
+        return fail("bad equation");
+    snprintf(buf, (size_t)len, "%s", h->p.img.names[eq - 1].c_str());
+    return 0;
+}
+
+NGSF_API int ngsf_pattern(const ngsf_handle *h, int *colptr, int *rowidx)
+{
+    if (!h)
+        return fail("null handle");
+    const Image &m = h->p.img;
+    if (colptr)
+        memcpy(colptr, m.a_cp.data(), m.a_cp.size() * sizeof(int));
+    if (rowidx)
+        memcpy(rowidx, m.a_ri.data(), m.a_ri.size() * sizeof(int));
+    return 0;
+}
+
+NGSF_API int ngsf_probes(const ngsf_handle *h, int *eqs, int max)
+{
+    if (!h)
+        return fail("null handle");
+    int n = (int)h->p.probes.size();
+    for (int i = 0; i < n && i < max; i++)
+        eqs[i] = h->p.probes[i];
+    return n;
+}
+
+NGSF_API int ngsf_run(ngsf_handle *const *hs, int count, long long max_steps, double *seconds)
+{
+    try {
+        std::vector<Prepared *> cs;
+        for (int i = 0; i < count; i++) {
+            if (!hs[i])
+                return fail("null handle");
+            if (!hs[i]->p.dev)
+                return fail("circuit was compiled without a device (ngsf_compile)");
+            cs.push_back(&hs[i]->p);
+        }
+        run_batch(cs, max_steps > 0 ? max_steps : 100000000LL, seconds);
+        return 0;
+    } catch (const std::exception &e) {
+        return fail(e.what());
+    }
+}
+
+NGSF_API int ngsf_results(const ngsf_handle *h, int *ires, double *fres)
+{
+    if (!h || h->p.ires.empty())
+        return fail("no results");
+    if (ires)
+        memcpy(ires, h->p.ires.data(), NGSF_R_COUNT * sizeof(int));
+    if (fres)
+        memcpy(fres, h->p.fres.data(), NGSF_F_COUNT * sizeof(double));
+    return 0;
+}
+
+NGSF_API int ngsf_points(const ngsf_handle *h, double *buf, int maxpoints)
+{
+    if (!h)
+        return fail("null handle");
+    int w = 1 + (int)h->p.probes.size();
+    int np = (int)(h->p.points.size() / (size_t)w);
+    if (np > maxpoints)
+        np = maxpoints;
+    if (buf && np)
+        memcpy(buf, h->p.points.data(), (size_t)np * w * sizeof(double));
+    return np;
+}
+
+NGSF_API int ngsf_capture(ngsf_handle *h, double *ax, double *rhs, double *rhsold, double *meta,
+                          int maxcap)
+{
+    try {
+        if (!h || h->p.ires.empty())
+            return fail("no results");
+        int nc = h->p.ires[NGSF_R_NCAP];
+        std::vector<double> a, r, m;
+        h->p.dev->read_capture(nc, a, r, m);
+        int n1 = h->p.img.n + 1;
+        int nnz = (int)h->p.img.a_ri.size();
+        int capmax = (int)(r.size() / (2 * (size_t)n1));
+        int k = nc < maxcap ? nc : maxcap;
+        if (k > capmax)
+            k = capmax;
+        for (int c = 0; c < k; c++) {
+            if (ax)
+                memcpy(ax + (size_t)c * nnz, a.data() + (size_t)c * nnz, nnz * sizeof(double));
+            if (rhs)
+                memcpy(rhs + (size_t)c * n1, r.data() + (size_t)c * n1, n1 * sizeof(double));
+            if (rhsold)
+                memcpy(rhsold + (size_t)c * n1, r.data() + (size_t)(capmax + c) * n1,
+                       n1 * sizeof(double));
+            if (meta)
+                memcpy(meta + 4 * c, m.data() + 4 * c, 4 * sizeof(double));
+        }
+        return k;
+    } catch (const std::exception &e) {
+        return fail(e.what());
+    }
+}
+
+NGSF_API double ngsf_lu_flops(const ngsf_handle *h) { return h ? h->p.img.lu_flops : 0.0; }
+
+NGSF_API long long ngsf_device_bytes(const ngsf_handle *h)
+{
+    return (h && h->p.dev) ? (long long)h->p.dev->bytes() : 0;
+}
+
+}  // extern "C"
+
+/* ====================================================================== */
+/* sharedspice layer                                                       */
+/* ====================================================================== */
+namespace {
+
+struct Vec {
+    std::string name;
+    std::vector<double> data;
+    vector_info info{};
+};
+
+struct Plot {
+    std::string name, title, type;
+    std::vector<std::unique_ptr<Vec>> vecs;
+};
+
+struct Shared {
+    std::recursive_mutex mu;
+    SendChar *pfcn = nullptr;
+    SendStat *statfcn = nullptr;
+    ControlledExit *ngexit = nullptr;
+    SendData *datfcn = nullptr;
+    SendInitData *initfcn = nullptr;
+    BGThreadRunning *bgfcn = nullptr;
+    void *user = nullptr;
+    int ident = 0;
+    std::string deck;                 /* current circuit text */
+    std::vector<std::unique_ptr<Plot>> plots;
+    int cur = -1;
+    std::thread bg;
+    bool running = false;
+    std::vector<char *> nameList;     /* storage for AllPlots/AllVecs */
+    std::vector<std::string> nameStore;
+    std::vector<double> extraBreaks;
+    int tranCount = 0;
+} S;
+
+void say(const char *fmt, ...)
+{
+    char buf[2048];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (S.pfcn)
+        S.pfcn(buf, S.ident, S.user);
+}
+
+std::string lower(std::string s)
+{
+    for (auto &c : s)
+        c = (char)tolower((unsigned char)c);
+    return s;
+}
+
+/* replace (or add) the .tran card of the deck */
+std::string with_tran(const std::string &deck, const std::string &tranArgs)
+{
+    std::istringstream is(deck);
+    std::ostringstream os;
+    std::string line;
+    bool first = true;
+    while (std::getline(is, line)) {
+        std::string l = lower(line);
+        size_t b = l.find_first_not_of(" \t");
+        if (!first && b != std::string::npos && l.compare(b, 5, ".tran") == 0)
+            continue;
+        if (!first && b != std::string::npos && l.compare(b, 4, ".end") == 0 &&
+            (l.size() == b + 4 || isspace((unsigned char)l[b + 4]))) {
+            if (!tranArgs.empty())
+                os << ".tran " << tranArgs << "\n";
+            os << line << "\n";
+            first = false;
+            continue;
+        }
+        os << line << "\n";
+        first = false;
+    }
+    return os.str();
+}
+
+int do_tran(const std::string &tranArgs)
+{
+    std::string deck;
+    {
+        std::lock_guard<std::recursive_mutex> g(S.mu);
+        if (S.deck.empty()) {
+            say("stderr Error: there is no circuit loaded");
+            return 1;
+        }
+        deck = tranArgs.empty() ? S.deck : with_tran(S.deck, tranArgs);
+    }
+    ngsf_handle *h = ngsf_open(deck.c_str(), nullptr, 1 << 22, 0);
+    if (!h) {
+        say("stderr Error: %s", ngsf_last_error());
+        return 1;
+    }
+    if (S.statfcn) {
+        char st[] = "tran 0.0%";
+        S.statfcn(st, S.ident, S.user);
+    }
+    int rc = ngsf_run(&h, 1, 0, nullptr);
+    if (rc) {
+        say("stderr Error: %s", ngsf_last_error());
+        ngsf_close(h);
+        return 1;
+    }
+    int ires[NGSF_R_COUNT];
+    ngsf_results(h, ires, nullptr);
+    if (ires[NGSF_R_STATUS] != 0) {
+        say("stderr Error: transient analysis failed with code %d (time %g)", ires[NGSF_R_STATUS],
+            h->p.fres[NGSF_F_TIME]);
+    }
+    auto plot = std::make_unique<Plot>();
+    {
+        std::lock_guard<std::recursive_mutex> g(S.mu);
+        plot->name = "tran" + std::to_string(++S.tranCount);
+        plot->title = h->p.ckt->title;
+        plot->type = "transient";
+    }
+    int n = h->p.img.n;
+    int np = ires[NGSF_R_NPOINTS];
+    int w = 1 + (int)h->p.probes.size();
+    auto tv = std::make_unique<Vec>();
+    tv->name = "time";
+    std::vector<std::unique_ptr<Vec>> vs;
+    for (int i = 0; i < n; i++) {
+        auto v = std::make_unique<Vec>();
+        v->name = h->p.img.names[i];
+        vs.push_back(std::move(v));
+    }
+    const std::vector<double> &pts = h->p.points;
+    for (int k = 0; k < np && (size_t)(k + 1) * w <= pts.size(); k++) {
+        tv->data.push_back(pts[(size_t)k * w]);
+        for (int i = 0; i < n; i++)
+            vs[i]->data.push_back(pts[(size_t)k * w + 1 + i]);
+    }
+    plot->vecs.push_back(std::move(tv));
+    for (auto &v : vs)
+        plot->vecs.push_back(std::move(v));
+    for (auto &v : plot->vecs) {
+        v->info.v_name = (char *)v->name.c_str();
+        v->info.v_type = v->name == "time" ? 1 : (v->name.find("#branch") != std::string::npos ? 4 : 3);
+        v->info.v_flags = 1;   /* VF_REAL */
+        v->info.v_realdata = v->data.data();
+        v->info.v_compdata = nullptr;
+        v->info.v_length = (int)v->data.size();
+    }
+    /* SendInitData once, then SendData per accepted point */
+    if (S.initfcn) {
+        std::vector<vecinfo> vi(plot->vecs.size());
+        std::vector<pvecinfo> pvi(plot->vecs.size());
+        for (size_t i = 0; i < plot->vecs.size(); i++) {
+            vi[i].number = (int)i;
+            vi[i].vecname = (char *)plot->vecs[i]->name.c_str();
+            vi[i].is_real = true;
+            vi[i].pdvec = &plot->vecs[i]->info;
+            vi[i].pdvecscale = &plot->vecs[0]->info;
+            pvi[i] = &vi[i];
+        }
+        vecinfoall all{(char *)plot->name.c_str(), (char *)plot->title.c_str(),
+                       (char *)"", (char *)plot->type.c_str(), (int)vi.size(), pvi.data()};
+        S.initfcn(&all, S.ident, S.user);
+    }
+    if (S.datfcn) {
+        size_t nv = plot->vecs.size();
+        std::vector<vecvalues> vv(nv);
+        std::vector<pvecvalues> pv(nv);
+        for (size_t i = 0; i < nv; i++) {
+            vv[i].name = (char *)plot->vecs[i]->name.c_str();
+            vv[i].cimag = 0;
+            vv[i].is_scale = i == 0;
+            vv[i].is_complex = false;
+            pv[i] = &vv[i];
+        }
+        for (int k = 0; k < (int)plot->vecs[0]->data.size(); k++) {
+            for (size_t i = 0; i < nv; i++)
+                vv[i].creal = plot->vecs[i]->data[k];
+            vecvaluesall all{(int)nv, k, pv.data()};
+            S.datfcn(&all, (int)nv, S.ident, S.user);
+        }
+    }
+    {
+        std::lock_guard<std::recursive_mutex> g(S.mu);
+        S.plots.push_back(std::move(plot));
+        S.cur = (int)S.plots.size() - 1;
+    }
+    ngsf_close(h);
+    if (S.statfcn) {
+        char st[] = "--ready--";
+        S.statfcn(st, S.ident, S.user);
+    }
+    return ires[NGSF_R_STATUS] == 0 ? 0 : 1;
+}
+
+std::string g_lastTran;
+
+int command(const std::string &raw)
+{
+    std::string cmd = raw;
+    size_t b = cmd.find_first_not_of(" \t");
+    if (b == std::string::npos)
+        return 0;
+    cmd = cmd.substr(b);
+    std::istringstream is(cmd);
+    std::string verb;
+    is >> verb;
+    verb = lower(verb);
+    std::string rest;
+    std::getline(is, rest);
+    if (verb == "source") {
+        std::string path = rest.substr(rest.find_first_not_of(" \t") == std::string::npos
+                                           ? rest.size()
+                                           : rest.find_first_not_of(" \t"));
+        std::ifstream f(path);
+        if (!f) {
+            say("stderr Error: cannot open %s", path.c_str());
+            return 1;
+        }
+        std::stringstream ss;
+        ss << f.rdbuf();
+        std::lock_guard<std::recursive_mutex> g(S.mu);
+        S.deck = ss.str();
+        return 0;
+    }
+    if (verb == "tran") {
+        g_lastTran = rest;
+        return do_tran(rest);
+    }
+    if (verb == "run")
+        return do_tran("");
+    if (verb == "bg_run" || verb == "bg_tran") {
+        if (S.running)
+            return 1;
+        std::string args = verb == "bg_tran" ? rest : "";
+        if (S.bg.joinable())
+            S.bg.join();
+        S.running = true;
+        if (S.bgfcn)
+            S.bgfcn(false, S.ident, S.user);
+        S.bg = std::thread([args] {
+            do_tran(args);
+            S.running = false;
+            if (S.bgfcn)
+                S.bgfcn(true, S.ident, S.user);
+        });
+        return 0;
+    }
+    if (verb == "bg_halt" || verb == "bg_resume" || verb == "halt") {
+        /* the whole run executes on the device as one launch; halting mid
+         * run is not offered, the calls only synchronise */
+        if (S.bg.joinable())
+            S.bg.join();
+        return 0;
+    }
+    if (verb == "remcirc" || verb == "destroy" || verb == "reset") {
+        std::lock_guard<std::recursive_mutex> g(S.mu);
+        if (verb == "remcirc")
+            S.deck.clear();
+        if (verb == "destroy")
+            S.plots.clear(), S.cur = -1;
+        return 0;
+    }
+    if (verb == "echo") {
+        say("stdout %s", rest.c_str());
+        return 0;
+    }
+    if (verb == "quit" || verb == "exit") {
+        if (S.ngexit)
+            S.ngexit(0, false, true, S.ident, S.user);
+        return 0;
+    }
+    if (verb == "set" || verb == "unset" || verb == "option" || verb == "setplot") {
+        if (verb == "setplot") {
+            std::string nm;
+            std::istringstream r(rest);
+            r >> nm;
+            for (size_t i = 0; i < S.plots.size(); i++)
+                if (S.plots[i]->name == nm)
+                    S.cur = (int)i;
+        }
+        return 0;
+    }
+    say("stderr Error: unsupported command %s", verb.c_str());
+    return 1;
+}
+
+}  // namespace
+
+extern "C" {
+
+IMPEXP int ngSpice_Init(SendChar *printfcn, SendStat *statfcn, ControlledExit *ngexit,
+                        SendData *sdata, SendInitData *sinitdata, BGThreadRunning *bgtrun,
+                        void *userData)
+{
+    std::lock_guard<std::recursive_mutex> g(S.mu);
+    S.pfcn = printfcn;
+    S.statfcn = statfcn;
+    S.ngexit = ngexit;
+    S.datfcn = sdata;
+    S.initfcn = sinitdata;
+    S.bgfcn = bgtrun;
+    S.user = userData;
+    return 0;
+}
+
+IMPEXP int ngSpice_Init_Sync(GetVSRCData *vsrcdat, GetISRCData *isrcdat, GetSyncData *syncdat,
+                             int *ident, void *userData)
+{
+    (void)vsrcdat;
+    (void)isrcdat;
+    (void)syncdat;
+    std::lock_guard<std::recursive_mutex> g(S.mu);
+    if (ident)
+        S.ident = *ident;
+    if (userData)
+        S.user = userData;
+    return 0;
+}
+
+IMPEXP int ngSpice_Command(char *cmd)
+{
+    if (!cmd) {
+        /* NULL command: the reference clears its internal state */
+        return 0;
+    }
+    try {
+        return command(cmd);
+    } catch (const std::exception &e) {
+        say("stderr Error: %s", e.what());
+        return 1;
+    }
+}
+
+IMPEXP pvector_info ngGet_Vec_Info(char *vecname)
+{
+    if (!vecname)
+        return nullptr;
+    std::lock_guard<std::recursive_mutex> g(S.mu);
+    if (S.cur < 0)
+        return nullptr;
+    std::string nm = lower(vecname);
+    /* accept v(node) and i(source) the way vector lookup does */
+    if (nm.size() > 3 && nm[1] == '(' && nm.back() == ')') {
+        std::string inner = nm.substr(2, nm.size() - 3);
+        if (nm[0] == 'v')
+            nm = inner;
+        else if (nm[0] == 'i')
+            nm = inner + "#branch";
+    }
+    for (auto &v : S.plots[S.cur]->vecs)
+        if (v->name == nm)
+            return &v->info;
+    return nullptr;
+}
+
+IMPEXP int ngSpice_Circ(char **circarray)
+{
+    if (!circarray)
+        return 1;
+    std::ostringstream os;
+    for (int i = 0; circarray[i]; i++)
+        os << circarray[i] << "\n";
+    std::lock_guard<std::recursive_mutex> g(S.mu);
+    S.deck = os.str();
+    return 0;
+}
+
+IMPEXP char *ngSpice_CurPlot(void)
+{
+    std::lock_guard<std::recursive_mutex> g(S.mu);
+    static std::string name;
+    name = S.cur >= 0 ? S.plots[S.cur]->name : "const";
+    return (char *)name.c_str();
+}
+
+IMPEXP char **ngSpice_AllPlots(void)
+{
+    std::lock_guard<std::recursive_mutex> g(S.mu);
+    S.nameStore.clear();
+    for (auto it = S.plots.rbegin(); it != S.plots.rend(); ++it)
+        S.nameStore.push_back((*it)->name);
+    S.nameStore.push_back("const");
+    S.nameList.clear();
+    for (auto &s : S.nameStore)
+        S.nameList.push_back((char *)s.c_str());
+    S.nameList.push_back(nullptr);
+    return S.nameList.data();
+}
+
+IMPEXP char **ngSpice_AllVecs(char *plotname)
+{
+    std::lock_guard<std::recursive_mutex> g(S.mu);
+    S.nameStore.clear();
+    for (auto &p : S.plots)
+        if (plotname && p->name == plotname)
+            for (auto &v : p->vecs)
+                S.nameStore.push_back(v->name);
+    S.nameList.clear();
+    for (auto &s : S.nameStore)
+        S.nameList.push_back((char *)s.c_str());
+    S.nameList.push_back(nullptr);
+    return S.nameList.data();
+}
+
+IMPEXP NG_BOOL ngSpice_running(void) { return S.running; }
+
+IMPEXP NG_BOOL ngSpice_SetBkpt(double time)
+{
+    std::lock_guard<std::recursive_mutex> g(S.mu);
+    S.extraBreaks.push_back(time);
+    return false;   /* breakpoints set from the host are not forwarded to a run */
+}
+
+IMPEXP int ngSpice_nospinit(void) { return 0; }
+IMPEXP int ngSpice_nospiceinit(void) { return 0; }
+IMPEXP int ngSpice_LockRealloc(void)
+{
+    S.mu.lock();
+    return 0;
+}
+IMPEXP int ngSpice_UnlockRealloc(void)
+{
+    S.mu.unlock();
+    return 0;
+}
+IMPEXP int ngSpice_Reset(void)
+{
+    if (S.bg.joinable())
+        S.bg.join();
+    std::lock_guard<std::recursive_mutex> g(S.mu);
+    S.deck.clear();
+    S.plots.clear();
+    S.cur = -1;
+    return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,1902 @@
+/*
+ * GPU transient engine: the whole `.tran` of one circuit runs inside one
+ * thread block, with no host round trip between time points.
+ *
+ *   DCtran   (src/spicelib/analysis/dctran.c:67-971, XSPICE variant)
+ *     -> CKTop / NIiter  (src/maths/ni/niiter.c:29-367)
+ *          -> CKTload     per-device load functions writing stamp slots,
+ *                         then a deterministic gather into matrix / rhs
+ *          -> SMPluFac    left-looking LU refactor on the fixed pivots
+ *          -> SMPsolve    level-scheduled forward / backward substitution
+ *          -> NIconvTest  + device convergence tests (block reductions)
+ *     -> CKTtrunc / CKTterr   block min-reduction over all charges
+ *     -> CKTaccept / CKTsetBreak / CKTclrBreak   breakpoint table
+ *
+ * Control scalars (time, delta, order, mode, ...) live in shared memory;
+ * thread 0 updates them between __syncthreads().  Every loop over
+ * instances, equations or matrix entries is strided across the block.
+ * A batch of independent circuits is one launch with one block per circuit.
+ *
+ * All arithmetic is FP64.  Every spin or iteration is bounded: Newton loops
+ * by NIiter's iteration limit, the time loop by a step budget
+ * (NGSF_E_WATCHDOG), so a kernel always returns with a status word.
+ */
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
+#include "ngsf_types.h"
+
+#define NGSF_THREADS 256
+/* MIN / MAX exactly as the reference macros (src/include/ngspice/macros.h) */
+#define NG_MAX(a, b) ((a) > (b) ? (a) : (b))
+#define NG_MIN(a, b) ((a) < (b) ? (a) : (b))
+#define NGSF_WARPS (NGSF_THREADS / 32)
+
+namespace {
+
+struct Ctl {
+    double time, delta, olddelta, newdelta, saveDelta;
+    double deltaOld[7];
+    double ag[7];
+    double redd[NGSF_WARPS];
+    int redi[NGSF_WARPS];
+    int order, mode, firsttime, iterno, noncon, nbreaks;
+    int ring[4];
+    int rhsSel;            /* 0: rhs=A, rhsOld=B ; 1: swapped */
+    int status, accepted, rejected, numIter, tranIter, timePts, npoints, ncap;
+    int badpivot, opiter;
+    int flag;
+    /* resumable state: where the run stands when the kernel exits for a
+     * host re-pivot, and the loop locals it needs to continue */
+    int phase, shouldReorder, savedIter, savedNoncon, iters0, reorders;
+    long long steps;
+    double delta0;
+    /* CKTop fallbacks: gmin stepping and source stepping (cktop.c) */
+    int opPhase, gi, itersBefore;
+    double gmin, diagGmin, srcFact, factor, oldGmin, gtarget, startgmin, convFact, raise;
+};
+
+/* ---------------------------------------------------------------- */
+/* block reductions                                                  */
+/* ---------------------------------------------------------------- */
+__device__ int block_or(Ctl &s, int v)
+{
+    unsigned m = __ballot_sync(0xffffffffu, v != 0);
+    if ((threadIdx.x & 31) == 0)
+        s.redi[threadIdx.x >> 5] = m != 0;
+    __syncthreads();
+    int r = 0;
+    for (int w = 0; w < NGSF_WARPS; w++)
+        r |= s.redi[w];
+    __syncthreads();
+    return r;
+}
+
+__device__ double block_min(Ctl &s, double v)
+{
+    for (int o = 16; o > 0; o >>= 1)
+        v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0)
+        s.redd[threadIdx.x >> 5] = v;
+    __syncthreads();
+    double r = s.redd[0];
+    for (int w = 1; w < NGSF_WARPS; w++)
+        r = fmin(r, s.redd[w]);
+    __syncthreads();
+    return r;
+}
+
+/* AlmostEqualUlps (src/maths/misc/equality.c:27-63): two's-complement
+ * lexicographic distance in ulps. */
+__device__ bool almost_equal_ulps(double a, double b, int maxUlps)
+{
+    if (a == b)
+        return true;
+    long long ai = __double_as_longlong(a);
+    if (ai < 0)
+        ai = (long long)0x8000000000000000ULL - ai;
+    long long bi = __double_as_longlong(b);
+    if (bi < 0)
+        bi = (long long)0x8000000000000000ULL - bi;
+    long long d = ai - bi;
+    if (d < 0)
+        d = -d;
+    return d <= maxUlps;
+}
+
+/* ---------------------------------------------------------------- */
+/* device support (src/spicelib/devices/devsup.c)                   */
+/* ---------------------------------------------------------------- */
+__device__ double dev_limvds(double vnew, double vold)
+{
+    if (vold >= 3.5) {
+        if (vnew > vold)
+            vnew = NG_MIN(vnew, (3 * vold) + 2);
+        else if (vnew < 3.5)
+            vnew = NG_MAX(vnew, 2);
+    } else {
+        if (vnew > vold)
+            vnew = NG_MIN(vnew, 4);
+        else
+            vnew = NG_MAX(vnew, -.5);
+    }
+    return vnew;
+}
+
+__device__ double dev_pnjlim(double vnew, double vold, double vt, double vcrit, int *icheck)
+{
+    double arg;
+    if ((vnew > vcrit) && (fabs(vnew - vold) > (vt + vt))) {
+        if (vold > 0) {
+            arg = (vnew - vold) / vt;
+            if (arg > 0)
+                vnew = vold + vt * (2 + log(arg - 2));
+            else
+                vnew = vold - vt * (2 + log(2 - arg));
+        } else {
+            vnew = vt * log(vnew / vt);
+        }
+        *icheck = 1;
+    } else {
+        if (vnew < 0) {
+            if (vold > 0)
+                arg = -1 * vold - 1;
+            else
+                arg = 2 * vold - 1;
+            if (vnew < arg) {
+                vnew = arg;
+                *icheck = 1;
+            } else {
+                *icheck = 0;
+            }
+        } else {
+            *icheck = 0;
+        }
+    }
+    return vnew;
+}
+
+__device__ double dev_fetlim(double vnew, double vold, double vto)
+{
+    double vtsthi = fabs(2 * (vold - vto)) + 2;
+    double vtstlo = fabs(vold - vto) + 1;
+    double vtox = vto + 3.5;
+    double delv = vnew - vold;
+    if (vold >= vto) {
+        if (vold >= vtox) {
+            if (delv <= 0) {
+                if (vnew >= vtox) {
+                    if (-delv > vtstlo)
+                        vnew = vold - vtstlo;
+                } else {
+                    vnew = NG_MAX(vnew, vto + 2);
+                }
+            } else {
+                if (delv >= vtsthi)
+                    vnew = vold + vtsthi;
+            }
+        } else {
+            if (delv <= 0)
+                vnew = NG_MAX(vnew, vto - .5);
+            else
+                vnew = NG_MIN(vnew, vto + 4);
+        }
+    } else {
+        if (delv <= 0) {
+            if (-delv > vtsthi)
+                vnew = vold - vtsthi;
+        } else {
+            double vtemp = vto + .5;
+            if (vnew <= vtemp) {
+                if (delv > vtstlo)
+                    vnew = vold + vtstlo;
+            } else {
+                vnew = vtemp;
+            }
+        }
+    }
+    return vnew;
+}
+
+/* DEVqmeyer: Meyer gate capacitances (devsup.c:674-736) */
+__device__ void dev_qmeyer(double vgs, double vgd, double von, double vdsat,
+                           double *capgs, double *capgd, double *capgb,
+                           double phi, double cox)
+{
+    const double MAGIC_VDS = 0.025;
+    double vgst = vgs - von;
+    vdsat = NG_MAX(vdsat, MAGIC_VDS);
+    if (vgst <= -phi) {
+        *capgb = cox / 2;
+        *capgs = 0;
+        *capgd = 0;
+    } else if (vgst <= -phi / 2) {
+        *capgb = -vgst * cox / (2 * phi);
+        *capgs = 0;
+        *capgd = 0;
+    } else if (vgst <= 0) {
+        *capgb = -vgst * cox / (2 * phi);
+        *capgs = vgst * cox / (1.5 * phi) + cox / 3;
+        double vds = vgs - vgd;
+        if (vds >= vdsat) {
+            *capgd = 0;
+        } else {
+            double vddif = 2.0 * vdsat - vds;
+            double vddif1 = vdsat - vds;
+            double vddif2 = vddif * vddif;
+            *capgd = *capgs * (1.0 - vdsat * vdsat / vddif2);
+            *capgs = *capgs * (1.0 - vddif1 * vddif1 / vddif2);
+        }
+    } else {
+        double vds = vgs - vgd;
+        vdsat = NG_MAX(vdsat, MAGIC_VDS);
+        if (vdsat <= vds) {
+            *capgs = cox / 3;
+            *capgd = 0;
+            *capgb = 0;
+        } else {
+            double vddif = 2.0 * vdsat - vds;
+            double vddif1 = vdsat - vds;
+            double vddif2 = vddif * vddif;
+            *capgd = cox * (1.0 - vdsat * vdsat / vddif2) / 3;
+            *capgs = cox * (1.0 - vddif1 * vddif1 / vddif2) / 3;
+            *capgb = 0;
+        }
+    }
+}
+
+/* NIintegrate, trapezoidal (src/maths/ni/niinteg.c:18-80) */
+__device__ void ni_integrate(const Ctl &s, double *st0, const double *st1,
+                             double *geq, double *ceq, double cap, int qcap)
+{
+    int ccap = qcap + 1;
+    if (s.order == 1)
+        st0[ccap] = s.ag[0] * st0[qcap] + s.ag[1] * st1[qcap];
+    else
+        st0[ccap] = -st1[ccap] * s.ag[1] + s.ag[0] * (st0[qcap] - st1[qcap]);
+    *ceq = st0[ccap] - s.ag[0] * st0[qcap];
+    *geq = s.ag[0] * cap;
+}
+
+/* ---------------------------------------------------------------- */
+/* per-iteration context                                             */
+/* ---------------------------------------------------------------- */
+struct Iter {
+    double *st0, *st1, *st2, *st3;
+    double *rhs, *rhsOld;
+};
+
+__device__ Iter iter_ctx(const ngsf_ckt_t &C, const Ctl &s)
+{
+    Iter it;
+    it.st0 = C.states + (size_t)s.ring[0] * C.nstates;
+    it.st1 = C.states + (size_t)s.ring[1] * C.nstates;
+    it.st2 = C.states + (size_t)s.ring[2] * C.nstates;
+    it.st3 = C.states + (size_t)s.ring[3] * C.nstates;
+    it.rhs = s.rhsSel ? C.rhsOld : C.rhs;
+    it.rhsOld = s.rhsSel ? C.rhs : C.rhsOld;
+    return it;
+}
+
+/* ---------------------------------------------------------------- */
+/* independent source value at the current time (VSRCload/ISRCload)   */
+/* ---------------------------------------------------------------- */
+__device__ double src_value(const ngsf_src_t &S, int i, const Ctl &s, const ngsf_opts_t &o)
+{
+    int mode = s.mode;
+    if ((mode & (NGSF_MODEDCOP | NGSF_MODEDCTRANCURVE)) && S.dcgiven[i])
+        return S.dc[i];
+    double time = (mode & NGSF_MODEDC) ? 0.0 : s.time;
+    const double *cf = S.coef + (size_t)i * NGSF_MAX_COEFFS;
+    int nc = S.ncoef[i];
+    double value = 0.0;
+    switch (S.kind[i]) {
+    default:
+        value = S.dc[i];
+        break;
+    case WF_PULSE: {
+        double V1 = cf[0], V2 = cf[1];
+        double TD = nc > 2 ? cf[2] : 0.0;
+        double TR = nc > 3 && cf[3] > 0.0 ? cf[3] : o.tstep;
+        double TF = nc > 4 && cf[4] > 0.0 ? cf[4] : o.tstep;
+        double PW = nc > 5 && cf[5] >= 0.0 ? cf[5] : 0.0;
+        double PER = nc > 6 && cf[6] > 0.0 ? cf[6] : TR + TF + PW;
+        double PHASE = nc > 7 ? cf[7] : 0.0;
+        double tmax = 1e99;
+        time -= TD;
+        if (PHASE > 0.0)
+            tmax = PHASE * PER;
+        if (time > tmax) {
+            value = V1;
+        } else {
+            if (time > PER) {
+                double basetime = PER * floor(time / PER);
+                time -= basetime;
+            }
+            if (time <= 0 || time >= TR + PW + TF)
+                value = V1;
+            else if (time >= TR && time <= TR + PW)
+                value = V2;
+            else if (time > 0 && time < TR)
+                value = V1 + (V2 - V1) * (time) / TR;
+            else
+                value = V2 + (V1 - V2) * (time - (TR + PW)) / TF;
+        }
+        break;
+    }
+    case WF_SINE: {
+        double PHASE = nc > 5 ? cf[5] : 0.0;
+        double phase = PHASE * M_PI / 180.0;
+        double VO = cf[0], VA = cf[1];
+        double FREQ = nc > 2 && cf[2] != 0.0 ? cf[2] : (1 / o.tstop);
+        double TD = nc > 3 ? cf[3] : 0.0;
+        double THETA = nc > 4 ? cf[4] : 0.0;
+        time -= TD;
+        if (time <= 0)
+            value = VO + VA * sin(phase);
+        else
+            value = VO + VA * sin(FREQ * time * 2.0 * M_PI + phase) * exp(-time * THETA);
+        break;
+    }
+    case WF_PWL: {
+        if (time <= cf[0]) {
+            value = cf[1];
+            break;
+        }
+        double end_time = cf[nc - 2];
+        if (time > end_time) {
+            value = cf[nc - 1];
+            break;
+        }
+        for (int k = 2; k < nc; k += 2) {
+            double itime = cf[k];
+            if (itime >= time) {
+                time -= cf[k - 2];
+                time /= cf[k] - cf[k - 2];
+                value = cf[k - 1];
+                value += time * (cf[k + 1] - cf[k - 1]);
+                break;
+            }
+        }
+        break;
+    }
+    }
+    return value;
+}
+
+/* ---------------------------------------------------------------- */
+/* device loads                                                      */
+/* ---------------------------------------------------------------- */
+/* CAPload (src/spicelib/devices/cap/capload.c:15-87) */
+__device__ void cap_load(const ngsf_ckt_t &C, const Ctl &s, const Iter &it)
+{
+    const ngsf_cap_t &K = C.cap;
+    int n = K.n, mode = s.mode;
+    if (!(mode & (NGSF_MODETRAN | NGSF_MODETRANOP))) {
+        for (int i = threadIdx.x; i < n; i += blockDim.x)
+            for (int k = 0; k < 6; k++)
+                C.stampv[K.stamp0 + k * n + i] = 0.0;
+        return;
+    }
+    bool cond1 = ((mode & NGSF_MODEDC) && (mode & NGSF_MODEINITJCT)) ||
+                 ((mode & NGSF_MODEUIC) && (mode & NGSF_MODEINITTRAN));
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        int p = K.node[i], q = K.node[n + i], st = K.st[i];
+        double m = K.m[i], cap = K.c[i];
+        double vcap = cond1 ? K.ic[i] : it.rhsOld[p] - it.rhsOld[q];
+        double g = 0.0, ceqv = 0.0;
+        double *sv = C.stampv + K.stamp0 + i;
+        if (mode & NGSF_MODETRAN) {
+            if (mode & NGSF_MODEINITPRED) {
+                it.st0[st] = it.st1[st];
+            } else {
+                it.st0[st] = cap * vcap;
+                if (mode & NGSF_MODEINITTRAN)
+                    it.st1[st] = it.st0[st];
+            }
+            double geq, ceq;
+            ni_integrate(s, it.st0, it.st1, &geq, &ceq, cap, st);
+            if (mode & NGSF_MODEINITTRAN)
+                it.st1[st + 1] = it.st0[st + 1];
+            g = m * geq;
+            ceqv = m * ceq;
+            sv[0] = g;
+            sv[n] = g;
+            sv[2 * n] = -g;
+            sv[3 * n] = -g;
+            sv[4 * n] = -ceqv;
+            sv[5 * n] = ceqv;
+        } else {
+            it.st0[st] = cap * vcap;
+            for (int k = 0; k < 6; k++)
+                sv[k * n] = 0.0;
+        }
+    }
+}
+
+/* RESload (src/spicelib/devices/res/resload.c:15-40) */
+__device__ void res_load(const ngsf_ckt_t &C)
+{
+    const ngsf_res_t &K = C.res;
+    int n = K.n;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        double g = K.g[i];
+        double *sv = C.stampv + K.stamp0 + i;
+        sv[0] = g;
+        sv[n] = g;
+        sv[2 * n] = -g;
+        sv[3 * n] = -g;
+    }
+}
+
+/* VSRCload / ISRCload (vsrc/vsrcload.c, isrc/isrcload.c) */
+__device__ void src_load(const ngsf_ckt_t &C, const Ctl &s)
+{
+    {
+        const ngsf_src_t &K = C.vsrc;
+        int n = K.n;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            double *sv = C.stampv + K.stamp0 + i;
+            sv[0] = 1.0;
+            sv[n] = -1.0;
+            sv[2 * n] = 1.0;
+            sv[3 * n] = -1.0;
+            double value = src_value(K, i, s, C.opt);
+            if (s.mode & NGSF_MODETRANOP)
+                value *= s.srcFact;
+            sv[4 * n] = value;
+        }
+    }
+    {
+        const ngsf_src_t &K = C.isrc;
+        int n = K.n;
+        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+            double *sv = C.stampv + K.stamp0 + i;
+            double value = src_value(K, i, s, C.opt);
+            if (s.mode & NGSF_MODETRANOP)
+                value *= s.srcFact;
+            double m = K.m[i];
+            sv[0] = m * value;
+            sv[n] = -(m * value);
+        }
+    }
+}
+
+/* MOS1load (src/spicelib/devices/mos1/mos1load.c:17-941), default build:
+ * no sensitivity, bypass option 0, PREDICTOR undefined. */
+__device__ int mos1_load_one(const ngsf_ckt_t &C, const Ctl &s, const Iter &it, int i)
+{
+    const ngsf_mos1_t &K = C.mos1;
+    const int n = K.n;
+    const double *P = K.p;
+    double *H = K.h;
+#define MP(f) P[(size_t)(f) * n + i]
+#define MH(f) H[(size_t)(f) * n + i]
+    const int mode = s.mode;
+    const int dN = K.node[M1N_D * n + i], gN = K.node[M1N_G * n + i];
+    const int bN = K.node[M1N_B * n + i];
+    const int dpN = K.node[M1N_DP * n + i], spN = K.node[M1N_SP * n + i];
+    (void)dN;
+    double *st0 = it.st0 + K.st[i];
+    const double *st1 = it.st1 + K.st[i];
+    const double *st2 = it.st2 + K.st[i];
+    const double type = MP(M1P_TYPE);
+    const double vt = MP(M1P_VT);
+    const double DrainSatCur = MP(M1P_DSAT), SourceSatCur = MP(M1P_SSAT);
+    const double GateSourceOverlapCap = MP(M1P_CGSO);
+    const double GateDrainOverlapCap = MP(M1P_CGDO);
+    const double GateBulkOverlapCap = MP(M1P_CGBO);
+    const double Beta = MP(M1P_BETA), OxideCap = MP(M1P_COX);
+    const double gmin = s.gmin;
+    const int off = MP(M1P_OFF) != 0.0;
+    int Check = 1;
+    double xfact = 0.0;
+    double vbs, vgs, vds, vbd, vgd, vgb;
+
+    if ((mode & (NGSF_MODEINITFLOAT | NGSF_MODEINITPRED | NGSF_MODEINITSMSIG |
+                 NGSF_MODEINITTRAN)) ||
+        ((mode & NGSF_MODEINITFIX) && !off)) {
+        if (mode & (NGSF_MODEINITPRED | NGSF_MODEINITTRAN)) {
+            xfact = s.delta / s.deltaOld[1];
+            st0[M1S_VBS] = st1[M1S_VBS];
+            vbs = (1 + xfact) * (st1[M1S_VBS]) - (xfact * (st2[M1S_VBS]));
+            st0[M1S_VGS] = st1[M1S_VGS];
+            vgs = (1 + xfact) * (st1[M1S_VGS]) - (xfact * (st2[M1S_VGS]));
+            st0[M1S_VDS] = st1[M1S_VDS];
+            vds = (1 + xfact) * (st1[M1S_VDS]) - (xfact * (st2[M1S_VDS]));
+            st0[M1S_VBD] = st0[M1S_VBS] - st0[M1S_VDS];
+        } else {
+            vbs = type * (it.rhsOld[bN] - it.rhsOld[spN]);
+            vgs = type * (it.rhsOld[gN] - it.rhsOld[spN]);
+            vds = type * (it.rhsOld[dpN] - it.rhsOld[spN]);
+        }
+        vbd = vbs - vds;
+        vgd = vgs - vds;
+        double vgdo = st0[M1S_VGS] - st0[M1S_VDS];
+        double von = type * MH(M1H_VON);
+        if (st0[M1S_VDS] >= 0) {
+            vgs = dev_fetlim(vgs, st0[M1S_VGS], von);
+            vds = vgs - vgd;
+            vds = dev_limvds(vds, st0[M1S_VDS]);
+            vgd = vgs - vds;
+        } else {
+            vgd = dev_fetlim(vgd, vgdo, von);
+            vds = vgs - vgd;
+            vds = -dev_limvds(-vds, -(st0[M1S_VDS]));
+            vgs = vgd + vds;
+        }
+        if (vds >= 0) {
+            vbs = dev_pnjlim(vbs, st0[M1S_VBS], vt, MP(M1P_SVCRIT), &Check);
+            vbd = vbs - vds;
+        } else {
+            vbd = dev_pnjlim(vbd, st0[M1S_VBD], vt, MP(M1P_DVCRIT), &Check);
+            vbs = vbd + vds;
+        }
+    } else {
+        if ((mode & NGSF_MODEINITJCT) && !off) {
+            vds = type * MP(M1P_ICVDS);
+            vgs = type * MP(M1P_ICVGS);
+            vbs = type * MP(M1P_ICVBS);
+            if ((vds == 0) && (vgs == 0) && (vbs == 0) &&
+                ((mode & (NGSF_MODETRAN | NGSF_MODEDCOP | NGSF_MODEDCTRANCURVE)) ||
+                 (!(mode & NGSF_MODEUIC)))) {
+                vbs = -1;
+                vgs = type * MP(M1P_TVTO);
+                vds = 0;
+            }
+        } else {
+            vbs = vgs = vds = 0;
+        }
+    }
+    vbd = vbs - vds;
+    vgd = vgs - vds;
+    vgb = vgs - vbs;
+
+    double gbs, cbs, gbd, cbd;
+    if (vbs <= -3 * vt) {
+        gbs = gmin;
+        cbs = gbs * vbs - SourceSatCur;
+    } else {
+        double evbs = exp(NG_MIN(709.0, vbs / vt));
+        gbs = SourceSatCur * evbs / vt + gmin;
+        cbs = SourceSatCur * (evbs - 1) + gmin * vbs;
+    }
+    if (vbd <= -3 * vt) {
+        gbd = gmin;
+        cbd = gbd * vbd - DrainSatCur;
+    } else {
+        double evbd = exp(NG_MIN(709.0, vbd / vt));
+        gbd = DrainSatCur * evbd / vt + gmin;
+        cbd = DrainSatCur * (evbd - 1) + gmin * vbd;
+    }
+    int dmode = vds >= 0 ? 1 : -1;
+
+    double cdrain, gm, gds, gmbs, von, vdsat;
+    {
+        double arg, betap, sarg, vgst;
+        double vbx = dmode == 1 ? vbs : vbd;
+        const double tPhi = MP(M1P_TPHI), gamma = MP(M1P_GAMMA);
+        const double lambda = MP(M1P_LAMBDA);
+        if (vbx <= 0) {
+            sarg = sqrt(tPhi - vbx);
+        } else {
+            sarg = sqrt(tPhi);
+            sarg = sarg - vbx / (sarg + sarg);
+            sarg = NG_MAX(0.0, sarg);
+        }
+        von = (MP(M1P_TVBI) * type) + gamma * sarg;
+        vgst = (dmode == 1 ? vgs : vgd) - von;
+        vdsat = NG_MAX(vgst, 0.0);
+        if (sarg <= 0)
+            arg = 0;
+        else
+            arg = gamma / (sarg + sarg);
+        if (vgst <= 0) {
+            cdrain = 0;
+            gm = 0;
+            gds = 0;
+            gmbs = 0;
+        } else {
+            betap = Beta * (1 + lambda * (vds * dmode));
+            if (vgst <= (vds * dmode)) {
+                cdrain = betap * vgst * vgst * .5;
+                gm = betap * vgst;
+                gds = lambda * Beta * vgst * vgst * .5;
+                gmbs = gm * arg;
+            } else {
+                cdrain = betap * (vds * dmode) * (vgst - .5 * (vds * dmode));
+                gm = betap * (vds * dmode);
+                gds = betap * (vgst - (vds * dmode)) +
+                      lambda * Beta * (vds * dmode) * (vgst - .5 * (vds * dmode));
+                gmbs = gm * arg;
+            }
+        }
+    }
+    MH(M1H_VON) = type * von;
+    MH(M1H_VDSAT) = type * vdsat;
+    double cd = dmode * cdrain - cbd;
+    double capbs = MH(M1H_CAPBS), capbd = MH(M1H_CAPBD);
+
+    if (mode & (NGSF_MODETRAN | NGSF_MODETRANOP | NGSF_MODEINITSMSIG)) {
+        const double Cbs = MP(M1P_CBS), Cbssw = MP(M1P_CBSSW);
+        const double Cbd = MP(M1P_CBD), Cbdsw = MP(M1P_CBDSW);
+        const double tDepCap = MP(M1P_TDEPCAP), tBulkPot = MP(M1P_TBULKPOT);
+        const double mj = MP(M1P_MJ), mjsw = MP(M1P_MJSW);
+        if (Cbs != 0 || Cbssw != 0) {
+            if (vbs < tDepCap) {
+                const double arg = 1 - vbs / tBulkPot;
+                double sarg, sargsw;
+                if (mj == mjsw) {
+                    if (mj == .5)
+                        sarg = sargsw = 1 / sqrt(arg);
+                    else
+                        sarg = sargsw = exp(-mj * log(arg));
+                } else {
+                    if (mj == .5)
+                        sarg = 1 / sqrt(arg);
+                    else
+                        sarg = exp(-mj * log(arg));
+                    if (mjsw == .5)
+                        sargsw = 1 / sqrt(arg);
+                    else
+                        sargsw = exp(-mjsw * log(arg));
+                }
+                st0[M1S_QBS] = tBulkPot * (Cbs * (1 - arg * sarg) / (1 - mj) +
+                                           Cbssw * (1 - arg * sargsw) / (1 - mjsw));
+                capbs = Cbs * sarg + Cbssw * sargsw;
+            } else {
+                st0[M1S_QBS] = MP(M1P_F4S) + vbs * (MP(M1P_F2S) + vbs * (MP(M1P_F3S) / 2));
+                capbs = MP(M1P_F2S) + MP(M1P_F3S) * vbs;
+            }
+        } else {
+            st0[M1S_QBS] = 0;
+            capbs = 0;
+        }
+        if (Cbd != 0 || Cbdsw != 0) {
+            if (vbd < tDepCap) {
+                const double arg = 1 - vbd / tBulkPot;
+                double sarg, sargsw;
+                if (mj == .5 && mjsw == .5) {
+                    sarg = sargsw = 1 / sqrt(arg);
+                } else {
+                    if (mj == .5)
+                        sarg = 1 / sqrt(arg);
+                    else
+                        sarg = exp(-mj * log(arg));
+                    if (mjsw == .5)
+                        sargsw = 1 / sqrt(arg);
+                    else
+                        sargsw = exp(-mjsw * log(arg));
+                }
+                st0[M1S_QBD] = tBulkPot * (Cbd * (1 - arg * sarg) / (1 - mj) +
+                                           Cbdsw * (1 - arg * sargsw) / (1 - mjsw));
+                capbd = Cbd * sarg + Cbdsw * sargsw;
+            } else {
+                st0[M1S_QBD] = MP(M1P_F4D) + vbd * (MP(M1P_F2D) + vbd * MP(M1P_F3D) / 2);
+                capbd = MP(M1P_F2D) + vbd * MP(M1P_F3D);
+            }
+        } else {
+            st0[M1S_QBD] = 0;
+            capbd = 0;
+        }
+        if ((mode & NGSF_MODETRAN) ||
+            ((mode & NGSF_MODEINITTRAN) && !(mode & NGSF_MODEUIC))) {
+            double geq, ceq;
+            ni_integrate(s, st0, st1, &geq, &ceq, capbd, M1S_QBD);
+            gbd += geq;
+            cbd += st0[M1S_CQBD];
+            cd -= st0[M1S_CQBD];
+            ni_integrate(s, st0, st1, &geq, &ceq, capbs, M1S_QBS);
+            gbs += geq;
+            cbs += st0[M1S_CQBS];
+        }
+    }
+    MH(M1H_CAPBS) = capbs;
+    MH(M1H_CAPBD) = capbd;
+
+    int noncon = 0;
+    if (!off || !(mode & (NGSF_MODEINITFIX | NGSF_MODEINITSMSIG)))
+        if (Check == 1)
+            noncon = 1;
+
+    st0[M1S_VBS] = vbs;
+    st0[M1S_VBD] = vbd;
+    st0[M1S_VGS] = vgs;
+    st0[M1S_VDS] = vds;
+
+    double capgs = 0, capgd = 0, capgb = 0;
+    if (mode & (NGSF_MODETRAN | NGSF_MODETRANOP | NGSF_MODEINITSMSIG)) {
+        const double tPhi = MP(M1P_TPHI);
+        if (dmode > 0)
+            dev_qmeyer(vgs, vgd, von, vdsat, &st0[M1S_CAPGS], &st0[M1S_CAPGD],
+                       &st0[M1S_CAPGB], tPhi, OxideCap);
+        else
+            dev_qmeyer(vgd, vgs, von, vdsat, &st0[M1S_CAPGD], &st0[M1S_CAPGS],
+                       &st0[M1S_CAPGB], tPhi, OxideCap);
+        double vgs1 = st1[M1S_VGS];
+        double vgd1 = vgs1 - st1[M1S_VDS];
+        double vgb1 = vgs1 - st1[M1S_VBS];
+        if (mode & (NGSF_MODETRANOP | NGSF_MODEINITSMSIG)) {
+            capgs = 2 * st0[M1S_CAPGS] + GateSourceOverlapCap;
+            capgd = 2 * st0[M1S_CAPGD] + GateDrainOverlapCap;
+            capgb = 2 * st0[M1S_CAPGB] + GateBulkOverlapCap;
+        } else {
+            capgs = (st0[M1S_CAPGS] + st1[M1S_CAPGS] + GateSourceOverlapCap);
+            capgd = (st0[M1S_CAPGD] + st1[M1S_CAPGD] + GateDrainOverlapCap);
+            capgb = (st0[M1S_CAPGB] + st1[M1S_CAPGB] + GateBulkOverlapCap);
+        }
+        if (mode & (NGSF_MODEINITPRED | NGSF_MODEINITTRAN)) {
+            st0[M1S_QGS] = (1 + xfact) * st1[M1S_QGS] - xfact * st2[M1S_QGS];
+            st0[M1S_QGD] = (1 + xfact) * st1[M1S_QGD] - xfact * st2[M1S_QGD];
+            st0[M1S_QGB] = (1 + xfact) * st1[M1S_QGB] - xfact * st2[M1S_QGB];
+        } else {
+            if (mode & NGSF_MODETRAN) {
+                st0[M1S_QGS] = (vgs - vgs1) * capgs + st1[M1S_QGS];
+                st0[M1S_QGD] = (vgd - vgd1) * capgd + st1[M1S_QGD];
+                st0[M1S_QGB] = (vgb - vgb1) * capgb + st1[M1S_QGB];
+            } else {
+                st0[M1S_QGS] = vgs * capgs;
+                st0[M1S_QGD] = vgd * capgd;
+                st0[M1S_QGB] = vgb * capgb;
+            }
+        }
+    }
+
+    double gcgs, ceqgs, gcgd, ceqgd, gcgb, ceqgb;
+    if ((mode & NGSF_MODEINITTRAN) || !(mode & NGSF_MODETRAN)) {
+        gcgs = ceqgs = gcgd = ceqgd = gcgb = ceqgb = 0;
+    } else {
+        if (capgs == 0)
+            st0[M1S_CQGS] = 0;
+        if (capgd == 0)
+            st0[M1S_CQGD] = 0;
+        if (capgb == 0)
+            st0[M1S_CQGB] = 0;
+        ni_integrate(s, st0, st1, &gcgs, &ceqgs, capgs, M1S_QGS);
+        ni_integrate(s, st0, st1, &gcgd, &ceqgd, capgd, M1S_QGD);
+        ni_integrate(s, st0, st1, &gcgb, &ceqgb, capgb, M1S_QGB);
+        ceqgs = ceqgs - gcgs * vgs + s.ag[0] * st0[M1S_QGS];
+        ceqgd = ceqgd - gcgd * vgd + s.ag[0] * st0[M1S_QGD];
+        ceqgb = ceqgb - gcgb * vgb + s.ag[0] * st0[M1S_QGB];
+    }
+
+    double ceqbs = type * (cbs - (gbs)*vbs);
+    double ceqbd = type * (cbd - (gbd)*vbd);
+    double xnrm, xrev, cdreq;
+    if (dmode >= 0) {
+        xnrm = 1;
+        xrev = 0;
+        cdreq = type * (cdrain - gds * vds - gm * vgs - gmbs * vbs);
+    } else {
+        xnrm = 0;
+        xrev = 1;
+        cdreq = -(type) * (cdrain - gds * (-vds) - gm * vgd - gmbs * vbd);
+    }
+    const double gdrain = MP(M1P_GDRAIN), gsource = MP(M1P_GSOURCE);
+    double *sv = C.stampv + K.stamp0 + i;
+    sv[0 * n] = gdrain;
+    sv[1 * n] = (gcgd + gcgs + gcgb);
+    sv[2 * n] = gsource;
+    sv[3 * n] = (gbd + gbs + gcgb);
+    sv[4 * n] = (gdrain + gds + gbd + xrev * (gm + gmbs) + gcgd);
+    sv[5 * n] = (gsource + gds + gbs + xnrm * (gm + gmbs) + gcgs);
+    sv[6 * n] = (-gdrain);
+    sv[7 * n] = -gcgb;
+    sv[8 * n] = -gcgd;
+    sv[9 * n] = -gcgs;
+    sv[10 * n] = (-gsource);
+    sv[11 * n] = -gcgb;
+    sv[12 * n] = -gbd;
+    sv[13 * n] = -gbs;
+    sv[14 * n] = (-gdrain);
+    sv[15 * n] = ((xnrm - xrev) * gm - gcgd);
+    sv[16 * n] = (-gbd + (xnrm - xrev) * gmbs);
+    sv[17 * n] = (-gds - xnrm * (gm + gmbs));
+    sv[18 * n] = (-(xnrm - xrev) * gm - gcgs);
+    sv[19 * n] = (-gsource);
+    sv[20 * n] = (-gbs - (xnrm - xrev) * gmbs);
+    sv[21 * n] = (-gds - xrev * (gm + gmbs));
+    sv[22 * n] = -(type * (ceqgs + ceqgb + ceqgd));
+    sv[23 * n] = -(ceqbs + ceqbd - type * ceqgb);
+    sv[24 * n] = (ceqbd - cdreq + type * ceqgd);
+    sv[25 * n] = cdreq + ceqbs + type * ceqgs;
+
+    MH(M1H_MODE) = dmode;
+    MH(M1H_CD) = cd;
+    MH(M1H_CBS) = cbs;
+    MH(M1H_CBD) = cbd;
+    MH(M1H_GBS) = gbs;
+    MH(M1H_GBD) = gbd;
+    MH(M1H_GM) = gm;
+    MH(M1H_GDS) = gds;
+    MH(M1H_GMBS) = gmbs;
+#undef MP
+#undef MH
+    return noncon;
+}
+
+/* MOS1convTest (src/spicelib/devices/mos1/mos1conv.c:13-99) */
+__device__ int mos1_conv_one(const ngsf_ckt_t &C, const Iter &it, int i)
+{
+    const ngsf_mos1_t &K = C.mos1;
+    const int n = K.n;
+    const double *P = K.p;
+    const double *H = K.h;
+    const double type = P[(size_t)M1P_TYPE * n + i];
+    const int gN = K.node[M1N_G * n + i], bN = K.node[M1N_B * n + i];
+    const int dpN = K.node[M1N_DP * n + i], spN = K.node[M1N_SP * n + i];
+    const double *st0 = it.st0 + K.st[i];
+    double vbs = type * (it.rhs[bN] - it.rhs[spN]);
+    double vgs = type * (it.rhs[gN] - it.rhs[spN]);
+    double vds = type * (it.rhs[dpN] - it.rhs[spN]);
+    double vbd = vbs - vds;
+    double vgd = vgs - vds;
+    double vgdo = st0[M1S_VGS] - st0[M1S_VDS];
+    double delvbs = vbs - st0[M1S_VBS];
+    double delvbd = vbd - st0[M1S_VBD];
+    double delvgs = vgs - st0[M1S_VGS];
+    double delvds = vds - st0[M1S_VDS];
+    double delvgd = vgd - vgdo;
+#define MH(f) H[(size_t)(f) * n + i]
+    double cdhat, cbhat;
+    if (MH(M1H_MODE) >= 0)
+        cdhat = MH(M1H_CD) - MH(M1H_GBD) * delvbd + MH(M1H_GMBS) * delvbs +
+                MH(M1H_GM) * delvgs + MH(M1H_GDS) * delvds;
+    else
+        cdhat = MH(M1H_CD) - (MH(M1H_GBD) - MH(M1H_GMBS)) * delvbd -
+                MH(M1H_GM) * delvgd + MH(M1H_GDS) * delvds;
+    cbhat = MH(M1H_CBS) + MH(M1H_CBD) + MH(M1H_GBD) * delvbd + MH(M1H_GBS) * delvbs;
+    double tol = C.opt.reltol * NG_MAX(fabs(cdhat), fabs(MH(M1H_CD))) + C.opt.abstol;
+    if (fabs(cdhat - MH(M1H_CD)) >= tol)
+        return 1;
+    tol = C.opt.reltol * NG_MAX(fabs(cbhat), fabs(MH(M1H_CBS) + MH(M1H_CBD))) + C.opt.abstol;
+    if (fabs(cbhat - (MH(M1H_CBS) + MH(M1H_CBD))) > tol)
+        return 1;
+#undef MH
+    return 0;
+}
+
+/* CKTload: zero, device loads, gather into matrix and rhs. */
+__device__ int ckt_load(const ngsf_ckt_t &C, Ctl &s, const Iter &it)
+{
+    int nc = 0;
+    cap_load(C, s, it);
+    for (int i = threadIdx.x; i < C.mos1.n; i += blockDim.x)
+        nc |= mos1_load_one(C, s, it, i);
+    res_load(C);
+    src_load(C, s);
+    nc = block_or(s, nc);   /* includes __syncthreads: stamps visible */
+    for (int p = threadIdx.x; p < C.nnz; p += blockDim.x) {
+        double acc = 0.0;
+        for (int q = C.gptr[p]; q < C.gptr[p + 1]; q++)
+            acc += C.stampv[C.gsrc[q]];
+        C.ax[p] = acc;
+    }
+    for (int r = threadIdx.x; r <= C.n; r += blockDim.x) {
+        double acc = 0.0;
+        for (int q = C.rptr[r]; q < C.rptr[r + 1]; q++)
+            acc += C.stampv[C.rsrc[q]];
+        it.rhs[r] = acc;
+    }
+    __syncthreads();
+    return nc;
+}
+
+/* SMPluFac: left-looking refactorization on the fixed pivot sequence.
+ * One warp per column; columns of one level are independent.
+ * Returns 1 when a pivot is zero or not finite, or when the pivot has lost
+ * so much ground to its column that |L(i,k)| > NGSF_GROWTH: the host then
+ * chooses new pivots from this matrix (the reference re-factors with
+ * pivoting when refactoring fails, src/maths/ni/niiter.c:161-195). */
+#define NGSF_GROWTH 1e6
+__device__ int lu_factor(const ngsf_ckt_t &C, Ctl &s)
+{
+    for (int q = threadIdx.x; q < C.nlu; q += blockDim.x)
+        C.lux[q] = 0.0;
+    __syncthreads();
+    for (int p = threadIdx.x; p < C.nnz; p += blockDim.x)
+        C.lux[C.a_lupos[p]] = C.ax[p];
+    __syncthreads();
+    if (s.diagGmin != 0.0) {
+        /* LoadGmin: gmin on every structural diagonal (klusmp.c:587-589) */
+        for (int j = threadIdx.x; j < C.n; j += blockDim.x)
+            if (C.a_diag[j] >= 0)
+                C.lux[C.a_lupos[C.a_diag[j]]] += s.diagGmin;
+        __syncthreads();
+    }
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    int bad = 0;
+    for (int l = 0; l < C.nlevels; l++) {
+        for (int c = C.lvl_ptr[l] + warp; c < C.lvl_ptr[l + 1]; c += NGSF_WARPS) {
+            int k = C.lvl_col[c];
+            for (int t = C.kptr[k]; t < C.kptr[k + 1]; t++) {
+                double xk = C.lux[C.kpos[t]];
+                for (int u = C.kseg[t] + lane; u < C.kseg[t + 1]; u += 32)
+                    C.lux[C.upd_dst[u]] -= C.lux[C.upd_src[u]] * xk;
+                __syncwarp();
+            }
+            double piv = C.lux[C.cdiag[k]];
+            if (!(fabs(piv) > 0.0) || !isfinite(piv))
+                bad = 1;
+            for (int q = C.cdiag[k] + 1 + lane; q < C.cend[k]; q += 32) {
+                double l_ik = C.lux[q] / piv;
+                C.lux[q] = l_ik;
+                if (!(fabs(l_ik) <= NGSF_GROWTH))
+                    bad = 1;
+            }
+            __syncwarp();
+        }
+        __syncthreads();
+    }
+    return block_or(s, bad);
+}
+
+/* SMPsolve: x = A^-1 b, in place on rhs (row-oriented, level scheduled). */
+__device__ void lu_solve(const ngsf_ckt_t &C, Ctl &s, double *rhs)
+{
+    double *w = C.work;
+    for (int k = threadIdx.x; k < C.n; k += blockDim.x)
+        w[k] = rhs[C.prow[k]];
+    __syncthreads();
+    for (int l = 0; l < C.nflevels; l++) {
+        for (int r = C.fl_ptr[l] + threadIdx.x; r < C.fl_ptr[l + 1]; r += blockDim.x) {
+            int k = C.fl_row[r];
+            double acc = w[k];
+            for (int q = C.lr_ptr[k]; q < C.lr_ptr[k + 1]; q++)
+                acc -= C.lux[C.lr_pos[q]] * w[C.lr_col[q]];
+            w[k] = acc;
+        }
+        __syncthreads();
+    }
+    for (int l = 0; l < C.nblevels; l++) {
+        for (int r = C.bl_ptr[l] + threadIdx.x; r < C.bl_ptr[l + 1]; r += blockDim.x) {
+            int k = C.bl_row[r];
+            double acc = w[k];
+            for (int q = C.ur_ptr[k]; q < C.ur_ptr[k + 1]; q++)
+                acc -= C.lux[C.ur_pos[q]] * w[C.ur_col[q]];
+            w[k] = acc / C.lux[C.cdiag[k]];
+        }
+        __syncthreads();
+    }
+    for (int k = threadIdx.x; k < C.n; k += blockDim.x)
+        rhs[C.pcol[k]] = w[k];
+    __syncthreads();
+}
+
+/* NIconvTest (src/maths/ni/niconv.c:21-90).
+ * The reference then calls CKTconvTest (cktop.c:126-145), which runs the
+ * device current tests (MOS1convTest, ...) but returns their *error code*,
+ * always OK; the CKTnoncon those tests increment is overwritten when NIiter
+ * stores NIconvTest's return value (niiter.c:286-289).  The device tests
+ * therefore never change a Newton decision, and the engine does not spend
+ * FP64 work on them (mos1_conv_one stays available for diagnostics). */
+__device__ int conv_test(const ngsf_ckt_t &C, Ctl &s, const Iter &it)
+{
+    int bad = 0;
+    for (int i = 1 + threadIdx.x; i <= C.n; i += blockDim.x) {
+        double nw = it.rhs[i], od = it.rhsOld[i];
+        if (isnan(nw)) {
+            bad = 1;
+            break;
+        }
+        double tol = C.opt.reltol * NG_MAX(fabs(od), fabs(nw)) +
+                     (C.ntype[i] ? C.opt.vntol : C.opt.abstol);
+        if (fabs(nw - od) > tol) {
+            bad = 1;
+            break;
+        }
+    }
+    return block_or(s, bad);
+}
+
+/* CKTterr (src/spicelib/analysis/cktterr.c:13-79), trapezoidal */
+__device__ double ckt_terr(const ngsf_ckt_t &C, const Ctl &s, int qcap, double timeStep)
+{
+    const ngsf_opts_t &o = C.opt;
+    const double *st0 = C.states + (size_t)s.ring[0] * C.nstates;
+    const double *st1 = C.states + (size_t)s.ring[1] * C.nstates;
+    int ccap = qcap + 1;
+    double volttol = o.abstol + o.reltol * NG_MAX(fabs(st0[ccap]), fabs(st1[ccap]));
+    double chargetol = NG_MAX(fabs(st0[qcap]), fabs(st1[qcap]));
+    chargetol = o.reltol * NG_MAX(chargetol, o.chgtol) / s.delta;
+    double tol = NG_MAX(volttol, chargetol);
+    double diff[8], deltmp[8];
+    for (int i = s.order + 1; i >= 0; i--)
+        diff[i] = C.states[(size_t)s.ring[i] * C.nstates + qcap];
+    for (int i = 0; i <= s.order; i++)
+        deltmp[i] = s.deltaOld[i];
+    int j = s.order;
+    for (;;) {
+        for (int i = 0; i <= j; i++)
+            diff[i] = (diff[i] - diff[i + 1]) / deltmp[i];
+        if (--j < 0)
+            break;
+        for (int i = 0; i <= j; i++)
+            deltmp[i] = deltmp[i + 1] + s.deltaOld[i];
+    }
+    const double trapCoeff[2] = {.5, .08333333333};
+    double factor = trapCoeff[s.order - 1];
+    double del = o.trtol * tol / NG_MAX(o.abstol, factor * fabs(diff[0]));
+    if (s.order == 2)
+        del = sqrt(del);
+    return NG_MIN(timeStep, del);
+}
+
+/* CKTtrunc: DEVtrunc over all charges, min-reduced. */
+__device__ double ckt_trunc(const ngsf_ckt_t &C, Ctl &s, double timeStep)
+{
+    double t = 1e300;   /* HUGE */
+    for (int i = threadIdx.x; i < C.cap.n; i += blockDim.x)
+        t = ckt_terr(C, s, C.cap.st[i], t);
+    for (int i = threadIdx.x; i < C.mos1.n; i += blockDim.x) {
+        int b = C.mos1.st[i];
+        t = ckt_terr(C, s, b + M1S_QGS, t);
+        t = ckt_terr(C, s, b + M1S_QGD, t);
+        t = ckt_terr(C, s, b + M1S_QGB, t);
+    }
+    t = block_min(s, t);
+    return NG_MIN(2 * timeStep, t);
+}
+
+/* ---------------------------------------------------------------- */
+/* breakpoints (analysis/cktsetbk.c, cktclrbk.c); thread 0 only        */
+/* ---------------------------------------------------------------- */
+__device__ int set_break(const ngsf_ckt_t &C, Ctl &s, double time)
+{
+    double *b = C.breaks;
+    if (almost_equal_ulps(time, s.time, 3))
+        return 0;
+    if (s.time > time)
+        return NGSF_E_BREAKS;
+    for (int i = 0; i < s.nbreaks; i++) {
+        if (b[i] > time) {
+            if ((b[i] - time) <= C.opt.minbreak) {
+                b[i] = time;
+                return 0;
+            }
+            if (i > 0 && time - b[i - 1] <= C.opt.minbreak)
+                return 0;
+            if (s.nbreaks >= C.breakcap)
+                return NGSF_E_BREAKS;
+            for (int j = s.nbreaks; j > i; j--)
+                b[j] = b[j - 1];
+            b[i] = time;
+            s.nbreaks++;
+            return 0;
+        }
+    }
+    if (time - b[s.nbreaks - 1] <= C.opt.minbreak)
+        return 0;
+    if (s.nbreaks >= C.breakcap)
+        return NGSF_E_BREAKS;
+    b[s.nbreaks++] = time;
+    return 0;
+}
+
+__device__ void clr_break(const ngsf_ckt_t &C, Ctl &s)
+{
+    double *b = C.breaks;
+    if (s.nbreaks > 2) {
+        for (int j = 1; j < s.nbreaks; j++)
+            b[j - 1] = b[j];
+        s.nbreaks--;
+    } else {
+        b[0] = b[1];
+        b[1] = C.opt.tstop;
+    }
+}
+
+/* VSRCaccept / ISRCaccept breakpoint requests for PULSE and PWL
+ * (vsrc/vsrcacct.c:23-330). */
+__device__ int src_accept(const ngsf_ckt_t &C, Ctl &s, const ngsf_src_t &K)
+{
+    const ngsf_opts_t &o = C.opt;
+    for (int i = 0; i < K.n; i++) {
+        const double *cf = K.coef + (size_t)i * NGSF_MAX_COEFFS;
+        int nc = K.ncoef[i];
+        if (K.kind[i] == WF_PULSE) {
+            double TD = nc > 2 ? cf[2] : 0.0;
+            double TR = nc > 3 && cf[3] > 0.0 ? cf[3] : o.tstep;
+            double TF = nc > 4 && cf[4] > 0.0 ? cf[4] : o.tstep;
+            double PW = nc > 5 && cf[5] >= 0.0 ? cf[5] : 0.0;
+            double PER = nc > 6 && cf[6] > 0.0 ? cf[6] : TR + TF + PW;
+            double PHASE = nc > 7 ? cf[7] : 0.0;
+            double time = s.time - TD;
+            if (PHASE > 0.0) {
+                double tmax = PHASE * PER;
+                if (time > tmax)
+                    continue;
+            }
+            if (s.time >= K.brk[i]) {
+                double wait;
+                if (time >= PER) {
+                    double basetime = PER * floor(time / PER);
+                    time -= basetime;
+                }
+                double atime = time + o.minbreak;
+                if (atime < 0.0)
+                    wait = -time;
+                else if (atime < TR)
+                    wait = TR - time;
+                else if (atime < TR + PW)
+                    wait = TR + PW - time;
+                else if (atime < TR + PW + TF)
+                    wait = TR + PW + TF - time;
+                else
+                    wait = PER - time;
+                K.brk[i] = s.time + wait;
+                int e = set_break(C, s, K.brk[i]);
+                if (e)
+                    return e;
+                K.brk[i] -= o.minbreak;
+            }
+        } else if (K.kind[i] == WF_PWL) {
+            if (s.time >= K.brk[i]) {
+                double time = s.time;   /* no delay (td) support */
+                double end = cf[nc - 2];
+                if (time > end) {
+                    K.brk[i] = o.tstop;
+                    continue;
+                }
+                double atime = time + o.minbreak;
+                for (int k = 0; k < nc; k += 2) {
+                    if (cf[k] > atime) {
+                        K.brk[i] = s.time + cf[k] - time;
+                        int e = set_break(C, s, K.brk[i]);
+                        if (e)
+                            return e;
+                        K.brk[i] -= o.minbreak;
+                        break;
+                    }
+                }
+            }
+        }
+    }
+    return 0;
+}
+
+/* ---------------------------------------------------------------- */
+/* NIiter                                                            */
+/* ---------------------------------------------------------------- */
+enum { PH_OP = 1, PH_NEXTTIME = 2, PH_STEP = 3, PH_STEP_NIITER = 4 };
+
+__device__ void capture(const ngsf_ckt_t &C, Ctl &s, const Iter &it)
+{
+    int c = s.ncap;
+    if (c >= C.capmax)
+        return;
+    for (int p = threadIdx.x; p < C.nnz; p += blockDim.x)
+        C.cap_lux[(size_t)c * C.nnz + p] = C.ax[p];
+    for (int r = threadIdx.x; r <= C.n; r += blockDim.x) {
+        C.cap_rhs[(size_t)c * (C.n + 1) + r] = it.rhs[r];
+        C.cap_rhs[(size_t)(C.capmax + c) * (C.n + 1) + r] = it.rhsOld[r];
+    }
+    if (threadIdx.x == 0) {
+        C.cap_meta[4 * c + 0] = s.time;
+        C.cap_meta[4 * c + 1] = s.delta;
+        C.cap_meta[4 * c + 2] = s.mode;
+        C.cap_meta[4 * c + 3] = s.order;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+        s.ncap = c + 1;
+    __syncthreads();
+}
+
+/* One NIiter call.  With resume set, the loaded matrix of the iteration
+ * that asked for the re-pivot is already in ax / rhs and the host has just
+ * planned new pivots for it: the iteration continues at the factorization.
+ * Returns NGSF_NEED_REORDER when the host must choose pivots from the
+ * current matrix first (the reference reorders at MODEINITJCT, at the
+ * first MODEINITFIX iteration and at the first two iterations after
+ * MODEINITTRAN: niiter.c:107-111, :328-346). */
+__device__ int ni_iter(const ngsf_ckt_t &C, Ctl &s, int maxIter, bool resume)
+{
+    if (maxIter < 100)
+        maxIter = 100;
+    int iterno = resume ? s.savedIter : 0;
+    for (;;) {
+        Iter it = iter_ctx(C, s);
+        int noncon;
+        if (resume) {
+            noncon = s.savedNoncon;
+        } else {
+            noncon = ckt_load(C, s, it);
+            iterno++;
+            if (C.capmax > 0)
+                capture(C, s, it);
+            bool want = (s.mode & NGSF_MODEINITJCT) ||
+                        ((s.mode & NGSF_MODEINITTRAN) && iterno == 1) || s.shouldReorder;
+            if (want) {
+                if (threadIdx.x == 0) {
+                    s.savedIter = iterno;
+                    s.savedNoncon = noncon;
+                    s.shouldReorder = 0;
+                }
+                __syncthreads();
+                return NGSF_NEED_REORDER;
+            }
+        }
+        int bad = lu_factor(C, s);
+        if (bad) {
+            if (resume) {
+                /* fresh pivots from this very matrix still fail: singular */
+                if (threadIdx.x == 0) {
+                    s.numIter += iterno;
+                    s.badpivot++;
+                }
+                __syncthreads();
+                return NGSF_E_SINGULAR;
+            }
+            if (threadIdx.x == 0) {
+                s.savedIter = iterno;
+                s.savedNoncon = noncon;
+                s.badpivot++;
+            }
+            __syncthreads();
+            return NGSF_NEED_REORDER;
+        }
+        resume = false;
+        lu_solve(C, s, it.rhs);
+        if (threadIdx.x == 0) {
+            it.rhs[0] = 0;
+            it.rhsOld[0] = 0;
+        }
+        __syncthreads();
+        if (iterno > maxIter) {
+            if (threadIdx.x == 0)
+                s.numIter += iterno;
+            __syncthreads();
+            return NGSF_E_ITERLIM;
+        }
+        if (noncon == 0 && iterno != 1)
+            noncon = conv_test(C, s, it);
+        else
+            noncon = 1;
+        int mode = s.mode;
+        int ret = -1, reorder = 0;
+        if (mode & NGSF_MODEINITFLOAT) {
+            if (noncon == 0)
+                ret = NGSF_OK;
+        } else if (mode & NGSF_MODEINITJCT) {
+            mode = (mode & ~NGSF_INITF) | NGSF_MODEINITFIX;
+            reorder = 1;
+        } else if (mode & NGSF_MODEINITFIX) {
+            if (noncon == 0)
+                mode = (mode & ~NGSF_INITF) | NGSF_MODEINITFLOAT;
+        } else if (mode & NGSF_MODEINITTRAN) {
+            if (iterno <= 1)
+                reorder = 1;
+            mode = (mode & ~NGSF_INITF) | NGSF_MODEINITFLOAT;
+        } else if (mode & NGSF_MODEINITPRED) {
+            mode = (mode & ~NGSF_INITF) | NGSF_MODEINITFLOAT;
+        }
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            if (ret == NGSF_OK)
+                s.numIter += iterno;
+            else {
+                s.mode = mode;
+                if (reorder)
+                    s.shouldReorder = 1;
+                s.rhsSel ^= 1;   /* SWAP(rhs, rhsOld) */
+            }
+        }
+        __syncthreads();
+        if (ret == NGSF_OK)
+            return NGSF_OK;
+    }
+}
+
+/* NIcomCof, trapezoidal (src/maths/ni/nicomcof.c:17-47) */
+__device__ void ni_comcof(const ngsf_ckt_t &C, Ctl &s)
+{
+    if (s.order == 1) {
+        s.ag[0] = 1 / s.delta;
+        s.ag[1] = -1 / s.delta;
+    } else {
+        s.ag[0] = 1.0 / s.delta / (1.0 - C.opt.xmu);
+        s.ag[1] = C.opt.xmu / (1.0 - C.opt.xmu);
+    }
+}
+
+__device__ void copy_state(const ngsf_ckt_t &C, int dst, int src, const Ctl &s)
+{
+    double *d = C.states + (size_t)s.ring[dst] * C.nstates;
+    const double *a = C.states + (size_t)s.ring[src] * C.nstates;
+    for (int i = threadIdx.x; i < C.nstates; i += blockDim.x)
+        d[i] = a[i];
+    __syncthreads();
+}
+
+__device__ void dump_point(const ngsf_ckt_t &C, Ctl &s)
+{
+    int np = s.npoints;
+    if (np < C.outcap) {
+        Iter it = iter_ctx(C, s);
+        double *row = C.out + (size_t)np * (1 + C.nprobe);
+        for (int j = threadIdx.x; j < C.nprobe; j += blockDim.x)
+            row[1 + j] = it.rhsOld[C.probe[j]];
+        if (threadIdx.x == 0)
+            row[0] = s.time;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+        s.npoints = np + 1;
+    __syncthreads();
+}
+
+/* ---------------------------------------------------------------- */
+/* CKTop (src/spicelib/analysis/cktop.c:27-125) with its fallbacks    */
+/* dynamic_gmin (:161-262), new_gmin (:329-422) and gillespie_src      */
+/* (:436-654), as a resumable state machine                          */
+/* ---------------------------------------------------------------- */
+enum { OPP_NEWTON = 1, OPP_DG, OPP_DG_FINAL, OPP_NG, OPP_NG_FINAL, OPP_SS0, OPP_SSG, OPP_SS };
+
+#define NGSF_GMINFACTOR 10.0
+#define NGSF_ITL2 50
+
+__device__ void op_zero(const ngsf_ckt_t &C, Ctl &s)
+{
+    Iter it = iter_ctx(C, s);
+    for (int i = threadIdx.x; i <= C.n; i += blockDim.x)
+        it.rhsOld[i] = 0;
+    for (int i = threadIdx.x; i < C.nstates; i += blockDim.x)
+        it.st0[i] = 0;
+    __syncthreads();
+}
+
+__device__ void op_save(const ngsf_ckt_t &C, Ctl &s)
+{
+    Iter it = iter_ctx(C, s);
+    for (int i = threadIdx.x; i <= C.n; i += blockDim.x)
+        C.opsave_rhs[i] = it.rhsOld[i];
+    for (int i = threadIdx.x; i < C.nstates; i += blockDim.x)
+        C.opsave_st[i] = it.st0[i];
+    __syncthreads();
+}
+
+__device__ void op_restore(const ngsf_ckt_t &C, Ctl &s)
+{
+    Iter it = iter_ctx(C, s);
+    for (int i = threadIdx.x; i <= C.n; i += blockDim.x)
+        it.rhsOld[i] = C.opsave_rhs[i];
+    for (int i = threadIdx.x; i < C.nstates; i += blockDim.x)
+        it.st0[i] = C.opsave_st[i];
+    __syncthreads();
+}
+
+/* Returns 0 when the operating point converged, NGSF_NEED_REORDER when
+ * paused, another code when every method failed. */
+__device__ int op_run(const ngsf_ckt_t &C, Ctl &s, bool resume)
+{
+    const ngsf_opts_t &o = C.opt;
+    const int firstmode = NGSF_MODETRANOP | NGSF_MODEINITJCT;
+    const int contmode = NGSF_MODETRANOP | NGSF_MODEINITFLOAT;
+    const double gshunt = 0.0;
+    for (int guard = 0; guard < 100000; guard++) {
+        const int ph = s.opPhase;
+        if (ph == OPP_NEWTON) {
+            int r = ni_iter(C, s, o.itl1, resume);
+            resume = false;
+            if (r == NGSF_NEED_REORDER || r == 0)
+                return r;
+            /* dynamic gmin stepping */
+            op_zero(C, s);
+            if (threadIdx.x == 0) {
+                s.mode = firstmode;
+                s.factor = NGSF_GMINFACTOR;
+                s.oldGmin = 1e-2;
+                s.diagGmin = s.oldGmin / s.factor;
+                s.gtarget = NG_MAX(s.gmin, gshunt);
+                s.itersBefore = s.numIter;
+                s.opPhase = OPP_DG;
+            }
+            __syncthreads();
+        } else if (ph == OPP_DG || ph == OPP_NG) {
+            bool trueGmin = ph == OPP_NG;
+            int r = ni_iter(C, s, NGSF_ITL2, resume);
+            resume = false;
+            if (r == NGSF_NEED_REORDER)
+                return r;
+            int iters = s.numIter - s.itersBefore;
+            double g = trueGmin ? s.gmin : s.diagGmin;
+            int action = 0;   /* 0 next step, 1 save, 2 restore, 3 done */
+            if (r == 0) {
+                action = g <= s.gtarget ? 3 : 1;
+            } else {
+                action = s.factor < 1.00005 ? 3 : 2;
+            }
+            if (action == 1)
+                op_save(C, s);
+            if (action == 2)
+                op_restore(C, s);
+            if (threadIdx.x == 0) {
+                if (r == 0)
+                    s.mode = contmode;
+                if (action == 1) {
+                    if (iters <= (NGSF_ITL2 / 4)) {
+                        s.factor *= sqrt(s.factor);
+                        if (s.factor > NGSF_GMINFACTOR)
+                            s.factor = NGSF_GMINFACTOR;
+                    }
+                    if (iters > (3 * NGSF_ITL2 / 4))
+                        s.factor = trueGmin ? NG_MAX(sqrt(s.factor), 3) : NG_MAX(sqrt(s.factor), 1.00005);
+                    s.oldGmin = g;
+                    if (g < s.factor * s.gtarget) {
+                        s.factor = g / s.gtarget;
+                        g = s.gtarget;
+                    } else {
+                        g /= s.factor;
+                    }
+                } else if (action == 2) {
+                    s.factor = sqrt(sqrt(s.factor));
+                    g = s.oldGmin / s.factor;
+                }
+                if (trueGmin)
+                    s.gmin = g;
+                else
+                    s.diagGmin = g;
+                if (action == 3) {
+                    if (trueGmin) {
+                        s.gmin = NG_MAX(s.startgmin, gshunt);
+                        s.opPhase = OPP_NG_FINAL;
+                    } else {
+                        s.diagGmin = gshunt;
+                        s.opPhase = OPP_DG_FINAL;
+                    }
+                }
+                s.itersBefore = s.numIter;
+            }
+            __syncthreads();
+        } else if (ph == OPP_DG_FINAL || ph == OPP_NG_FINAL) {
+            int r = ni_iter(C, s, o.itl1, resume);
+            resume = false;
+            if (r == NGSF_NEED_REORDER || r == 0)
+                return r;
+            if (ph == OPP_DG_FINAL) {
+                /* true gmin stepping */
+                op_zero(C, s);
+                if (threadIdx.x == 0) {
+                    s.mode = firstmode;
+                    s.startgmin = s.gmin;
+                    s.factor = NGSF_GMINFACTOR;
+                    s.oldGmin = 1e-2;
+                    s.gmin = s.oldGmin / s.factor;
+                    s.gtarget = NG_MAX(s.startgmin, gshunt);
+                    s.itersBefore = s.numIter;
+                    s.opPhase = OPP_NG;
+                }
+            } else {
+                /* Gillespie source stepping */
+                op_zero(C, s);
+                if (threadIdx.x == 0) {
+                    s.startgmin = s.gmin;   /* gminstart */
+                    s.mode = firstmode;
+                    s.srcFact = 0;
+                    s.convFact = 0;
+                    s.opPhase = OPP_SS0;
+                }
+            }
+            __syncthreads();
+        } else if (ph == OPP_SS0 || ph == OPP_SSG) {
+            int r = ni_iter(C, s, NGSF_ITL2, resume);
+            resume = false;
+            if (r == NGSF_NEED_REORDER)
+                return r;
+            bool startRaise = false, failed = false;
+            if (ph == OPP_SS0) {
+                if (r != 0) {
+                    if (threadIdx.x == 0) {
+                        double dg = (gshunt <= 0) ? s.gmin : gshunt;
+                        for (int i = 0; i < 10; i++)
+                            dg *= 10;
+                        s.diagGmin = dg;
+                        s.gi = 0;
+                        s.opPhase = OPP_SSG;
+                    }
+                    __syncthreads();
+                } else {
+                    startRaise = true;
+                }
+            } else {
+                if (r != 0) {
+                    failed = true;
+                } else {
+                    if (threadIdx.x == 0) {
+                        s.diagGmin /= 10;
+                        s.mode = contmode;
+                        s.gi++;
+                    }
+                    __syncthreads();
+                    if (s.gi > 10)
+                        startRaise = true;
+                }
+                if (failed || startRaise) {
+                    if (threadIdx.x == 0)
+                        s.diagGmin = gshunt;
+                    __syncthreads();
+                }
+            }
+            if (failed) {
+                if (threadIdx.x == 0)
+                    s.srcFact = 1;
+                __syncthreads();
+                return NGSF_E_ITERLIM;
+            }
+            if (startRaise) {
+                op_save(C, s);
+                if (threadIdx.x == 0) {
+                    s.raise = 0.001;
+                    s.srcFact = s.convFact + s.raise;
+                    s.itersBefore = s.numIter;
+                    s.opPhase = OPP_SS;
+                }
+                __syncthreads();
+            }
+        } else if (ph == OPP_SS) {
+            int r = ni_iter(C, s, NGSF_ITL2, resume);
+            resume = false;
+            if (r == NGSF_NEED_REORDER)
+                return r;
+            int iters = s.numIter - s.itersBefore;
+            bool brk = false;
+            if (r == 0) {
+                op_save(C, s);
+            } else {
+                brk = s.srcFact - s.convFact < 1e-8;
+                if (!brk) {
+                    /* restore uses the rhsOld selected below: swap first */
+                    op_restore(C, s);
+                }
+            }
+            if (threadIdx.x == 0) {
+                s.mode = contmode;
+                if (r == 0) {
+                    s.convFact = s.srcFact;
+                    s.srcFact = s.convFact + s.raise;
+                    if (iters <= (NGSF_ITL2 / 4))
+                        s.raise *= 1.5;
+                    if (iters > (3 * NGSF_ITL2 / 4))
+                        s.raise *= 0.5;
+                } else if (!brk) {
+                    s.raise /= 10;
+                    if (s.raise > 0.01)
+                        s.raise = 0.01;
+                    s.srcFact = s.convFact;
+                }
+                if (s.srcFact > 1)
+                    s.srcFact = 1;
+                s.itersBefore = s.numIter;
+            }
+            __syncthreads();
+            if (brk || !((s.raise >= 1e-7) && (s.convFact < 1))) {
+                int ok = s.convFact == 1;
+                if (threadIdx.x == 0) {
+                    s.diagGmin = s.gmin = s.startgmin;
+                    s.srcFact = 1;
+                }
+                __syncthreads();
+                return ok ? 0 : NGSF_E_ITERLIM;
+            }
+        } else {
+            return NGSF_E_NOOP;
+        }
+    }
+    return NGSF_E_NOOP;
+}
+
+/* ---------------------------------------------------------------- */
+/* DCtran, as a resumable state machine                              */
+/* ---------------------------------------------------------------- */
+__device__ int dc_tran(const ngsf_ckt_t &C, Ctl &s, long long maxSteps, bool resume)
+{
+    const ngsf_opts_t &o = C.opt;
+    const int maxOrder = o.maxord;
+    if (!resume) {
+        if (threadIdx.x == 0) {
+            s.delta = NG_MIN(o.tstop / 100, o.tstep) / 10;   /* local 'delta' */
+            s.delta0 = s.delta;
+            C.breaks[0] = 0;
+            C.breaks[1] = o.tstop;
+            s.nbreaks = 2;
+            s.time = 0;
+            s.firsttime = 1;
+            s.mode = NGSF_MODETRANOP | NGSF_MODEINITJCT;
+            s.order = 1;
+            s.phase = PH_OP;
+            s.opPhase = OPP_NEWTON;
+            s.steps = 0;
+        }
+        __syncthreads();
+    }
+    if (s.phase == PH_OP) {
+        /* CKTop: Newton on the operating point, then its fallbacks */
+        int conv = op_run(C, s, resume);
+        resume = false;
+        if (conv == NGSF_NEED_REORDER)
+            return conv;
+        if (conv != 0)
+            return conv == NGSF_E_SINGULAR ? conv : NGSF_E_NOOP;
+        if (threadIdx.x == 0) {
+            s.opiter = s.numIter;
+            s.timePts++;
+            s.order = 1;
+            for (int i = 0; i < 7; i++)
+                s.deltaOld[i] = o.tmax;
+            s.delta = s.delta0;              /* CKTdelta = delta */
+            s.saveDelta = o.tstop / 50;
+            s.mode = NGSF_MODETRAN | NGSF_MODEINITTRAN;
+            s.ag[0] = s.ag[1] = 0;
+            s.phase = PH_NEXTTIME;
+        }
+        __syncthreads();
+        copy_state(C, 1, 0, s);
+    }
+
+    for (;;) {
+        if (s.phase == PH_NEXTTIME) {
+            /* nextTime: CKTaccept, clear passed breakpoint, dump, finish test */
+            if (threadIdx.x == 0) {
+                int e = src_accept(C, s, C.vsrc);
+                if (!e)
+                    e = src_accept(C, s, C.isrc);
+                s.flag = e;
+                if (!e && s.time > C.breaks[0])
+                    clr_break(C, s);
+                s.accepted++;
+            }
+            __syncthreads();
+            if (s.flag)
+                return s.flag;
+            if (s.time >= o.tstart)
+                dump_point(C, s);
+            if (almost_equal_ulps(s.time, o.tstop, 100))
+                return NGSF_OK;
+            if (s.steps + 1 > maxSteps)
+                return NGSF_E_WATCHDOG;
+            /* resume: */
+            if (threadIdx.x == 0) {
+                s.steps++;
+                double *b = C.breaks;
+                s.delta = NG_MIN(s.delta, o.tmax);
+                if (almost_equal_ulps(s.time, b[0], 100) || b[0] - s.time <= o.delmin) {
+                    s.order = 1;
+                    s.delta = NG_MIN(s.delta, .1 * NG_MIN(s.saveDelta, b[1] - b[0]));
+                    if (s.firsttime)
+                        s.delta /= 10;
+                }
+                while ((b[0] <= s.time + o.minbreak || almost_equal_ulps(b[0], s.time, 100)) &&
+                       b[0] < o.tstop)
+                    clr_break(C, s);
+                if (s.time + s.delta > b[0]) {
+                    s.saveDelta = s.delta;
+                    s.delta = b[0] - s.time;
+                } else if (s.time + 1.9 * s.delta > b[0]) {
+                    s.saveDelta = s.delta;
+                    s.delta = (b[0] - s.time) / 2.;
+                }
+                for (int i = 5; i >= 0; i--)
+                    s.deltaOld[i + 1] = s.deltaOld[i];
+                s.deltaOld[0] = s.delta;
+                int temp = s.ring[maxOrder + 1];
+                for (int i = maxOrder; i >= 0; i--)
+                    s.ring[i + 1] = s.ring[i];
+                s.ring[0] = temp;
+                s.phase = PH_STEP;
+            }
+            __syncthreads();
+        }
+        if (s.phase == PH_STEP) {
+            if (threadIdx.x == 0) {
+                s.olddelta = s.delta;
+                s.time += s.delta;
+                s.deltaOld[0] = s.delta;
+                ni_comcof(C, s);
+                s.iters0 = s.numIter;
+                s.phase = PH_STEP_NIITER;
+            }
+            __syncthreads();
+        }
+        /* PH_STEP_NIITER */
+        int converged = ni_iter(C, s, o.itl4, resume);
+        resume = false;
+        if (converged == NGSF_NEED_REORDER)
+            return converged;
+        if (threadIdx.x == 0) {
+            s.tranIter += s.numIter - s.iters0;
+            s.timePts++;
+            s.mode = NGSF_MODETRAN | NGSF_MODEINITPRED;
+        }
+        __syncthreads();
+        if (s.firsttime) {
+            copy_state(C, 2, 1, s);
+            copy_state(C, 3, 1, s);
+        }
+        if (converged == NGSF_E_SINGULAR)
+            return converged;
+        if (converged != 0) {
+            if (threadIdx.x == 0) {
+                s.time = s.time - s.delta;
+                s.rejected++;
+                s.delta = s.delta / 8;
+                if (s.firsttime)
+                    s.mode = NGSF_MODETRAN | NGSF_MODEINITTRAN;
+                s.order = 1;
+            }
+            __syncthreads();
+        } else {
+            if (s.firsttime) {
+                __syncthreads();
+                if (threadIdx.x == 0) {
+                    s.firsttime = 0;
+                    s.phase = PH_NEXTTIME;
+                }
+                __syncthreads();
+                continue;
+            }
+            double newdelta = ckt_trunc(C, s, s.delta);
+            if (newdelta > .9 * s.delta) {
+                if (s.order == 1 && maxOrder > 1) {
+                    if (threadIdx.x == 0)
+                        s.order = 2;
+                    __syncthreads();
+                    newdelta = ckt_trunc(C, s, s.delta);
+                    if (threadIdx.x == 0 && newdelta <= 1.05 * s.delta)
+                        s.order = 1;
+                    __syncthreads();
+                }
+                if (threadIdx.x == 0) {
+                    s.delta = newdelta;
+                    s.phase = PH_NEXTTIME;
+                }
+                __syncthreads();
+                continue;
+            } else {
+                if (threadIdx.x == 0) {
+                    s.time = s.time - s.delta;
+                    s.rejected++;
+                    s.delta = newdelta;
+                }
+                __syncthreads();
+            }
+        }
+        if (s.delta <= o.delmin) {
+            if (s.olddelta > o.delmin) {
+                if (threadIdx.x == 0)
+                    s.delta = o.delmin;
+                __syncthreads();
+            } else {
+                return NGSF_E_TIMESTEP;
+            }
+        }
+        if (threadIdx.x == 0) {
+            s.steps++;
+            s.phase = PH_STEP;
+        }
+        __syncthreads();
+        if (s.steps > maxSteps)
+            return NGSF_E_WATCHDOG;
+    }
+}
+
+/* launch modes */
+#define RUN_FRESH 0
+#define RUN_RESUME 1
+#define RUN_PROBE 2
+
+__global__ void __launch_bounds__(NGSF_THREADS)
+tran_kernel(const ngsf_ckt_t *ckts, int nckt, int runMode, long long maxSteps)
+{
+    __shared__ Ctl s;
+    __shared__ __align__(16) ngsf_ckt_t Cs;
+    int b = blockIdx.x;
+    if (b >= nckt)
+        return;
+    {
+        const unsigned long long *src = (const unsigned long long *)(ckts + b);
+        unsigned long long *dst = (unsigned long long *)&Cs;
+        for (int w = threadIdx.x; w < (int)(sizeof(ngsf_ckt_t) / 8); w += blockDim.x)
+            dst[w] = src[w];
+    }
+    __syncthreads();
+    const ngsf_ckt_t &C = Cs;
+    if (runMode == RUN_RESUME) {
+        const int *src = (const int *)C.ctlsave;
+        int *dst = (int *)&s;
+        for (int w = threadIdx.x; w < (int)(sizeof(Ctl) / 4); w += blockDim.x)
+            dst[w] = src[w];
+        __syncthreads();
+    } else {
+        if (threadIdx.x == 0) {
+            for (int i = 0; i < 4; i++)
+                s.ring[i] = i;
+            s.rhsSel = 0;
+            s.status = 0;
+            s.accepted = s.rejected = s.numIter = s.tranIter = s.timePts = 0;
+            s.npoints = s.ncap = s.badpivot = s.opiter = 0;
+            s.order = 1;
+            s.delta = 0;
+            s.time = 0;
+            s.flag = 0;
+            s.phase = 0;
+            s.shouldReorder = 0;
+            s.savedIter = s.savedNoncon = s.iters0 = s.reorders = 0;
+            s.steps = 0;
+            s.gmin = C.opt.gmin;
+            s.diagGmin = 0.0;
+            s.srcFact = 1.0;
+            s.opPhase = 0;
+            for (int i = 0; i < 7; i++) {
+                s.ag[i] = 0;
+                s.deltaOld[i] = 0;
+            }
+        }
+        __syncthreads();
+        /* zero per-run buffers: states, rhs, per-instance memories */
+        for (size_t i = threadIdx.x; i < (size_t)4 * C.nstates; i += blockDim.x)
+            C.states[i] = 0.0;
+        for (int i = threadIdx.x; i <= C.n; i += blockDim.x) {
+            C.rhs[i] = 0.0;
+            C.rhsOld[i] = 0.0;
+        }
+        for (size_t i = threadIdx.x; i < (size_t)M1H_COUNT * C.mos1.n; i += blockDim.x)
+            C.mos1.h[i] = 0.0;
+        for (int i = threadIdx.x; i < C.vsrc.n; i += blockDim.x)
+            C.vsrc.brk[i] = -1.0;
+        for (int i = threadIdx.x; i < C.isrc.n; i += blockDim.x)
+            C.isrc.brk[i] = -1.0;
+        __syncthreads();
+    }
+    int status;
+    if (runMode == RUN_PROBE) {
+        if (threadIdx.x == 0)
+            s.mode = NGSF_MODETRANOP | NGSF_MODEINITJCT;
+        __syncthreads();
+        Iter it = iter_ctx(C, s);
+        ckt_load(C, s, it);
+        status = NGSF_OK;
+    } else {
+        status = dc_tran(C, s, maxSteps, runMode == RUN_RESUME);
+    }
+    __syncthreads();
+    if (status == NGSF_NEED_REORDER) {
+        if (threadIdx.x == 0)
+            s.reorders++;
+        __syncthreads();
+        int *dst = (int *)C.ctlsave;
+        const int *src = (const int *)&s;
+        for (int w = threadIdx.x; w < (int)(sizeof(Ctl) / 4); w += blockDim.x)
+            dst[w] = src[w];
+    }
+    if (threadIdx.x == 0) {
+        C.result[NGSF_R_STATUS] = status;
+        C.result[NGSF_R_NPOINTS] = s.npoints;
+        C.result[NGSF_R_ACCEPTED] = s.accepted;
+        C.result[NGSF_R_REJECTED] = s.rejected;
+        C.result[NGSF_R_NUMITER] = s.numIter;
+        C.result[NGSF_R_TRANITER] = s.tranIter;
+        C.result[NGSF_R_TIMEPTS] = s.timePts;
+        C.result[NGSF_R_NCAP] = s.ncap;
+        C.result[NGSF_R_OPITER] = s.opiter;
+        C.result[NGSF_R_BADPIVOT] = s.badpivot;
+        C.result[NGSF_R_REORDERS] = s.reorders;
+        C.fresult[NGSF_F_TIME] = s.time;
+        C.fresult[NGSF_F_DELTA] = s.delta;
+        C.fresult[NGSF_F_DIAGGMIN] = s.diagGmin;
+    }
+}
+
+}  // namespace
+
+extern "C" int ngsf_ctl_bytes(void) { return (int)sizeof(Ctl); }
+
+extern "C" cudaError_t ngsf_launch_tran(const ngsf_ckt_t *d_ckts, int nckt, int runMode,
+                                        long long maxSteps, cudaStream_t stream)
+{
+    if (nckt <= 0)
+        return cudaSuccess;
+    tran_kernel<<<nckt, NGSF_THREADS, 0, stream>>>(d_ckts, nckt, runMode, maxSteps);
+    return cudaGetLastError();
+}

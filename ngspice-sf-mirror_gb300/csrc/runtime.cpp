@@ -1,0 +1,457 @@
+/*
+ * Host runtime: owns the device copy of compiled circuits and drives the
+ * GPU transient engine.
+ *
+ * One run of `.tran` on a circuit goes:
+ *   1. upload the compiled image into one device arena;
+ *   2. launch: operating point and time loop run on the GPU; the kernel
+ *      pauses wherever the reference would re-factor with pivoting
+ *      (SMPreorder at MODEINITJCT, the first MODEINITFIX iteration, the
+ *      first two iterations after MODEINITTRAN, or a failed refactor);
+ *   3. at a pause the host chooses pivots from the stamped matrix
+ *      (sparse.cpp), uploads the new LU plan and relaunches; the kernel
+ *      resumes from its saved control block;
+ *   4. download of accepted points and counters.
+ * A batch runs many circuits per launch, one block each; only the paused
+ * ones are relaunched.
+ */
+#include <cuda_runtime.h>
+
+#include <chrono>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "circuit.h"
+#include "runtime.h"
+#include "sparse.h"
+
+extern "C" cudaError_t ngsf_launch_tran(const ngsf_ckt_t *d_ckts, int nckt, int runMode,
+                                        long long maxSteps, cudaStream_t stream);
+extern "C" int ngsf_ctl_bytes(void);
+
+namespace ngsf {
+
+namespace {
+
+void ck(cudaError_t e, const char *what)
+{
+    if (e != cudaSuccess)
+        throw std::runtime_error(std::string("CUDA error in ") + what + ": " +
+                                 cudaGetErrorString(e));
+}
+
+/* bump allocator over one device allocation */
+struct Arena {
+    size_t used = 0;
+    std::vector<std::pair<size_t, const void *>> uploads;   /* offset, host src */
+    std::vector<size_t> sizes;
+    size_t take(size_t bytes)
+    {
+        size_t off = (used + 255) & ~(size_t)255;
+        used = off + bytes;
+        return off;
+    }
+};
+
+}  // namespace
+
+struct DeviceCircuit::Impl {
+    char *base = nullptr;
+    size_t bytes = 0;
+    char *lubase = nullptr;
+    size_t lubytes = 0;
+    ngsf_ckt_t h{};            /* device pointers */
+    ngsf_ckt_t *d_desc = nullptr;
+};
+
+DeviceCircuit::DeviceCircuit() : impl(new Impl) {}
+DeviceCircuit::~DeviceCircuit()
+{
+    if (impl->base)
+        cudaFree(impl->base);
+    if (impl->lubase)
+        cudaFree(impl->lubase);
+    if (impl->d_desc)
+        cudaFree(impl->d_desc);
+    delete impl;
+}
+
+/* Lay out every array of the image in one arena and copy it up. */
+void DeviceCircuit::upload(const Image &img, const std::vector<int> &probes, int outcap,
+                           int capmax)
+{
+    Arena a;
+    struct Plan {
+        size_t off;
+        const void *src;
+        size_t bytes;
+    };
+    std::vector<Plan> plans;
+    auto put = [&](const void *src, size_t bytes) -> size_t {
+        size_t off = a.take(bytes ? bytes : 8);
+        if (src && bytes)
+            plans.push_back({off, src, bytes});
+        return off;
+    };
+    auto puti = [&](const std::vector<int> &v) { return put(v.data(), v.size() * sizeof(int)); };
+    auto putd = [&](const std::vector<double> &v) {
+        return put(v.data(), v.size() * sizeof(double));
+    };
+    auto zero = [&](size_t bytes) { return put(nullptr, bytes); };
+
+    const int n = img.n;
+    const int nnz = (int)img.a_ri.size();
+    struct Off {
+        size_t mos1_node, mos1_st, mos1_p, mos1_h;
+        size_t res_node, res_g;
+        size_t cap_node, cap_st, cap_c, cap_m, cap_ic;
+        size_t vs[9], is[9];
+        size_t ntype, stampv, ax, gptr, gsrc, rptr, rsrc, a_diag, opsave_rhs, opsave_st;
+        size_t lux, lvl_ptr, lvl_col, cdiag, cend, cbeg, kptr, kdep, kpos, kseg, upd_dst,
+            upd_src, prow, pcol, fl_ptr, fl_row, bl_ptr, bl_row, lr_ptr, lr_col, lr_pos,
+            ur_ptr, ur_col, ur_pos, work;
+        size_t states, rhs, rhsOld, breaks, out, probe, cap_ax, cap_rhs, cap_meta, result,
+            fresult, ctlsave;
+    } o{};
+    o.mos1_node = puti(img.mos1_node);
+    o.mos1_st = puti(img.mos1_st);
+    o.mos1_p = putd(img.mos1_p);
+    o.mos1_h = zero((size_t)M1H_COUNT * img.nmos1 * sizeof(double));
+    o.res_node = puti(img.res_node);
+    o.res_g = putd(img.res_g);
+    o.cap_node = puti(img.cap_node);
+    o.cap_st = puti(img.cap_st);
+    o.cap_c = putd(img.cap_c);
+    o.cap_m = putd(img.cap_m);
+    o.cap_ic = putd(img.cap_ic);
+    auto put_src = [&](size_t *s, const std::vector<int> &node, const std::vector<int> &kind,
+                       const std::vector<int> &nc, const std::vector<double> &coef,
+                       const std::vector<double> &dc, const std::vector<int> &dcg,
+                       const std::vector<double> &m, int cnt) {
+        s[0] = puti(node);
+        s[1] = puti(kind);
+        s[2] = puti(nc);
+        s[3] = putd(coef);
+        s[4] = putd(dc);
+        s[5] = puti(dcg);
+        s[6] = putd(m);
+        s[7] = zero((size_t)cnt * sizeof(double));
+    };
+    put_src(o.vs, img.vsrc_node, img.vsrc_kind, img.vsrc_ncoef, img.vsrc_coef, img.vsrc_dc,
+            img.vsrc_dcgiven, img.vsrc_m, img.nvsrc);
+    put_src(o.is, img.isrc_node, img.isrc_kind, img.isrc_ncoef, img.isrc_coef, img.isrc_dc,
+            img.isrc_dcgiven, img.isrc_m, img.nisrc);
+    o.ntype = puti(img.ntype);
+    o.stampv = zero((size_t)img.nstamp * sizeof(double));
+    o.ax = zero((size_t)nnz * sizeof(double));
+    o.gptr = puti(img.gptr);
+    o.gsrc = puti(img.gsrc);
+    o.rptr = puti(img.rptr);
+    o.rsrc = puti(img.rsrc);
+    o.a_diag = puti(img.a_diag);
+    o.opsave_rhs = zero((size_t)(n + 1) * sizeof(double));
+    o.opsave_st = zero((size_t)(img.nstates + 1) * sizeof(double));
+    o.work = zero((size_t)(n + 1) * sizeof(double));
+    o.states = zero((size_t)4 * (img.nstates + 1) * sizeof(double));
+    o.rhs = zero((size_t)(n + 1) * sizeof(double));
+    o.rhsOld = zero((size_t)(n + 1) * sizeof(double));
+    const int breakcap = 2 + 4 * (img.nvsrc + img.nisrc) + 64;
+    o.breaks = zero((size_t)breakcap * sizeof(double));
+    probes_ = probes;
+    o.out = zero((size_t)outcap * (1 + probes.size()) * sizeof(double));
+    o.probe = puti(probes_);
+    o.cap_ax = zero((size_t)capmax * nnz * sizeof(double));
+    o.cap_rhs = zero((size_t)2 * capmax * (n + 1) * sizeof(double));
+    o.cap_meta = zero((size_t)4 * capmax * sizeof(double));
+    o.ctlsave = zero((size_t)ngsf_ctl_bytes() + 64);
+    o.result = zero(NGSF_R_COUNT * sizeof(int));
+    o.fresult = zero(NGSF_F_COUNT * sizeof(double));
+
+    if (impl->base)
+        cudaFree(impl->base);
+    impl->bytes = a.used;
+    ck(cudaMalloc(&impl->base, a.used), "cudaMalloc(arena)");
+    ck(cudaMemset(impl->base, 0, a.used), "cudaMemset(arena)");
+    for (auto &p : plans)
+        ck(cudaMemcpy(impl->base + p.off, p.src, p.bytes, cudaMemcpyHostToDevice),
+           "cudaMemcpy(upload)");
+
+    char *b = impl->base;
+    auto I = [&](size_t off) { return (int *)(b + off); };
+    auto D = [&](size_t off) { return (double *)(b + off); };
+    ngsf_ckt_t &h = impl->h;
+    memset(&h, 0, sizeof(h));
+    h.n = n;
+    h.nstates = img.nstates;
+    h.nstamp = img.nstamp;
+    h.nnz = nnz;
+    h.opt = img.opt;
+    h.mos1 = {img.nmos1, I(o.mos1_node), I(o.mos1_st), D(o.mos1_p), D(o.mos1_h),
+              img.mos1_stamp0};
+    h.res = {img.nres, I(o.res_node), D(o.res_g), img.res_stamp0};
+    h.cap = {img.ncap, I(o.cap_node), I(o.cap_st), D(o.cap_c), D(o.cap_m), D(o.cap_ic),
+             img.cap_stamp0};
+    h.vsrc = {img.nvsrc, I(o.vs[0]), I(o.vs[1]), I(o.vs[2]), D(o.vs[3]), D(o.vs[4]),
+              I(o.vs[5]), D(o.vs[6]), D(o.vs[7]), img.vsrc_stamp0};
+    h.isrc = {img.nisrc, I(o.is[0]), I(o.is[1]), I(o.is[2]), D(o.is[3]), D(o.is[4]),
+              I(o.is[5]), D(o.is[6]), D(o.is[7]), img.isrc_stamp0};
+    h.ntype = I(o.ntype);
+    h.stampv = D(o.stampv);
+    h.ax = D(o.ax);
+    h.gptr = I(o.gptr);
+    h.gsrc = I(o.gsrc);
+    h.rptr = I(o.rptr);
+    h.rsrc = I(o.rsrc);
+    h.a_diag = I(o.a_diag);
+    h.opsave_rhs = D(o.opsave_rhs);
+    h.opsave_st = D(o.opsave_st);
+    h.work = D(o.work);
+    h.states = D(o.states);
+    h.rhs = D(o.rhs);
+    h.rhsOld = D(o.rhsOld);
+    h.breaks = D(o.breaks);
+    h.breakcap = breakcap;
+    h.out = D(o.out);
+    h.probe = I(o.probe);
+    h.nprobe = (int)probes.size();
+    h.outcap = outcap;
+    h.cap_lux = D(o.cap_ax);
+    h.cap_rhs = D(o.cap_rhs);
+    h.cap_meta = D(o.cap_meta);
+    h.capmax = capmax;
+    h.ctlsave = (void *)(b + o.ctlsave);
+    h.result = I(o.result);
+    h.fresult = D(o.fresult);
+    if (!impl->d_desc)
+        ck(cudaMalloc(&impl->d_desc, sizeof(ngsf_ckt_t)), "cudaMalloc(desc)");
+    ck(cudaMemcpy(impl->d_desc, &h, sizeof(h), cudaMemcpyHostToDevice), "cudaMemcpy(desc)");
+    n_ = n;
+    nnz_ = nnz;
+    outcap_ = outcap;
+    capmax_ = capmax;
+}
+
+const ngsf_ckt_t &DeviceCircuit::desc() const { return impl->h; }
+ngsf_ckt_t *DeviceCircuit::device_desc() const { return impl->d_desc; }
+size_t DeviceCircuit::bytes() const { return impl->bytes + impl->lubytes; }
+
+/* Upload the LU plan (pivot sequence, layout, update lists, levels) into
+ * its own allocation, replacing the previous plan. */
+void DeviceCircuit::upload_lu(const Image &img)
+{
+    Arena a;
+    struct Plan {
+        size_t off;
+        const void *src;
+        size_t bytes;
+    };
+    std::vector<Plan> plans;
+    auto put = [&](const void *src, size_t bytes) -> size_t {
+        size_t off = a.take(bytes ? bytes : 8);
+        if (src && bytes)
+            plans.push_back({off, src, bytes});
+        return off;
+    };
+    auto puti = [&](const std::vector<int> &v) { return put(v.data(), v.size() * sizeof(int)); };
+    size_t o_lux = put(nullptr, (size_t)img.nlu * sizeof(double));
+    size_t o_a_lupos = puti(img.a_lupos), o_lvl_ptr = puti(img.lvl_ptr),
+           o_lvl_col = puti(img.lvl_col), o_cdiag = puti(img.cdiag), o_cend = puti(img.cend),
+           o_cbeg = puti(img.cbeg), o_kptr = puti(img.kptr), o_kdep = puti(img.kdep),
+           o_kpos = puti(img.kpos), o_kseg = puti(img.kseg), o_upd_dst = puti(img.upd_dst),
+           o_upd_src = puti(img.upd_src), o_prow = puti(img.prow), o_pcol = puti(img.pcol),
+           o_fl_ptr = puti(img.fl_ptr), o_fl_row = puti(img.fl_row), o_bl_ptr = puti(img.bl_ptr),
+           o_bl_row = puti(img.bl_row), o_lr_ptr = puti(img.lr_ptr), o_lr_col = puti(img.lr_col),
+           o_lr_pos = puti(img.lr_pos), o_ur_ptr = puti(img.ur_ptr), o_ur_col = puti(img.ur_col),
+           o_ur_pos = puti(img.ur_pos);
+    if (impl->lubase)
+        cudaFree(impl->lubase);
+    impl->lubase = nullptr;
+    impl->lubytes = a.used;
+    ck(cudaMalloc(&impl->lubase, a.used), "cudaMalloc(lu arena)");
+    for (auto &p : plans)
+        ck(cudaMemcpy(impl->lubase + p.off, p.src, p.bytes, cudaMemcpyHostToDevice),
+           "cudaMemcpy(lu upload)");
+    char *b = impl->lubase;
+    auto I = [&](size_t off) { return (int *)(b + off); };
+    ngsf_ckt_t &h = impl->h;
+    h.nlu = img.nlu;
+    h.nlevels = (int)img.lvl_ptr.size() - 1;
+    h.nflevels = (int)img.fl_ptr.size() - 1;
+    h.nblevels = (int)img.bl_ptr.size() - 1;
+    h.lux = (double *)(b + o_lux);
+    h.a_lupos = I(o_a_lupos);
+    h.lvl_ptr = I(o_lvl_ptr);
+    h.lvl_col = I(o_lvl_col);
+    h.cdiag = I(o_cdiag);
+    h.cend = I(o_cend);
+    h.cbeg = I(o_cbeg);
+    h.kptr = I(o_kptr);
+    h.kdep = I(o_kdep);
+    h.kpos = I(o_kpos);
+    h.kseg = I(o_kseg);
+    h.upd_dst = I(o_upd_dst);
+    h.upd_src = I(o_upd_src);
+    h.prow = I(o_prow);
+    h.pcol = I(o_pcol);
+    h.fl_ptr = I(o_fl_ptr);
+    h.fl_row = I(o_fl_row);
+    h.bl_ptr = I(o_bl_ptr);
+    h.bl_row = I(o_bl_row);
+    h.lr_ptr = I(o_lr_ptr);
+    h.lr_col = I(o_lr_col);
+    h.lr_pos = I(o_lr_pos);
+    h.ur_ptr = I(o_ur_ptr);
+    h.ur_col = I(o_ur_col);
+    h.ur_pos = I(o_ur_pos);
+    ck(cudaMemcpy(impl->d_desc, &h, sizeof(h), cudaMemcpyHostToDevice), "cudaMemcpy(desc)");
+}
+
+std::vector<double> DeviceCircuit::read_ax()
+{
+    std::vector<double> ax(nnz_);
+    ck(cudaMemcpy(ax.data(), impl->h.ax, nnz_ * sizeof(double), cudaMemcpyDeviceToHost),
+       "cudaMemcpy(ax)");
+    return ax;
+}
+
+void DeviceCircuit::read_results(std::vector<int> &ires, std::vector<double> &fres)
+{
+    ires.resize(NGSF_R_COUNT);
+    fres.resize(NGSF_F_COUNT);
+    ck(cudaMemcpy(ires.data(), impl->h.result, NGSF_R_COUNT * sizeof(int),
+                  cudaMemcpyDeviceToHost), "cudaMemcpy(result)");
+    ck(cudaMemcpy(fres.data(), impl->h.fresult, NGSF_F_COUNT * sizeof(double),
+                  cudaMemcpyDeviceToHost), "cudaMemcpy(fresult)");
+}
+
+void DeviceCircuit::read_points(int npoints, std::vector<double> &out)
+{
+    int np = std::min(npoints, outcap_);
+    out.resize((size_t)np * (1 + probes_.size()));
+    if (np)
+        ck(cudaMemcpy(out.data(), impl->h.out, out.size() * sizeof(double),
+                      cudaMemcpyDeviceToHost), "cudaMemcpy(out)");
+}
+
+void DeviceCircuit::read_capture(int ncap, std::vector<double> &ax, std::vector<double> &rhs,
+                                 std::vector<double> &meta)
+{
+    int nc = std::min(ncap, capmax_);
+    ax.resize((size_t)nc * nnz_);
+    rhs.resize((size_t)2 * capmax_ * (n_ + 1));
+    meta.resize((size_t)4 * nc);
+    if (!nc)
+        return;
+    ck(cudaMemcpy(ax.data(), impl->h.cap_lux, ax.size() * sizeof(double),
+                  cudaMemcpyDeviceToHost), "cudaMemcpy(cap ax)");
+    ck(cudaMemcpy(rhs.data(), impl->h.cap_rhs, rhs.size() * sizeof(double),
+                  cudaMemcpyDeviceToHost), "cudaMemcpy(cap rhs)");
+    ck(cudaMemcpy(meta.data(), impl->h.cap_meta, meta.size() * sizeof(double),
+                  cudaMemcpyDeviceToHost), "cudaMemcpy(cap meta)");
+}
+
+/* ------------------------------------------------------------------ */
+/* Prepared circuit: compile + pivot plan, device resident              */
+/* ------------------------------------------------------------------ */
+void prepare(Prepared &p, const std::string &netlist, const std::vector<std::string> &probeNames,
+             int outcap, int capmax)
+{
+    p.ckt = parse_netlist(netlist);
+    compile(*p.ckt, p.img);
+    std::vector<int> probes;
+    if (probeNames.empty()) {
+        for (int i = 1; i <= p.img.n; i++)
+            probes.push_back(i);
+    } else {
+        for (auto &nm : probeNames) {
+            int id = -1;
+            for (int i = 0; i < p.img.n; i++)
+                if (p.img.names[i] == nm)
+                    id = i + 1;
+            if (id < 0)
+                throw NetlistError("unknown probe " + nm);
+            probes.push_back(id);
+        }
+    }
+    p.probes = probes;
+    p.dev = std::make_unique<DeviceCircuit>();
+    p.dev->upload(p.img, probes, outcap, capmax);
+    p.dev->upload_lu(p.img);     /* empty plan: the first iteration asks for one */
+}
+
+/* Run .tran on all circuits: launch; circuits that paused for a re-pivot
+ * get new pivots from the matrix they stamped and resume in the next
+ * launch, until every circuit has finished. */
+int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *seconds,
+              int *launches)
+{
+    std::vector<Prepared *> pending(cs.begin(), cs.end());
+    int mode = 0;   /* RUN_FRESH */
+    double total = 0;
+    int nl = 0;
+    ngsf_ckt_t *d = nullptr;
+    ck(cudaMalloc(&d, std::max<size_t>(1, cs.size()) * sizeof(ngsf_ckt_t)), "cudaMalloc(descs)");
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    try {
+        while (!pending.empty()) {
+            if (nl > 64 + 8 * (int)cs.size())
+                throw std::runtime_error("too many re-pivot rounds");
+            std::vector<ngsf_ckt_t> descs;
+            for (auto *c : pending)
+                descs.push_back(c->dev->desc());
+            ck(cudaMemcpy(d, descs.data(), descs.size() * sizeof(ngsf_ckt_t),
+                          cudaMemcpyHostToDevice), "cudaMemcpy(descs)");
+            cudaEventRecord(e0, 0);
+            ck(ngsf_launch_tran(d, (int)descs.size(), mode, maxSteps, 0), "launch(tran)");
+            cudaEventRecord(e1, 0);
+            ck(cudaEventSynchronize(e1), "tran");
+            float ms = 0;
+            cudaEventElapsedTime(&ms, e0, e1);
+            total += ms * 1e-3;
+            nl++;
+            std::vector<Prepared *> next;
+            for (auto *c : pending) {
+                c->dev->read_results(c->ires, c->fres);
+                if (c->ires[NGSF_R_STATUS] == NGSF_NEED_REORDER) {
+                    std::vector<double> ax = c->dev->read_ax();
+                    /* the factorization sees gmin on the diagonal (LoadGmin) */
+                    double dg = c->fres[NGSF_F_DIAGGMIN];
+                    if (dg != 0.0)
+                        for (int j = 0; j < c->img.n; j++)
+                            if (c->img.a_diag[j] >= 0)
+                                ax[c->img.a_diag[j]] += dg;
+                    std::string err;
+                    if (!plan_lu(c->img.n, c->img.a_cp, c->img.a_ri, ax, c->img.opt.pivrel,
+                                 c->img.opt.pivtol, c->img, err)) {
+                        c->ires[NGSF_R_STATUS] = NGSF_E_SINGULAR;
+                        continue;
+                    }
+                    c->dev->upload_lu(c->img);
+                    next.push_back(c);
+                } else {
+                    c->dev->read_points(c->ires[NGSF_R_NPOINTS], c->points);
+                }
+            }
+            pending.swap(next);
+            mode = 1;   /* RUN_RESUME */
+        }
+    } catch (...) {
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        cudaFree(d);
+        throw;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(d);
+    if (seconds)
+        *seconds = total;
+    if (launches)
+        *launches = nl;
+    return 0;
+}
+
+}  // namespace ngsf

@@ -1,0 +1,57 @@
+/* Host runtime of the GPU transient engine; see runtime.cpp. */
+#ifndef NGSF_RUNTIME_H
+#define NGSF_RUNTIME_H
+
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "circuit.h"
+#include "ngsf_types.h"
+
+namespace ngsf {
+
+class DeviceCircuit {
+public:
+    DeviceCircuit();
+    ~DeviceCircuit();
+    DeviceCircuit(const DeviceCircuit &) = delete;
+    DeviceCircuit &operator=(const DeviceCircuit &) = delete;
+
+    void upload(const Image &img, const std::vector<int> &probes, int outcap, int capmax);
+    void upload_lu(const Image &img);
+    std::vector<double> read_ax();
+    void read_results(std::vector<int> &ires, std::vector<double> &fres);
+    void read_points(int npoints, std::vector<double> &out);
+    void read_capture(int ncap, std::vector<double> &ax, std::vector<double> &rhs,
+                      std::vector<double> &meta);
+    const ngsf_ckt_t &desc() const;
+    ngsf_ckt_t *device_desc() const;
+    size_t bytes() const;
+
+private:
+    struct Impl;
+    Impl *impl;
+    std::vector<int> probes_;
+    int n_ = 0, nnz_ = 0, outcap_ = 0, capmax_ = 0;
+};
+
+/* A circuit compiled, pivoted and resident on the device. */
+struct Prepared {
+    std::unique_ptr<Circuit> ckt;
+    Image img;
+    std::vector<int> probes;
+    std::unique_ptr<DeviceCircuit> dev;
+    std::vector<int> ires;
+    std::vector<double> fres;
+    std::vector<double> points;   /* [npoints][1 + nprobe] */
+};
+
+void prepare(Prepared &p, const std::string &netlist, const std::vector<std::string> &probes,
+             int outcap, int capmax);
+int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *seconds,
+              int *launches = nullptr);
+
+}  // namespace ngsf
+
+#endif

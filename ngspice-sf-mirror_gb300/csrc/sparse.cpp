@@ -1,0 +1,302 @@
+/*
+ * Host symbolic + pivoting analysis of the circuit matrix (the SMPreorder /
+ * SMPpreOrder half of the SMP interface, src/maths/KLU/klusmp.c:753-806,
+ * 1256-1285).
+ *
+ * The reference factors with pivoting when NIiter asks for a reorder
+ * (MODEINITJCT, first MODEINITTRAN iteration; src/maths/ni/niiter.c:107-146)
+ * and re-factors on the fixed pivot sequence otherwise (klu_refactor).  Here
+ * the pivoting factorization runs once on the host on the first stamped
+ * matrix: a right-looking Markowitz elimination with threshold partial
+ * pivoting (a pivot must satisfy |a| >= pivrel * max|column| and
+ * |a| > pivtol, the PivRel / PivTol meaning of SMPreorder).  It yields the
+ * pivot sequence and the exact fill pattern of L and U.  The GPU then
+ * re-factors every Newton iteration on that fixed pattern (engine.cu),
+ * left-looking, one column per warp, columns grouped by dependency level.
+ */
+#include <algorithm>
+#include <cmath>
+#include <map>
+#include <set>
+#include <unordered_map>
+
+#include "circuit.h"
+#include "sparse.h"
+
+namespace ngsf {
+
+bool plan_lu(int n, const std::vector<int> &cp, const std::vector<int> &ri,
+             const std::vector<double> &ax, double pivrel, double pivtol,
+             Image &img, std::string &err)
+{
+    /* ---------------- numeric Markowitz elimination ------------------ */
+    std::vector<std::unordered_map<int, double>> rows(n);
+    std::vector<std::set<int>> cols(n);
+    for (int j = 0; j < n; j++)
+        for (int p = cp[j]; p < cp[j + 1]; p++) {
+            rows[ri[p]][j] += ax[p];
+            cols[j].insert(ri[p]);
+        }
+    std::set<std::pair<int, int>> colq;  /* (count, col) */
+    for (int j = 0; j < n; j++)
+        colq.insert({(int)cols[j].size(), j});
+    std::vector<int> prow(n), pcol(n);
+    std::vector<std::vector<int>> Lrows(n), Ucols(n);
+    std::vector<char> rowDone(n, 0), colDone(n, 0);
+
+    for (int k = 0; k < n; k++) {
+        long bestCost = -1;
+        int bp = -1, bq = -1;
+        double bmag = 0;
+        int examined = 0;
+        for (auto it = colq.begin(); it != colq.end(); ++it) {
+            int q = it->second;
+            int cc = it->first;
+            if (bestCost >= 0 && (examined >= 6 || (long)(cc - 1) * 0 >= bestCost))
+                break;
+            if (cc == 0)
+                continue;
+            double cmax = 0;
+            for (int i : cols[q])
+                cmax = std::max(cmax, std::fabs(rows[i][q]));
+            if (!(cmax > 0))
+                continue;
+            bool found = false;
+            for (int i : cols[q]) {
+                double a = std::fabs(rows[i][q]);
+                if (a < pivrel * cmax || a <= pivtol)
+                    continue;
+                long cost = (long)((int)rows[i].size() - 1) * (long)(cc - 1);
+                if (bestCost < 0 || cost < bestCost || (cost == bestCost && a > bmag)) {
+                    bestCost = cost;
+                    bp = i;
+                    bq = q;
+                    bmag = a;
+                }
+                found = true;
+            }
+            if (found)
+                examined++;
+            if (bestCost == 0)
+                break;
+        }
+        if (bp < 0) {
+            err = "singular matrix at elimination step " + std::to_string(k);
+            return false;
+        }
+        int p = bp, q = bq;
+        prow[k] = p;
+        pcol[k] = q;
+        double d = rows[p][q];
+        /* U row k: columns of row p except q */
+        for (auto &e : rows[p])
+            if (e.first != q)
+                Ucols[k].push_back(e.first);
+        std::sort(Ucols[k].begin(), Ucols[k].end());
+        /* L column k: rows of column q except p */
+        for (int i : cols[q])
+            if (i != p)
+                Lrows[k].push_back(i);
+        /* Schur update */
+        for (int i : Lrows[k]) {
+            double l = rows[i][q] / d;
+            for (auto &e : rows[p]) {
+                int j = e.first;
+                if (j == q)
+                    continue;
+                auto f = rows[i].find(j);
+                if (f == rows[i].end()) {
+                    rows[i][j] = -l * e.second;
+                    colq.erase({(int)cols[j].size(), j});
+                    cols[j].insert(i);
+                    colq.insert({(int)cols[j].size(), j});
+                } else {
+                    f->second -= l * e.second;
+                }
+            }
+        }
+        /* remove pivot row and column from the active matrix */
+        for (auto &e : rows[p]) {
+            int j = e.first;
+            colq.erase({(int)cols[j].size(), j});
+            cols[j].erase(p);
+            if (j != q)
+                colq.insert({(int)cols[j].size(), j});
+        }
+        for (int i : Lrows[k])
+            rows[i].erase(q);
+        colq.erase({(int)cols[q].size(), q});
+        cols[q].clear();
+        rows[p].clear();
+        rowDone[p] = colDone[q] = 1;
+    }
+
+    /* ---------------- LU layout in pivot order ----------------------- */
+    std::vector<int> rpos(n), cpos(n);
+    for (int k = 0; k < n; k++) {
+        rpos[prow[k]] = k;
+        cpos[pcol[k]] = k;
+    }
+    /* column k: U rows m<k (sorted), diagonal, L rows i>k (sorted) */
+    std::vector<std::vector<int>> ucol(n), lcol(n);
+    for (int m = 0; m < n; m++)
+        for (int j : Ucols[m])
+            ucol[cpos[j]].push_back(m);
+    for (int k = 0; k < n; k++) {
+        for (int i : Lrows[k])
+            lcol[k].push_back(rpos[i]);
+        std::sort(lcol[k].begin(), lcol[k].end());
+        std::sort(ucol[k].begin(), ucol[k].end());
+    }
+    img.cbeg.assign(n, 0);
+    img.cdiag.assign(n, 0);
+    img.cend.assign(n, 0);
+    int pos = 0;
+    for (int k = 0; k < n; k++) {
+        img.cbeg[k] = pos;
+        pos += (int)ucol[k].size();
+        img.cdiag[k] = pos;
+        pos += 1;
+        pos += (int)lcol[k].size();
+        img.cend[k] = pos;
+    }
+    img.nlu = pos;
+    auto posIn = [&](int k, int row) -> int {
+        if (row == k)
+            return img.cdiag[k];
+        if (row < k) {
+            auto it = std::lower_bound(ucol[k].begin(), ucol[k].end(), row);
+            if (it == ucol[k].end() || *it != row)
+                return -1;
+            return img.cbeg[k] + (int)(it - ucol[k].begin());
+        }
+        auto it = std::lower_bound(lcol[k].begin(), lcol[k].end(), row);
+        if (it == lcol[k].end() || *it != row)
+            return -1;
+        return img.cdiag[k] + 1 + (int)(it - lcol[k].begin());
+    };
+
+    /* A entries -> LU positions */
+    img.a_lupos.assign(ri.size(), -1);
+    for (int j = 0; j < n; j++)
+        for (int p = cp[j]; p < cp[j + 1]; p++) {
+            int q = posIn(cpos[j], rpos[ri[p]]);
+            if (q < 0) {
+                err = "internal: matrix entry missing from the LU pattern";
+                return false;
+            }
+            img.a_lupos[p] = q;
+        }
+
+    /* left-looking update lists and column levels */
+    std::vector<int> level(n, 0);
+    img.kptr.assign(n + 1, 0);
+    img.kdep.clear();
+    img.kpos.clear();
+    img.kseg.clear();
+    img.upd_dst.clear();
+    img.upd_src.clear();
+    img.kseg.push_back(0);
+    double flops = 0;
+    for (int k = 0; k < n; k++) {
+        int lv = 0;
+        for (size_t t = 0; t < ucol[k].size(); t++) {
+            int m = ucol[k][t];
+            lv = std::max(lv, level[m] + 1);
+            img.kdep.push_back(m);
+            img.kpos.push_back(img.cbeg[k] + (int)t);
+            for (size_t s = 0; s < lcol[m].size(); s++) {
+                int i = lcol[m][s];
+                int dst = posIn(k, i);
+                if (dst < 0) {
+                    err = "internal: fill closure violated";
+                    return false;
+                }
+                img.upd_dst.push_back(dst);
+                img.upd_src.push_back(img.cdiag[m] + 1 + (int)s);
+            }
+            flops += (double)lcol[m].size();
+            img.kseg.push_back((int)img.upd_dst.size());
+        }
+        flops += (double)lcol[k].size();
+        level[k] = lv;
+        img.kptr[k + 1] = (int)img.kdep.size();
+    }
+    img.lu_flops = flops;
+    int nlev = 0;
+    for (int k = 0; k < n; k++)
+        nlev = std::max(nlev, level[k] + 1);
+    img.lvl_ptr.assign(nlev + 1, 0);
+    for (int k = 0; k < n; k++)
+        img.lvl_ptr[level[k] + 1]++;
+    for (int l = 0; l < nlev; l++)
+        img.lvl_ptr[l + 1] += img.lvl_ptr[l];
+    img.lvl_col.assign(n, 0);
+    {
+        std::vector<int> fill(img.lvl_ptr.begin(), img.lvl_ptr.end() - 1);
+        for (int k = 0; k < n; k++)
+            img.lvl_col[fill[level[k]]++] = k;
+    }
+
+    /* triangular solves, row oriented in pivot order */
+    std::vector<std::vector<std::pair<int, int>>> lrow(n), urow(n);
+    for (int m = 0; m < n; m++) {
+        for (size_t s = 0; s < lcol[m].size(); s++)
+            lrow[lcol[m][s]].push_back({m, img.cdiag[m] + 1 + (int)s});
+        for (size_t t = 0; t < ucol[m].size(); t++)
+            urow[ucol[m][t]].push_back({m, img.cbeg[m] + (int)t});
+    }
+    img.lr_ptr.assign(n + 1, 0);
+    img.ur_ptr.assign(n + 1, 0);
+    img.lr_col.clear();
+    img.lr_pos.clear();
+    img.ur_col.clear();
+    img.ur_pos.clear();
+    std::vector<int> fl(n, 0), bl(n, 0);
+    for (int k = 0; k < n; k++) {
+        std::sort(lrow[k].begin(), lrow[k].end());
+        for (auto &e : lrow[k]) {
+            img.lr_col.push_back(e.first);
+            img.lr_pos.push_back(e.second);
+            fl[k] = std::max(fl[k], fl[e.first] + 1);
+        }
+        img.lr_ptr[k + 1] = (int)img.lr_col.size();
+    }
+    for (int k = 0; k < n; k++) {
+        std::sort(urow[k].begin(), urow[k].end());
+        for (auto &e : urow[k]) {
+            img.ur_col.push_back(e.first);
+            img.ur_pos.push_back(e.second);
+        }
+        img.ur_ptr[k + 1] = (int)img.ur_col.size();
+    }
+    for (int k = n - 1; k >= 0; k--)
+        for (auto &e : urow[k])
+            bl[k] = std::max(bl[k], bl[e.first] + 1);
+    auto group = [&](const std::vector<int> &lv, std::vector<int> &ptr, std::vector<int> &idx) {
+        int nl = 0;
+        for (int k = 0; k < n; k++)
+            nl = std::max(nl, lv[k] + 1);
+        ptr.assign(nl + 1, 0);
+        for (int k = 0; k < n; k++)
+            ptr[lv[k] + 1]++;
+        for (int l = 0; l < nl; l++)
+            ptr[l + 1] += ptr[l];
+        idx.assign(n, 0);
+        std::vector<int> f(ptr.begin(), ptr.end() - 1);
+        for (int k = 0; k < n; k++)
+            idx[f[lv[k]]++] = k;
+    };
+    group(fl, img.fl_ptr, img.fl_row);
+    group(bl, img.bl_ptr, img.bl_row);
+
+    img.prow.resize(n);
+    img.pcol.resize(n);
+    for (int k = 0; k < n; k++) {
+        img.prow[k] = prow[k] + 1;
+        img.pcol[k] = pcol[k] + 1;
+    }
+    return true;
+}
+
+}  // namespace ngsf

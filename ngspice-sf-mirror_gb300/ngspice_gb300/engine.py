@@ -1,0 +1,174 @@
+"""ctypes binding of libngspice_gb300.so (include/ngspice_gb300.h and
+include/sharedspice.h).
+
+The library is the product: this module only loads it and converts
+arguments.  There is no CPU fallback: if the library or a CUDA device is
+missing, the calls fail with the library's error message.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "lib", "libngspice_gb300.so")
+
+# integer result slots (ngsf_types.h NGSF_R_*)
+R_STATUS, R_NPOINTS, R_ACCEPTED, R_REJECTED, R_NUMITER, R_TRANITER, R_TIMEPTS, \
+    R_NCAP, R_OPITER, R_BADPIVOT, R_REORDERS = range(11)
+R_COUNT = 11
+
+# C-ABI symbols declared in include/*.h
+EXPORTS = [
+    "ngsf_open", "ngsf_compile", "ngsf_close", "ngsf_last_error", "ngsf_info",
+    "ngsf_eq_name", "ngsf_pattern", "ngsf_probes", "ngsf_run", "ngsf_results",
+    "ngsf_points", "ngsf_capture", "ngsf_lu_flops", "ngsf_device_bytes",
+    "ngSpice_Init", "ngSpice_Init_Sync", "ngSpice_Command", "ngGet_Vec_Info",
+    "ngSpice_Circ", "ngSpice_CurPlot", "ngSpice_AllPlots", "ngSpice_AllVecs",
+    "ngSpice_running", "ngSpice_SetBkpt", "ngSpice_nospinit", "ngSpice_nospiceinit",
+    "ngSpice_LockRealloc", "ngSpice_UnlockRealloc", "ngSpice_Reset",
+]
+
+_lib = None
+
+
+class EngineError(RuntimeError):
+    pass
+
+
+def lib(path: str | None = None) -> C.CDLL:
+    """Load (once) and type the shared library."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    p = path or LIB_PATH
+    if not os.path.exists(p):
+        raise EngineError(f"{p} is missing: build it with ngspice_gb300.build.build()")
+    L = C.CDLL(p)
+    vp, ip, dp, cp = C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_char_p
+    L.ngsf_open.restype = vp
+    L.ngsf_open.argtypes = [cp, cp, C.c_int, C.c_int]
+    L.ngsf_compile.restype = vp
+    L.ngsf_compile.argtypes = [cp]
+    L.ngsf_close.argtypes = [vp]
+    L.ngsf_last_error.restype = cp
+    L.ngsf_info.argtypes = [vp, ip, ip, ip, ip]
+    L.ngsf_eq_name.argtypes = [vp, C.c_int, cp, C.c_int]
+    L.ngsf_pattern.argtypes = [vp, ip, ip]
+    L.ngsf_probes.argtypes = [vp, ip, C.c_int]
+    L.ngsf_run.argtypes = [C.POINTER(vp), C.c_int, C.c_longlong, dp]
+    L.ngsf_results.argtypes = [vp, ip, dp]
+    L.ngsf_points.argtypes = [vp, dp, C.c_int]
+    L.ngsf_capture.argtypes = [vp, dp, dp, dp, dp, C.c_int]
+    L.ngsf_lu_flops.restype = C.c_double
+    L.ngsf_lu_flops.argtypes = [vp]
+    L.ngsf_device_bytes.restype = C.c_longlong
+    L.ngsf_device_bytes.argtypes = [vp]
+    _lib = L
+    return L
+
+
+def last_error() -> str:
+    return (lib().ngsf_last_error() or b"").decode()
+
+
+def _ptr(a: np.ndarray, ct):
+    return a.ctypes.data_as(C.POINTER(ct))
+
+
+class Circuit:
+    """One compiled circuit (device resident unless host_only)."""
+
+    def __init__(self, netlist: str, probes: list[str] | None = None, outcap: int = 200000,
+                 capmax: int = 0, host_only: bool = False):
+        L = lib()
+        if host_only:
+            h = L.ngsf_compile(netlist.encode())
+        else:
+            pr = " ".join(probes).encode() if probes else None
+            h = L.ngsf_open(netlist.encode(), pr, int(outcap), int(capmax))
+        if not h:
+            raise EngineError(last_error())
+        self._h = C.c_void_p(h)
+        n, nnz, ns, nlu = C.c_int(), C.c_int(), C.c_int(), C.c_int()
+        L.ngsf_info(self._h, C.byref(n), C.byref(nnz), C.byref(ns), C.byref(nlu))
+        self.n, self.nnz, self.nstates, self.nlu = n.value, nnz.value, ns.value, nlu.value
+        self.host_only = host_only
+
+    def close(self):
+        if self._h:
+            lib().ngsf_close(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self):
+        return self._h
+
+    def names(self) -> list[str]:
+        buf = C.create_string_buffer(512)
+        out = []
+        for i in range(1, self.n + 1):
+            lib().ngsf_eq_name(self._h, i, buf, 512)
+            out.append(buf.value.decode())
+        return out
+
+    def pattern(self) -> tuple[np.ndarray, np.ndarray]:
+        cp = np.zeros(self.n + 1, np.int32)
+        ri = np.zeros(self.nnz, np.int32)
+        lib().ngsf_pattern(self._h, _ptr(cp, C.c_int), _ptr(ri, C.c_int))
+        return cp, ri
+
+    def probes(self) -> np.ndarray:
+        buf = np.zeros(self.n + 1, np.int32)
+        k = lib().ngsf_probes(self._h, _ptr(buf, C.c_int), self.n + 1)
+        return buf[:k].copy()
+
+    def results(self) -> np.ndarray:
+        ires = np.zeros(R_COUNT, np.int32)
+        fres = np.zeros(2)
+        if lib().ngsf_results(self._h, _ptr(ires, C.c_int), _ptr(fres, C.c_double)):
+            raise EngineError(last_error())
+        return ires
+
+    def points(self) -> tuple[np.ndarray, np.ndarray]:
+        """(times[np], values[np, nprobe]) of the accepted points."""
+        ires = self.results()
+        npts = int(ires[R_NPOINTS])
+        w = 1 + len(self.probes())
+        buf = np.zeros((max(npts, 1), w))
+        k = lib().ngsf_points(self._h, _ptr(buf, C.c_double), npts)
+        return buf[:k, 0].copy(), buf[:k, 1:].copy()
+
+    def capture(self, maxcap: int) -> dict:
+        ax = np.zeros((maxcap, self.nnz))
+        rhs = np.zeros((maxcap, self.n + 1))
+        rhsold = np.zeros((maxcap, self.n + 1))
+        meta = np.zeros((maxcap, 4))
+        k = lib().ngsf_capture(self._h, _ptr(ax, C.c_double), _ptr(rhs, C.c_double),
+                               _ptr(rhsold, C.c_double), _ptr(meta, C.c_double), maxcap)
+        if k < 0:
+            raise EngineError(last_error())
+        return {"ax": ax[:k], "rhs": rhs[:k], "rhsold": rhsold[:k], "meta": meta[:k]}
+
+    def lu_flops(self) -> float:
+        return float(lib().ngsf_lu_flops(self._h))
+
+    def device_bytes(self) -> int:
+        return int(lib().ngsf_device_bytes(self._h))
+
+
+def run(circuits: list[Circuit], max_steps: int = 0) -> float:
+    """Run .tran on all circuits in one GPU launch; returns device seconds."""
+    arr = (C.c_void_p * len(circuits))(*[c.handle for c in circuits])
+    sec = C.c_double(0)
+    if lib().ngsf_run(arr, len(circuits), int(max_steps), C.byref(sec)):
+        raise EngineError(last_error())
+    return sec.value
