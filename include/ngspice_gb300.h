@@ -71,6 +71,12 @@ NGSF_API int ngsf_capture(ngsf_handle *h, double *ax, double *rhs, double *rhsol
                           double *meta, int maxcap);
 /* floating-point operations of one LU refactorization (multiply-adds) */
 NGSF_API double ngsf_lu_flops(const ngsf_handle *h);
+/* kernel launches made by the last ngsf_run on this thread (the time loop
+ * pauses for host re-pivoting where the reference re-factors) */
+NGSF_API int ngsf_last_launches(void);
+/* instance counts for roofline accounting: counts[10] = mos1, res, cap,
+ * vsrc, isrc, matrix nonzeros, L+U nonzeros, unknowns, bsim4, diode */
+NGSF_API int ngsf_workload(const ngsf_handle *h, long long *counts);
 /* device bytes held by the circuit */
 NGSF_API long long ngsf_device_bytes(const ngsf_handle *h);
 

@@ -33,6 +33,7 @@ struct ngsf_handle {
 
 namespace {
 thread_local std::string g_err;
+thread_local int g_launches = 0;
 
 int fail(const std::string &msg, int code = -1)
 {
@@ -134,7 +135,7 @@ NGSF_API int ngsf_run(ngsf_handle *const *hs, int count, long long max_steps, do
                 return fail("circuit was compiled without a device (ngsf_compile)");
             cs.push_back(&hs[i]->p);
         }
-        run_batch(cs, max_steps > 0 ? max_steps : 100000000LL, seconds);
+        run_batch(cs, max_steps > 0 ? max_steps : 100000000LL, seconds, &g_launches);
         return 0;
     } catch (const std::exception &e) {
         return fail(e.what());
@@ -198,6 +199,26 @@ NGSF_API int ngsf_capture(ngsf_handle *h, double *ax, double *rhs, double *rhsol
 }
 
 NGSF_API double ngsf_lu_flops(const ngsf_handle *h) { return h ? h->p.img.lu_flops : 0.0; }
+
+NGSF_API int ngsf_last_launches(void) { return g_launches; }
+
+NGSF_API int ngsf_workload(const ngsf_handle *h, long long *counts)
+{
+    if (!h)
+        return fail("null handle");
+    const Image &m = h->p.img;
+    counts[0] = m.nmos1;
+    counts[1] = m.nres;
+    counts[2] = m.ncap;
+    counts[3] = m.nvsrc;
+    counts[4] = m.nisrc;
+    counts[5] = (long long)m.a_ri.size();
+    counts[6] = m.nlu;
+    counts[7] = m.n;
+    counts[8] = 0;   /* BSIM4 instances */
+    counts[9] = m.ndio;
+    return 0;
+}
 
 NGSF_API long long ngsf_device_bytes(const ngsf_handle *h)
 {

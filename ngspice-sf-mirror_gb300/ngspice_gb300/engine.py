@@ -25,6 +25,7 @@ EXPORTS = [
     "ngsf_open", "ngsf_compile", "ngsf_close", "ngsf_last_error", "ngsf_info",
     "ngsf_eq_name", "ngsf_pattern", "ngsf_probes", "ngsf_run", "ngsf_results",
     "ngsf_points", "ngsf_capture", "ngsf_lu_flops", "ngsf_device_bytes",
+    "ngsf_last_launches", "ngsf_workload",
     "ngSpice_Init", "ngSpice_Init_Sync", "ngSpice_Command", "ngGet_Vec_Info",
     "ngSpice_Circ", "ngSpice_CurPlot", "ngSpice_AllPlots", "ngSpice_AllVecs",
     "ngSpice_running", "ngSpice_SetBkpt", "ngSpice_nospinit", "ngSpice_nospiceinit",
@@ -66,6 +67,8 @@ def lib(path: str | None = None) -> C.CDLL:
     L.ngsf_lu_flops.argtypes = [vp]
     L.ngsf_device_bytes.restype = C.c_longlong
     L.ngsf_device_bytes.argtypes = [vp]
+    L.ngsf_last_launches.restype = C.c_int
+    L.ngsf_workload.argtypes = [vp, C.POINTER(C.c_longlong)]
     _lib = L
     return L
 
@@ -163,6 +166,16 @@ class Circuit:
 
     def device_bytes(self) -> int:
         return int(lib().ngsf_device_bytes(self._h))
+
+    def workload(self) -> dict:
+        a = (C.c_longlong * 10)()
+        lib().ngsf_workload(self._h, a)
+        keys = ["mos1", "res", "cap", "vsrc", "isrc", "nnz", "nlu", "n", "bsim4", "dio"]
+        return dict(zip(keys, [int(x) for x in a]))
+
+
+def last_launches() -> int:
+    return int(lib().ngsf_last_launches())
 
 
 def run(circuits: list[Circuit], max_steps: int = 0) -> float:

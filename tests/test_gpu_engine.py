@@ -1,0 +1,121 @@
+"""GPU: the CUDA transient engine against the reference golden fixtures and
+the CPU oracle port, through the C ABI."""
+import numpy as np
+import pytest
+
+import port
+from conftest import golden
+from tolerances import matrix_violation, rhs_violation, waveform_violation
+
+pytestmark = pytest.mark.gpu
+
+CASES = ["rc_ladder", "inverter_chain32"]
+
+
+@pytest.fixture(scope="module")
+def E(built_lib):
+    from ngspice_gb300 import engine
+    return engine
+
+
+def run_one(E, text, capmax=0, **kw):
+    c = E.Circuit(text, capmax=capmax, **kw)
+    E.run([c], max_steps=1_000_000)
+    return c
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_tran_matches_reference(E, name):
+    g = golden(name)
+    c = run_one(E, str(g["netlist"]))
+    r = c.results()
+    ref = g["stats"]
+    assert r[E.R_STATUS] == 0
+    assert r[E.R_ACCEPTED] == ref[3]
+    assert r[E.R_REJECTED] == ref[4]
+    assert r[E.R_TRANITER] == ref[1]
+    t, v = c.points()
+    np.testing.assert_array_equal(t, g["times"])
+    assert waveform_violation(c.names(), g["times"], g["values"], t, v) < 0.01
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_newton_iterations_stamp_like_reference(E, name):
+    """Per-iteration stamped matrix and right-hand side against the reference
+    dump, from the first transient iteration on (the operating-point Newton
+    path may take a different number of gmin steps when its iterates are
+    chaotic, but it converges to the same point)."""
+    g = golden(name)
+    k = len(g["it_kind"])
+    c = run_one(E, str(g["netlist"]), capmax=k + 400)
+    cap = c.capture(k + 400)
+    cp, ri = c.pattern()
+    ref_modes = g["it_meta"][:, 2].astype(int)
+    my_modes = cap["meta"][:, 2].astype(int)
+    r0 = int(np.argmax(ref_modes & 0x1000))
+    m0 = int(np.argmax(my_modes & 0x1000))
+    if name == "rc_ladder":
+        assert r0 == m0            # linear circuit: identical OP path
+    n = c.n
+    checked = 0
+    for i in range(k - r0):
+        kr, km = r0 + i, m0 + i
+        if km >= len(cap["ax"]):
+            break
+        assert g["it_meta"][kr][0] == cap["meta"][km][0]      # same time point
+        assert ref_modes[kr] == my_modes[km]                  # same mode
+        p0, p1 = g["it_ptr"][kr], g["it_ptr"][kr + 1]
+        assert matrix_violation(g["it_rows"][p0:p1], g["it_cols"][p0:p1],
+                                g["it_vals"][p0:p1], cp, ri, cap["ax"][km]) <= 1.0
+        assert rhs_violation(g["it_rhs"][kr][1:n + 1], cap["rhs"][km][1:n + 1]) <= 1.0
+        checked += 1
+    assert checked > 20
+
+
+def test_engine_matches_oracle_port(E):
+    """A circuit with no golden fixture: GPU against the CPU oracle port."""
+    from ngspice_gb300 import netlists
+    text = netlists.inverter_chain(stages=12, tstop="8n", load="35f")
+    c = run_one(E, text)
+    o = port.simulate(text)
+    r = c.results()
+    assert r[E.R_ACCEPTED] == o["stats"]["accepted"]
+    t, v = c.points()
+    np.testing.assert_array_equal(t, o["times"])
+    assert waveform_violation(c.names(), o["times"], o["values"], t, v) < 0.01
+
+
+def test_batch_equals_single_runs(E):
+    """Circuits of different size in one launch give bit-identical results
+    to the same circuits run alone (each block owns its circuit)."""
+    from ngspice_gb300 import netlists
+    texts = [netlists.inverter_chain(stages=s, tstop="4n") for s in (4, 9, 16)]
+    texts.append(str(golden("rc_ladder")["netlist"]))
+    alone = [run_one(E, t) for t in texts]
+    batch = [E.Circuit(t) for t in texts]
+    E.run(batch, max_steps=1_000_000)
+    for a, b in zip(alone, batch):
+        ta, va = a.points()
+        tb, vb = b.points()
+        np.testing.assert_array_equal(ta, tb)
+        np.testing.assert_array_equal(va, vb)
+
+
+def test_step_budget_stops_with_status(E):
+    g = golden("inverter_chain32")
+    c = E.Circuit(str(g["netlist"]))
+    E.run([c], max_steps=50)
+    r = c.results()
+    assert r[E.R_STATUS] == 121          # step budget exhausted, no hang
+    assert 0 < r[E.R_ACCEPTED] <= 51
+
+
+def test_probe_subset(E):
+    g = golden("inverter_chain32")
+    c = E.Circuit(str(g["netlist"]), probes=["n32", "n1"])
+    E.run([c], max_steps=1_000_000)
+    t, v = c.points()
+    names = list(g["names"])
+    ref = g["values"][:, [names.index("n32"), names.index("n1")]]
+    np.testing.assert_array_equal(t, g["times"])
+    assert np.max(np.abs(v - ref)) < 1e-9

@@ -1,0 +1,57 @@
+"""CPU: the product library loads, exports its C ABI, and its host compiler
+numbers equations and lays out the matrix exactly as the reference does."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, golden
+
+
+def declared_symbols():
+    names = set()
+    for h in ("sharedspice.h", "ngspice_gb300.h"):
+        text = open(os.path.join(ROOT, "include", h)).read()
+        names |= set(re.findall(r"\b(ng[A-Za-z_]+)\s*\(", text))
+    return {n for n in names if not n.startswith("ngcomplex")}
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    lib = ctypes.CDLL(built_lib)
+    missing = [s for s in sorted(declared_symbols()) if not hasattr(lib, s)]
+    assert not missing, missing
+    from ngspice_gb300 import engine
+    assert set(engine.EXPORTS) <= declared_symbols()
+
+
+@pytest.mark.parametrize("name", ["rc_ladder", "inverter_chain32"])
+def test_equation_names_and_pattern_match_reference(built_lib, name):
+    from ngspice_gb300 import engine as E
+    g = golden(name)
+    c = E.Circuit(str(g["netlist"]), host_only=True)
+    assert c.names() == list(g["names"])
+    cp, ri = c.pattern()
+    mine = {(int(ri[p]), j) for j in range(c.n) for p in range(cp[j], cp[j + 1])}
+    p0, p1 = g["it_ptr"][0], g["it_ptr"][1]
+    ref = set(zip(g["it_rows"][p0:p1].tolist(), g["it_cols"][p0:p1].tolist()))
+    assert mine == ref
+
+
+def test_unsupported_input_is_reported(built_lib):
+    from ngspice_gb300 import engine as E
+    with pytest.raises(E.EngineError, match="unsupported element"):
+        E.Circuit("t\nq1 c b e qmod\n.tran 1n 10n\n.end\n", host_only=True)
+    with pytest.raises(E.EngineError, match="no .tran"):
+        E.Circuit("t\nr1 a 0 1k\nv1 a 0 1\n.end\n", host_only=True)
+    with pytest.raises(E.EngineError, match="shorted VSRC"):
+        E.Circuit("t\nv1 a a 1\nr1 a 0 1\n.tran 1n 2n\n.end\n", host_only=True)
+
+
+def test_run_refuses_host_only_circuit(built_lib):
+    from ngspice_gb300 import engine as E
+    g = golden("rc_ladder")
+    c = E.Circuit(str(g["netlist"]), host_only=True)
+    with pytest.raises(E.EngineError, match="without a device"):
+        E.run([c])
