@@ -39,14 +39,15 @@ BYTES_CAP = 136
 BYTES_SRC = 120
 
 
-def workload_text(name: str) -> tuple[str, dict]:
+def workload_text(name: str, tstop: str | None = None) -> tuple[str, dict]:
     from ngspice_gb300 import netlists
     if name == "c0":
-        return netlists.inverter_chain(), {
+        tstop = tstop or "20n"
+        return netlists.inverter_chain(tstop=tstop), {
             "circuit": "32-stage MOS1 CMOS inverter chain (level 1, VTO +-0.7 V, KP 110/50 uA/V^2,"
                        " LAMBDA 0.04, W/L 2u/1u and 4u/1u, VDD 3.3 V, 20 fF loads,"
                        " PULSE(0 3.3 0 100p 100p 2n 4n))",
-            "tran": ".tran 10p 20n"}
+            "tran": f".tran 10p {tstop}"}
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -255,10 +256,12 @@ def main():
     ap.add_argument("--instances", type=int, default=1216)
     ap.add_argument("--cpu-sample", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--tstop", default=None,
+                    help="shorter .tran stop time (small cases for profiling)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
-    text, tdesc = workload_text(args.workload)
+    text, tdesc = workload_text(args.workload, args.tstop)
     wdesc = {"workload": f"{args.workload.upper()}: {tdesc['circuit']}, {tdesc['tran']},"
                          f" {args.instances} independent instances per launch",
              "instances_per_gpu": args.instances, "l2": "flushed between timed steps",

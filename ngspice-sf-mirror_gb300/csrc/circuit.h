@@ -113,6 +113,10 @@ struct Image {
     int n = 0, nstates = 0, nstamp = 0, nlu = 0;
     ngsf_opts_t opt{};
     /* devices */
+    int nb4 = 0;
+    std::vector<int> b4_node, b4_st;
+    std::vector<double> b4_p;
+    int b4_stamp0 = 0;
     int nmos1 = 0, ndio = 0, nres = 0, ncap = 0, nvsrc = 0, nisrc = 0;
     std::vector<int> mos1_node, mos1_st;
     std::vector<double> mos1_p;
@@ -145,6 +149,10 @@ struct Image {
     double lu_flops = 0;   /* multiply-adds of one refactorization */
     std::vector<std::string> names;  /* equation names 1..n */
 };
+
+/* BSIM4 instance resolution (bsim4_setup.cpp): fills B4P_COUNT values. */
+void bsim4_params(const Circuit &c, const Model &m, const Instance &in, double *p,
+                  bool &needDp, bool &needSp);
 
 /* CKTsetup + CKTtemp + SMPpreOrder equivalent. */
 void compile(Circuit &c, Image &img);

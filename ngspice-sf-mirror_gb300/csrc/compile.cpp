@@ -19,6 +19,7 @@
 #include <functional>
 #include <numeric>
 
+#include "bsim4.h"
 #include "circuit.h"
 
 namespace ngsf {
@@ -295,13 +296,27 @@ void compile(Circuit &c, Image &img)
 
     /* ---------------- setup: internal nodes, branches, states -------- */
     std::vector<std::array<double, M1P_COUNT>> m1p;
+    std::vector<std::array<double, B4P_COUNT>> b4p;
     int states = 0;
     for (int kind = 0; kind < K_COUNT; kind++) {
         for (int idx : c.order[kind]) {
             Instance &in = c.inst[idx];
             switch (kind) {
-            case K_BSIM4:
-                throw NetlistError("BSIM4 instance " + in.name + ": device kind not built");
+            case K_BSIM4: {
+                /* BSIM4setup: state chunk, then internal drain/source nodes
+                 * (b4set.c:2317-2530) */
+                in.states = states;
+                states += B4S_COUNT;
+                std::array<double, B4P_COUNT> p{};
+                bool needDp, needSp;
+                bsim4_params(c, c.models[in.model], in, p.data(), needDp, needSp);
+                int d = in.nodes[0], g = in.nodes[1], s = in.nodes[2], b = in.nodes[3];
+                int dp = needDp ? mk_internal(c, in.name + "#drain", true) : d;
+                int sp = needSp ? mk_internal(c, in.name + "#source", true) : s;
+                in.inodes = {d, g, s, b, dp, sp};
+                b4p.push_back(p);
+                break;
+            }
             case K_DIO:
                 throw NetlistError("diode instance " + in.name + ": device kind not built");
             case K_CAP:
@@ -360,7 +375,49 @@ void compile(Circuit &c, Image &img)
         return base;
     };
 
-    /* CAP (kind order: bsim4, cap, dio, isrc, mos1, res, vsrc) */
+    /* BSIM4 (kind order: bsim4, cap, dio, isrc, mos1, res, vsrc).  Stamp
+     * sequence of BSIM4LoadRhsMat for the supported selectors
+     * (b4ld.c:5448-5620): rhs d' g' b' s', then the matrix terms. */
+    {
+        const auto &ord = c.order[K_BSIM4];
+        int nk = (int)ord.size();
+        img.nb4 = nk;
+        img.b4_node.assign(B4N_COUNT * nk, 0);
+        img.b4_st.assign(nk, 0);
+        img.b4_p.assign((size_t)B4P_COUNT * nk, 0.0);
+        for (int i = 0; i < nk; i++) {
+            const Instance &in = c.inst[ord[i]];
+            for (int t = 0; t < B4N_COUNT; t++)
+                img.b4_node[t * nk + i] = in.inodes[t];
+            img.b4_st[i] = in.states;
+            for (int t = 0; t < B4P_COUNT; t++)
+                img.b4_p[(size_t)t * nk + i] = b4p[i][t];
+        }
+        img.b4_stamp0 = add_kind(nk, B4_NSTAMP, [&](int i, int k) -> Stamp {
+            enum { D = B4N_D, G = B4N_G, S = B4N_S, B = B4N_B, DP = B4N_DP, SP = B4N_SP };
+            static const int pat[B4_NSTAMP][2] = {
+                {-1, DP}, {-1, G}, {-1, B}, {-1, SP},
+                /* GPgp GPdp GPsp GPbp */
+                {G, G}, {G, DP}, {G, SP}, {G, B},
+                /* DPdp DPd DPgp DPsp DPbp Ddp Dd */
+                {DP, DP}, {DP, D}, {DP, G}, {DP, SP}, {DP, B}, {D, DP}, {D, D},
+                /* SPdp SPgp SPsp SPs SPbp Ssp Ss */
+                {SP, DP}, {SP, G}, {SP, SP}, {SP, S}, {SP, B}, {S, SP}, {S, S},
+                /* BPdp BPgp BPsp BPbp */
+                {B, DP}, {B, G}, {B, SP}, {B, B},
+                /* GIDL: DPdp DPgp DPsp DPbp BPdp BPgp BPsp BPbp */
+                {DP, DP}, {DP, G}, {DP, SP}, {DP, B}, {B, DP}, {B, G}, {B, SP}, {B, B},
+                /* GISL: SPdp SPgp SPsp SPbp BPdp BPgp BPsp BPbp */
+                {SP, DP}, {SP, G}, {SP, SP}, {SP, B}, {B, DP}, {B, G}, {B, SP}, {B, B}};
+            int map[B4N_COUNT];
+            for (int t = 0; t < B4N_COUNT; t++)
+                map[t] = img.b4_node[t * nk + i];
+            if (pat[k][0] < 0)
+                return {-1, map[pat[k][1]]};
+            return {map[pat[k][0]], map[pat[k][1]]};
+        });
+    }
+    /* CAP */
     {
         const auto &ord = c.order[K_CAP];
         int nk = (int)ord.size();

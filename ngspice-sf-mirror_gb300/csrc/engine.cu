@@ -26,11 +26,9 @@
 #include <stdint.h>
 
 #include "ngsf_types.h"
+#include "devsup.cuh"
 
 #define NGSF_THREADS 256
-/* MIN / MAX exactly as the reference macros (src/include/ngspice/macros.h) */
-#define NG_MAX(a, b) ((a) > (b) ? (a) : (b))
-#define NG_MIN(a, b) ((a) < (b) ? (a) : (b))
 #define NGSF_WARPS (NGSF_THREADS / 32)
 
 namespace {
@@ -108,98 +106,6 @@ __device__ bool almost_equal_ulps(double a, double b, int maxUlps)
 /* ---------------------------------------------------------------- */
 /* device support (src/spicelib/devices/devsup.c)                   */
 /* ---------------------------------------------------------------- */
-__device__ double dev_limvds(double vnew, double vold)
-{
-    if (vold >= 3.5) {
-        if (vnew > vold)
-            vnew = NG_MIN(vnew, (3 * vold) + 2);
-        else if (vnew < 3.5)
-            vnew = NG_MAX(vnew, 2);
-    } else {
-        if (vnew > vold)
-            vnew = NG_MIN(vnew, 4);
-        else
-            vnew = NG_MAX(vnew, -.5);
-    }
-    return vnew;
-}
-
-__device__ double dev_pnjlim(double vnew, double vold, double vt, double vcrit, int *icheck)
-{
-    double arg;
-    if ((vnew > vcrit) && (fabs(vnew - vold) > (vt + vt))) {
-        if (vold > 0) {
-            arg = (vnew - vold) / vt;
-            if (arg > 0)
-                vnew = vold + vt * (2 + log(arg - 2));
-            else
-                vnew = vold - vt * (2 + log(2 - arg));
-        } else {
-            vnew = vt * log(vnew / vt);
-        }
-        *icheck = 1;
-    } else {
-        if (vnew < 0) {
-            if (vold > 0)
-                arg = -1 * vold - 1;
-            else
-                arg = 2 * vold - 1;
-            if (vnew < arg) {
-                vnew = arg;
-                *icheck = 1;
-            } else {
-                *icheck = 0;
-            }
-        } else {
-            *icheck = 0;
-        }
-    }
-    return vnew;
-}
-
-__device__ double dev_fetlim(double vnew, double vold, double vto)
-{
-    double vtsthi = fabs(2 * (vold - vto)) + 2;
-    double vtstlo = fabs(vold - vto) + 1;
-    double vtox = vto + 3.5;
-    double delv = vnew - vold;
-    if (vold >= vto) {
-        if (vold >= vtox) {
-            if (delv <= 0) {
-                if (vnew >= vtox) {
-                    if (-delv > vtstlo)
-                        vnew = vold - vtstlo;
-                } else {
-                    vnew = NG_MAX(vnew, vto + 2);
-                }
-            } else {
-                if (delv >= vtsthi)
-                    vnew = vold + vtsthi;
-            }
-        } else {
-            if (delv <= 0)
-                vnew = NG_MAX(vnew, vto - .5);
-            else
-                vnew = NG_MIN(vnew, vto + 4);
-        }
-    } else {
-        if (delv <= 0) {
-            if (-delv > vtsthi)
-                vnew = vold - vtsthi;
-        } else {
-            double vtemp = vto + .5;
-            if (vnew <= vtemp) {
-                if (delv > vtstlo)
-                    vnew = vold + vtstlo;
-            } else {
-                vnew = vtemp;
-            }
-        }
-    }
-    return vnew;
-}
-
-/* DEVqmeyer: Meyer gate capacitances (devsup.c:674-736) */
 __device__ void dev_qmeyer(double vgs, double vgd, double von, double vdsat,
                            double *capgs, double *capgd, double *capgb,
                            double phi, double cox)
@@ -857,10 +763,37 @@ __device__ int mos1_conv_one(const ngsf_ckt_t &C, const Iter &it, int i)
     return 0;
 }
 
+#include "bsim4_load.cuh"
+
+__device__ int bsim4_load_one(const ngsf_ckt_t &C, const Ctl &s, const Iter &it, int i)
+{
+    const ngsf_bsim4_t &K = C.bsim4;
+    const int n = K.n;
+    B4Ctx x;
+    x.mode = s.mode;
+    x.order = s.order;
+    x.gmin = s.gmin;
+    x.delta = s.delta;
+    x.deltaOld1 = s.deltaOld[1];
+    x.ag0 = s.ag[0];
+    x.ag1 = s.ag[1];
+    x.rhsOld = it.rhsOld;
+    x.st0 = it.st0;
+    x.st1 = const_cast<double *>(it.st1);
+    x.st2 = it.st2;
+    int node[B4N_COUNT];
+    for (int t = 0; t < B4N_COUNT; t++)
+        node[t] = K.node[t * n + i];
+    return bsim4_eval(x, K.p + i, (size_t)n, K.h + i, (size_t)n, node, K.st[i],
+                      C.stampv + K.stamp0 + i, (size_t)n);
+}
+
 /* CKTload: zero, device loads, gather into matrix and rhs. */
 __device__ int ckt_load(const ngsf_ckt_t &C, Ctl &s, const Iter &it)
 {
     int nc = 0;
+    for (int i = threadIdx.x; i < C.bsim4.n; i += blockDim.x)
+        nc |= bsim4_load_one(C, s, it, i);
     cap_load(C, s, it);
     for (int i = threadIdx.x; i < C.mos1.n; i += blockDim.x)
         nc |= mos1_load_one(C, s, it, i);
@@ -1029,6 +962,12 @@ __device__ double ckt_trunc(const ngsf_ckt_t &C, Ctl &s, double timeStep)
     double t = 1e300;   /* HUGE */
     for (int i = threadIdx.x; i < C.cap.n; i += blockDim.x)
         t = ckt_terr(C, s, C.cap.st[i], t);
+    for (int i = threadIdx.x; i < C.bsim4.n; i += blockDim.x) {
+        int b = C.bsim4.st[i];
+        t = ckt_terr(C, s, b + B4S_QB, t);
+        t = ckt_terr(C, s, b + B4S_QG, t);
+        t = ckt_terr(C, s, b + B4S_QD, t);
+    }
     for (int i = threadIdx.x; i < C.mos1.n; i += blockDim.x) {
         int b = C.mos1.st[i];
         t = ckt_terr(C, s, b + M1S_QGS, t);
@@ -1843,6 +1782,8 @@ tran_kernel(const ngsf_ckt_t *ckts, int nckt, int runMode, long long maxSteps)
         }
         for (size_t i = threadIdx.x; i < (size_t)M1H_COUNT * C.mos1.n; i += blockDim.x)
             C.mos1.h[i] = 0.0;
+        for (size_t i = threadIdx.x; i < (size_t)B4H_COUNT * C.bsim4.n; i += blockDim.x)
+            C.bsim4.h[i] = 0.0;
         for (int i = threadIdx.x; i < C.vsrc.n; i += blockDim.x)
             C.vsrc.brk[i] = -1.0;
         for (int i = threadIdx.x; i < C.isrc.n; i += blockDim.x)

@@ -86,6 +86,16 @@ typedef struct {
     int stamp0;           /* first stamp slot; slot = stamp0 + k*n + i */
 } ngsf_mos1_t;
 
+/* -------- BSIM4 (field enums in bsim4.h) ------------------------------- */
+typedef struct {
+    int n;
+    const int *node;      /* [B4N_COUNT][n] */
+    const int *st;        /* [n] state offset */
+    const double *p;      /* [B4P_COUNT][n] */
+    double *h;            /* [B4H_COUNT][n] */
+    int stamp0;           /* first stamp slot; slot = stamp0 + k*n + i */
+} ngsf_bsim4_t;
+
 /* -------- diode ------------------------------------------------------- */
 enum { DN_POS, DN_NEG, DN_POSP, DN_COUNT };
 enum {
@@ -164,6 +174,7 @@ typedef struct {
     ngsf_opts_t opt;
 
     /* devices, in the reference device-table order for load/trunc/conv */
+    ngsf_bsim4_t bsim4;
     ngsf_dio_t dio;
     ngsf_mos1_t mos1;
     ngsf_res_t res;

@@ -24,6 +24,7 @@
 
 #include "circuit.h"
 #include "runtime.h"
+#include "bsim4.h"
 #include "sparse.h"
 
 extern "C" cudaError_t ngsf_launch_tran(const ngsf_ckt_t *d_ckts, int nckt, int runMode,
@@ -103,6 +104,7 @@ void DeviceCircuit::upload(const Image &img, const std::vector<int> &probes, int
     const int n = img.n;
     const int nnz = (int)img.a_ri.size();
     struct Off {
+        size_t b4_node, b4_st, b4_p, b4_h;
         size_t mos1_node, mos1_st, mos1_p, mos1_h;
         size_t res_node, res_g;
         size_t cap_node, cap_st, cap_c, cap_m, cap_ic;
@@ -114,6 +116,10 @@ void DeviceCircuit::upload(const Image &img, const std::vector<int> &probes, int
         size_t states, rhs, rhsOld, breaks, out, probe, cap_ax, cap_rhs, cap_meta, result,
             fresult, ctlsave;
     } o{};
+    o.b4_node = puti(img.b4_node);
+    o.b4_st = puti(img.b4_st);
+    o.b4_p = putd(img.b4_p);
+    o.b4_h = zero((size_t)B4H_COUNT * img.nb4 * sizeof(double));
     o.mos1_node = puti(img.mos1_node);
     o.mos1_st = puti(img.mos1_st);
     o.mos1_p = putd(img.mos1_p);
@@ -187,6 +193,7 @@ void DeviceCircuit::upload(const Image &img, const std::vector<int> &probes, int
     h.nstamp = img.nstamp;
     h.nnz = nnz;
     h.opt = img.opt;
+    h.bsim4 = {img.nb4, I(o.b4_node), I(o.b4_st), D(o.b4_p), D(o.b4_h), img.b4_stamp0};
     h.mos1 = {img.nmos1, I(o.mos1_node), I(o.mos1_st), D(o.mos1_p), D(o.mos1_h),
               img.mos1_stamp0};
     h.res = {img.nres, I(o.res_node), D(o.res_g), img.res_stamp0};

@@ -43,8 +43,8 @@ def sources() -> list[str]:
 
 def _compile(src: str) -> str:
     obj = os.path.join(BUILD, os.path.basename(src) + ".o")
-    deps = [src] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith(".h")]
-    deps += [os.path.join(INCLUDE, h) for h in os.listdir(INCLUDE) if h.endswith(".h")]
+    deps = [src] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh", ".def"))]
+    deps += [os.path.join(INCLUDE, h) for h in os.listdir(INCLUDE) if h.endswith((".h", ".cuh", ".def"))]
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps):
         return obj
     cmd = [nvcc()] + ARCH + COMMON + ["-c", src, "-o", obj]

@@ -83,6 +83,24 @@ typedef struct {
     double von, vdsat, cd, cbs, cbd, gbs, gbd, gm, gds, gmbs, capbs, capbd;
 } mos1_t;
 
+/* BSIM4: parameters resolved and evaluated by the shared model arithmetic
+ * (b4port.cpp); the port assembles the stamps in the reference order */
+#define B4_MAXPARAM 256
+#define B4_MAXSTAMP 64
+typedef struct {
+    int node[6];        /* d g s b dp sp */
+    int st;
+    double p[B4_MAXPARAM];
+    double h[4];
+} b4_t;
+int port_b4_nparam(void);
+int port_b4_nstamp(void);
+void port_b4_pattern(int *rows, int *cols);
+int port_b4_load_one(int mode, int order, double gmin, double delta, double deltaOld1,
+                     double ag0, double ag1, const double *rhsOld, double *st0, double *st1,
+                     const double *st2, const double *p, double *h, const int *node, int st,
+                     double *sv);
+
 typedef struct { int a, b; double g; } res_t;
 typedef struct { int a, b, st; double c, m, ic; } cap_t;
 typedef struct {
@@ -94,11 +112,12 @@ typedef struct {
     int n, nstates;
     int *ntype;
     /* devices in reference iteration order */
-    int nres, ncap, nvsrc, nisrc, nmos1;
+    int nres, ncap, nvsrc, nisrc, nmos1, nb4;
     res_t *res;
     cap_t *cap;
     src_t *vsrc, *isrc;
     mos1_t *mos1;
+    b4_t *b4;
     /* options */
     double reltol, abstol, vntol, chgtol, trtol, gmin0, pivtol, pivrel, xmu;
     double tstep, tstop, tstart, tmax, delmin, minbreak;
@@ -161,6 +180,7 @@ void port_free(port_t *c)
     free(c->vsrc);
     free(c->isrc);
     free(c->mos1);
+    free(c->b4);
     free(c->breaks);
     free(c);
 }
@@ -215,6 +235,17 @@ void port_add_mos1(port_t *c, const int *nodes, int st, const double *p)
     memcpy(m.p, p, sizeof m.p);
     c->mos1 = realloc(c->mos1, sizeof(mos1_t) * (c->nmos1 + 1));
     c->mos1[c->nmos1++] = m;
+}
+
+void port_add_b4(port_t *c, const int *nodes, int st, const double *p)
+{
+    b4_t m;
+    memset(&m, 0, sizeof m);
+    memcpy(m.node, nodes, sizeof m.node);
+    m.st = st;
+    memcpy(m.p, p, sizeof(double) * port_b4_nparam());
+    c->b4 = realloc(c->b4, sizeof(b4_t) * (c->nb4 + 1));
+    c->b4[c->nb4++] = m;
 }
 
 void port_set_output(port_t *c, double *out, int outcap)
@@ -855,15 +886,43 @@ static int mos1_conv(port_t *c)
     return 0;
 }
 
+/* BSIM4load + BSIM4LoadRhsMat (src/spicelib/devices/bsim4/b4ld.c:70-5623):
+ * per instance, its right-hand-side terms and then its matrix terms */
+static int b4_load(port_t *c)
+{
+    int nc = 0;
+    static int rows[B4_MAXSTAMP], cols[B4_MAXSTAMP], ns = -1;
+    if (ns < 0) {
+        port_b4_pattern(rows, cols);
+        ns = port_b4_nstamp();
+    }
+    double sv[B4_MAXSTAMP];
+    for (int i = 0; i < c->nb4; i++) {
+        b4_t *h = &c->b4[i];
+        nc |= port_b4_load_one(c->mode, c->order, c->gmin, c->delta, c->deltaOld[1], c->ag[0],
+                               c->ag[1], c->rhsOld, c->states[0], c->states[1], c->states[2],
+                               h->p, h->h, h->node, h->st, sv);
+        for (int k = 0; k < ns; k++) {
+            if (rows[k] < 0)
+                c->rhs[h->node[cols[k]]] += sv[k];
+            else
+                A_(c, h->node[rows[k]], h->node[cols[k]]) += sv[k];
+        }
+    }
+    c->rhs[0] = 0.0;
+    return nc;
+}
+
 static int ckt_load(port_t *c)
 {
     int n = c->n;
     memset(c->rhs, 0, sizeof(double) * (n + 1));
     memset(c->A, 0, sizeof(double) * (size_t)(n + 1) * (n + 1));
     /* reference device-table order: bsim4, cap, dio, isrc, mos1, res, vsrc */
+    int nc = b4_load(c);
     cap_load(c);
     src_load(c);
-    int nc = mos1_load(c);
+    nc |= mos1_load(c);
     res_load(c);
     vsrc_load(c);
     return nc;
@@ -1348,6 +1407,11 @@ static double terr(port_t *c, int qcap, double timeStep)
 static double trunc_step(port_t *c, double timeStep)
 {
     double t = 1e300;
+    for (int i = 0; i < c->nb4; i++) {
+        t = terr(c, c->b4[i].st + 11, t);   /* qb */
+        t = terr(c, c->b4[i].st + 13, t);   /* qg */
+        t = terr(c, c->b4[i].st + 15, t);   /* qd */
+    }
     for (int i = 0; i < c->ncap; i++)
         t = terr(c, c->cap[i].st, t);
     for (int i = 0; i < c->nmos1; i++) {

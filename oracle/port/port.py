@@ -35,13 +35,32 @@ ROOT2 = 1.4142135623730950488016887242097
 CTOK = 273.15
 
 
+CSRC = os.path.join(ROOT, "ngspice-sf-mirror_gb300", "csrc")
+
+
 def build(force: bool = False) -> str:
-    """Compile port.c into oracle/_port/libngport.so (gcc, no contraction)."""
+    """Compile port.c (gcc) and the BSIM4 glue b4port.cpp with the shared
+    model arithmetic (g++) into oracle/_port/libngport.so, without
+    floating-point contraction."""
     src = os.path.join(HERE, "port.c")
+    cxx = [os.path.join(HERE, "b4port.cpp"), os.path.join(CSRC, "bsim4_setup.cpp")]
+    deps = [src] + cxx + [os.path.join(CSRC, f) for f in os.listdir(CSRC)
+                          if f.endswith((".h", ".cuh", ".def"))]
     os.makedirs(OUT, exist_ok=True)
-    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(src):
-        cmd = ["gcc", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-o", LIB, src, "-lm"]
-        subprocess.run(cmd, check=True)
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(map(os.path.getmtime, deps)):
+        objs = []
+        flags = ["-O2", "-ffp-contract=off", "-fPIC"]
+        o = os.path.join(OUT, "port.o")
+        subprocess.run(["gcc"] + flags + ["-c", src, "-o", o], check=True)
+        objs.append(o)
+        for f in cxx:
+            o = os.path.join(OUT, os.path.basename(f) + ".o")
+            subprocess.run(["g++", "-std=c++17"] + flags + [f"-I{CSRC}", "-c", f, "-o", o],
+                           check=True)
+            objs.append(o)
+        tmp = LIB + ".tmp"
+        subprocess.run(["g++", "-shared", "-o", tmp] + objs + ["-lm"], check=True)
+        os.replace(tmp, LIB)
     return LIB
 
 
@@ -64,6 +83,15 @@ def lib():
         L.port_add_src.argtypes = [vp, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                    C.POINTER(C.c_double), C.c_double, C.c_int, C.c_double]
         L.port_add_mos1.argtypes = [vp, C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_double)]
+        L.port_add_b4.argtypes = [vp, C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_double)]
+        L.port_b4_nparam.restype = C.c_int
+        L.port_b4_nstate.restype = C.c_int
+        cp = C.POINTER(C.c_char_p)
+        dp = C.POINTER(C.c_double)
+        L.port_b4_params.restype = C.c_int
+        L.port_b4_params.argtypes = [C.c_char_p, C.c_int, C.c_int, cp, dp, C.c_char_p, C.c_int,
+                                     cp, dp, C.c_double, C.c_double, dp,
+                                     C.POINTER(C.c_int), C.POINTER(C.c_int), C.c_char_p, C.c_int]
         L.port_set_output.argtypes = [vp, C.POINTER(C.c_double), C.c_int]
         L.port_set_dump.argtypes = [vp] + [C.POINTER(C.c_double)] * 4 + [C.c_int]
         L.port_run.restype = C.c_int
@@ -243,9 +271,12 @@ class Circuit:
                 mname = t[5]
                 mtype, mp = self.models[mname]
                 level = int(mp.get("level", 1))
-                if level != 1:
-                    raise ValueError("oracle port: only MOS level 1")
-                inst.append((K_MOS1, t[0], nodes, mname, params(t, 6), None))
+                if level == 1:
+                    inst.append((K_MOS1, t[0], nodes, mname, params(t, 6), None))
+                elif level in (14, 54):
+                    inst.append((K_BSIM4, t[0], nodes, mname, params(t, 6), None))
+                else:
+                    raise ValueError("oracle port: MOS levels 1 and 54 only")
                 key = mname
             else:
                 raise ValueError(f"oracle port: unsupported element {t[0]}")
@@ -255,7 +286,7 @@ class Circuit:
         self.order = {kk: [] for kk in range(7)}
         groups = {}
         for idx, e in enumerate(inst):
-            key = ("default", e[0]) if e[0] != K_MOS1 else e[3]
+            key = ("default", e[0]) if e[0] not in (K_MOS1, K_BSIM4) else e[3]
             groups.setdefault(key, []).append(idx)
         for kk in range(7):
             keys = [key for key in groups if (inst[groups[key][0]][0] == kk)]
@@ -310,6 +341,14 @@ class Circuit:
                 if kind == K_CAP:
                     self.dev[kk].append((nodes, st, extra, p))
                     st += 2
+                elif kind == K_BSIM4:
+                    mtype, mp = self.models[extra]
+                    par, need_dp, need_sp = bsim4_params(extra, mtype, mp, name, p, self.opts)
+                    d, g, s, b = nodes
+                    dp = self.mk(name + "#drain", True) if need_dp else d
+                    sp = self.mk(name + "#source", True) if need_sp else s
+                    self.dev[kk].append(([d, g, s, b, dp, sp], st, par))
+                    st += lib().port_b4_nstate()
                 elif kind == K_MOS1:
                     mtype, mp = self.models[extra]
                     par, need_dp, need_sp = mos1_params(mtype, mp, p, self.opts)
@@ -359,6 +398,8 @@ class Circuit:
                                    len(wf["coef"]), cf, wf["dc"], wf["dcgiven"], 1.0)
             for nodes, st, par in self.dev[K_MOS1]:
                 L.port_add_mos1(h, (C.c_int * 6)(*nodes), st, (C.c_double * len(par))(*par))
+            for nodes, st, par in self.dev[K_BSIM4]:
+                L.port_add_b4(h, (C.c_int * 6)(*nodes), st, (C.c_double * len(par))(*par))
             for nodes, r, p in self.dev[K_RES]:
                 L.port_add_res(h, nodes[0], nodes[1], p.get("m", 1.0) / (r * 1.0 * 1.0))
             outcap = 1 << 16
@@ -533,6 +574,36 @@ def mos1_params(mtype: str, mp: dict, ip: dict, opts: dict):
     need_dp = rd != 0 or (rsh != 0 and nrd != 0)
     need_sp = rs != 0 or (rsh != 0 and nrs != 0)
     return [float(x) for x in par], need_dp, need_sp
+
+
+def _temps(opts: dict) -> tuple[float, float]:
+    temp = evaluate(opts["temp"]) + CTOK if "temp" in opts else 300.15
+    tnom = evaluate(opts["tnom"]) + CTOK if "tnom" in opts else 300.15
+    return temp, tnom
+
+
+def bsim4_params(mname: str, mtype: str, mp: dict, iname: str, ip: dict, opts: dict):
+    """BSIM4setup + BSIM4temp for one instance through the shared model
+    arithmetic (b4port.cpp); returns the parameter vector and whether
+    internal drain/source nodes are needed."""
+    L = lib()
+    mk = [k for k in mp if k != "level"]
+    ik = list(ip)
+    temp, tnom = _temps(opts)
+    npar = L.port_b4_nparam()
+    out = (C.c_double * npar)()
+    ndp, nsp = C.c_int(), C.c_int()
+    err = C.create_string_buffer(512)
+    rc = L.port_b4_params(mname.encode(), 1 if mtype == "nmos" else -1, len(mk),
+                          (C.c_char_p * max(1, len(mk)))(*[k.encode() for k in mk]),
+                          (C.c_double * max(1, len(mk)))(*[float(mp[k]) for k in mk]),
+                          iname.encode(), len(ik),
+                          (C.c_char_p * max(1, len(ik)))(*[k.encode() for k in ik]),
+                          (C.c_double * max(1, len(ik)))(*[float(ip[k]) for k in ik]),
+                          temp, tnom, out, C.byref(ndp), C.byref(nsp), err, 512)
+    if rc != 0:
+        raise ValueError("oracle port: " + err.value.decode())
+    return list(out), bool(ndp.value), bool(nsp.value)
 
 
 def simulate(text: str, **kw) -> dict:

@@ -10,6 +10,7 @@ from tolerances import matrix_violation, rhs_violation, waveform_violation
 pytestmark = pytest.mark.gpu
 
 CASES = ["rc_ladder", "inverter_chain32"]
+BSIM4_CASES = ["bsim4_chain8", "bsim4_logic_s3"]
 
 
 @pytest.fixture(scope="module")
@@ -68,6 +69,53 @@ def test_newton_iterations_stamp_like_reference(E, name):
         assert matrix_violation(g["it_rows"][p0:p1], g["it_cols"][p0:p1],
                                 g["it_vals"][p0:p1], cp, ri, cap["ax"][km]) <= 1.0
         assert rhs_violation(g["it_rhs"][kr][1:n + 1], cap["rhs"][km][1:n + 1]) <= 1.0
+        checked += 1
+    assert checked > 20
+
+
+@pytest.mark.parametrize("name", BSIM4_CASES)
+def test_bsim4_tran_matches_reference(E, name):
+    """BSIM4 decks: the same Newton and step counts as the reference; time
+    points equal to rounding (the device libm and the host libm differ in
+    the last bit of exp/log) and waveforms within 1% of the tolerance."""
+    g = golden(name)
+    c = run_one(E, str(g["netlist"]))
+    r = c.results()
+    ref = g["stats"]
+    assert r[E.R_STATUS] == 0
+    assert (r[E.R_ACCEPTED], r[E.R_REJECTED], r[E.R_TRANITER]) == (ref[3], ref[4], ref[1])
+    t, v = c.points()
+    assert len(t) == len(g["times"])
+    assert np.max(np.abs(t - g["times"])) <= 1e-9 * g["times"][-1]
+    assert waveform_violation(c.names(), g["times"], g["values"], t, v) < 0.01
+
+
+@pytest.mark.parametrize("name", BSIM4_CASES)
+def test_bsim4_newton_iterations_stamp_like_reference(E, name):
+    """Stamped Jacobian / right-hand side of every captured BSIM4 Newton
+    iteration from the first transient iteration on, within 1e-12 of the
+    reference's (row-scaled)."""
+    g = golden(name)
+    k = len(g["it_kind"])
+    c = run_one(E, str(g["netlist"]), capmax=k + 400)
+    cap = c.capture(k + 400)
+    cp, ri = c.pattern()
+    ref_modes = g["it_meta"][:, 2].astype(int)
+    my_modes = cap["meta"][:, 2].astype(int)
+    r0 = int(np.argmax(ref_modes & 0x1000))
+    m0 = int(np.argmax(my_modes & 0x1000))
+    assert ref_modes[r0] & 0x1000 and my_modes[m0] & 0x1000
+    n = c.n
+    checked = 0
+    for i in range(k - r0):
+        kr, km = r0 + i, m0 + i
+        if km >= len(cap["ax"]):
+            break
+        assert ref_modes[kr] == my_modes[km]
+        p0, p1 = g["it_ptr"][kr], g["it_ptr"][kr + 1]
+        assert matrix_violation(g["it_rows"][p0:p1], g["it_cols"][p0:p1],
+                                g["it_vals"][p0:p1], cp, ri, cap["ax"][km]) <= 1.0, kr
+        assert rhs_violation(g["it_rhs"][kr][1:n + 1], cap["rhs"][km][1:n + 1]) <= 1.0, kr
         checked += 1
     assert checked > 20
 

@@ -12,7 +12,7 @@ import port
 from conftest import golden
 from tolerances import waveform_violation
 
-CASES = ["rc_ladder", "inverter_chain32"]
+CASES = ["rc_ladder", "inverter_chain32", "bsim4_chain8"]
 
 
 @pytest.mark.parametrize("name", CASES)
@@ -29,6 +29,42 @@ def test_port_matches_reference(name):
     np.testing.assert_array_equal(r["times"], g["times"])
     # identical time points; values agree to rounding (1% of the tolerance)
     assert waveform_violation(r["names"], g["times"], g["values"], r["times"], r["values"]) < 0.01
+
+
+def test_port_bsim4_logic_matches_reference():
+    """Random BSIM4 logic (seed 3, ~120 transistors): identical Newton and
+    step counts; the accepted time points agree to rounding (the dense LU
+    of the port and KLU round differently) and the waveforms to 1% of the
+    tolerance."""
+    g = golden("bsim4_logic_s3")
+    r = port.simulate(str(g["netlist"]))
+    st, ref = r["stats"], g["stats"]
+    assert st["status"] == 0
+    assert (st["numIter"], st["tranIter"], st["accepted"], st["rejected"]) == \
+        (ref[0], ref[1], ref[3], ref[4])
+    assert np.max(np.abs(r["times"] - g["times"])) <= 1e-9 * g["times"][-1]
+    names = list(g["names"])
+    idx = [r["names"].index(x) for x in names]
+    assert waveform_violation(names, g["times"], g["values"], r["times"],
+                              r["values"][:, idx]) < 0.01
+
+
+def test_port_bsim4_newton_stamps_match_reference():
+    """Per-iteration stamped Jacobian and right-hand side of the first
+    200 Newton iterations of the BSIM4 inverter chain (operating point and
+    transient) within 1e-12, row-scaled, of the reference's."""
+    from tolerances import matrix_violation_dense
+    g = golden("bsim4_chain8")
+    r = port.simulate(str(g["netlist"]), dump=len(g["it_kind"]))
+    assert len(r["dump_ax"]) == len(g["it_kind"])
+    for it in range(len(g["it_kind"])):
+        p0, p1 = g["it_ptr"][it], g["it_ptr"][it + 1]
+        assert matrix_violation_dense(g["it_rows"][p0:p1], g["it_cols"][p0:p1],
+                                      g["it_vals"][p0:p1], r["dump_ax"][it]) <= 1.0, it
+        n = r["dump_ax"].shape[1] - 1
+        ref_rhs = g["it_rhs"][it][1:n + 1]
+        assert np.max(np.abs(r["dump_rhs"][it][1:] - ref_rhs)) <= \
+            1e-12 * max(np.max(np.abs(ref_rhs)), 1e-300)
 
 
 def test_planted_mistake_is_caught():

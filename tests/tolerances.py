@@ -47,3 +47,14 @@ def matrix_violation(ref_rows, ref_cols, ref_vals, cp, ri, ax):
 def rhs_violation(ref_rhs, rhs):
     scale = max(float(np.max(np.abs(ref_rhs))), 1e-300)
     return float(np.max(np.abs(ref_rhs - rhs))) / (1e-12 * scale)
+
+
+def matrix_violation_dense(ref_rows, ref_cols, ref_vals, a):
+    """matrix_violation for a dense (n+1)x(n+1) matrix whose row/column 0 is
+    ground; the reference entries carry 0-based equation indices."""
+    ref = np.zeros_like(a)
+    ref[np.asarray(ref_rows) + 1, np.asarray(ref_cols) + 1] = ref_vals
+    m, r = a[1:, 1:], ref[1:, 1:]
+    rowscale = np.max(np.abs(r), axis=1, keepdims=True)
+    scale = np.maximum(np.maximum(np.abs(m), np.abs(r)), np.maximum(rowscale, 1e-300))
+    return float(np.max(np.abs(m - r) / (1e-12 * scale)))
