@@ -60,8 +60,9 @@ NGSF_API int ngsf_probes(const ngsf_handle *h, int *eqs, int max);
 NGSF_API int ngsf_run(ngsf_handle *const *hs, int count, long long max_steps,
                       double *seconds);
 
-/* results: ires[NGSF_R_COUNT] (status, npoints, accepted, rejected,
- * numIter, tranIter, timePts, ncap, opIter, badPivot), fres[2] */
+/* results: ires[11] (status, npoints, accepted, rejected, numIter,
+ * tranIter, timePts, ncap, opIter, badPivot, reorders), fres[3] (time
+ * reached, last step, diagonal gmin in force) */
 NGSF_API int ngsf_results(const ngsf_handle *h, int *ires, double *fres);
 /* accepted points: buf[np][1 + nprobe] = time, probe values; returns np */
 NGSF_API int ngsf_points(const ngsf_handle *h, double *buf, int maxpoints);

@@ -215,7 +215,7 @@ NGSF_API int ngsf_workload(const ngsf_handle *h, long long *counts)
     counts[5] = (long long)m.a_ri.size();
     counts[6] = m.nlu;
     counts[7] = m.n;
-    counts[8] = 0;   /* BSIM4 instances */
+    counts[8] = m.nb4;
     counts[9] = m.ndio;
     return 0;
 }

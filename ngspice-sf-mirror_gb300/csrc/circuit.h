@@ -139,6 +139,7 @@ struct Image {
     std::vector<int> ntype;
     /* stamping */
     std::vector<int> gptr, gsrc, rptr, rsrc;
+    std::vector<int> heavy;   /* entries with more than 64 terms (rhs row r as -r-1) */
     /* A pattern: CSC over columns 0..n-1 (equation j+1), 0-based rows */
     std::vector<int> a_cp, a_ri, a_lupos, a_diag;
     /* LU */
@@ -146,6 +147,10 @@ struct Image {
     std::vector<int> upd_dst, upd_src, prow, pcol;
     std::vector<int> fl_ptr, fl_row, bl_ptr, bl_row;
     std::vector<int> lr_ptr, lr_col, lr_pos, ur_ptr, ur_col, ur_pos;
+    std::vector<int> fh_ptr, fh_row, bh_ptr, bh_row;   /* solve rows reduced by a warp */
+    /* right-looking level schedule (large matrices) */
+    std::vector<int> rl_ptr, rl_col, sc_ptr, sc_pos, sc_piv;
+    std::vector<int> ud_ptr, ud_dst, ud_cptr, ud_l, ud_u;
     double lu_flops = 0;   /* multiply-adds of one refactorization */
     std::vector<std::string> names;  /* equation names 1..n */
 };

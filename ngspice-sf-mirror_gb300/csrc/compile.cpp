@@ -619,6 +619,13 @@ void compile(Circuit &c, Image &img)
                 img.rsrc.push_back(s);
         img.rptr[i + 1] = (int)img.rsrc.size();
     }
+    img.heavy.clear();
+    for (int p = 0; p < nnz; p++)
+        if (img.gptr[p + 1] - img.gptr[p] > 64)
+            img.heavy.push_back(p);
+    for (int r = 0; r <= n; r++)
+        if (img.rptr[r + 1] - img.rptr[r] > 64)
+            img.heavy.push_back(-r - 1);
     for (int j = 0; j < n; j++)
         if (img.a_cp[j + 1] == img.a_cp[j])
             throw NetlistError("equation " + img.names[j] + " has no matrix entries (floating node)");

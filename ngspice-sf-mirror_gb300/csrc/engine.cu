@@ -22,6 +22,7 @@
  * (NGSF_E_WATCHDOG), so a kernel always returns with a status word.
  */
 #include <cuda_runtime.h>
+#include <cuda/atomic>
 #include <math.h>
 #include <stdint.h>
 
@@ -30,6 +31,8 @@
 
 #define NGSF_THREADS 256
 #define NGSF_WARPS (NGSF_THREADS / 32)
+/* a matrix cell or rhs entry with more contributions is summed by a warp */
+#define NGSF_HEAVY 64
 
 namespace {
 
@@ -788,29 +791,176 @@ __device__ int bsim4_load_one(const ngsf_ckt_t &C, const Ctl &s, const Iter &it,
                       C.stampv + K.stamp0 + i, (size_t)n);
 }
 
+/* ---------------------------------------------------------------- */
+/* wide launch: hand-over between block 0 and the worker blocks        */
+/* ---------------------------------------------------------------- */
+#define NGSF_WIDE_SPIN_LIMIT (1LL << 26)   /* x ~100 ns sleeps: a few seconds */
+
+/* the transistor share of block b out of nb: contiguous chunks */
+__device__ int wide_transistors(const ngsf_ckt_t &C, const Ctl &s, const Iter &it, int b, int nb)
+{
+    int nc = 0;
+    int chunk = (C.bsim4.n + nb - 1) / nb;
+    int lo = b * chunk, hi = min(C.bsim4.n, lo + chunk);
+    for (int i = lo + threadIdx.x; i < hi; i += blockDim.x)
+        nc |= bsim4_load_one(C, s, it, i);
+    chunk = (C.mos1.n + nb - 1) / nb;
+    lo = b * chunk;
+    hi = min(C.mos1.n, lo + chunk);
+    for (int i = lo + threadIdx.x; i < hi; i += blockDim.x)
+        nc |= mos1_load_one(C, s, it, i);
+    return nc;
+}
+
+/* block 0: publish the control words and a command (thread 0 only) */
+__device__ void wide_issue(const ngsf_ckt_t &C, const Ctl &s, int cmd)
+{
+    ngsf_wide_t *w = C.wide;
+    w->done = 0;
+    w->noncon = 0;
+    const unsigned long long *src = (const unsigned long long *)&s;
+    for (int k = 0; k < (int)((sizeof(Ctl) + 7) / 8); k++)
+        w->ctl[k] = src[k];
+    w->cmd = cmd;
+    cuda::atomic_ref<int, cuda::thread_scope_device> seq(w->seq);
+    seq.fetch_add(1, cuda::memory_order_release);
+}
+
+/* block 0: wait until the other nb-1 blocks finished (thread 0 only);
+ * returns their convergence flag, or 1 with err set when the wait ran out */
+__device__ int wide_collect(const ngsf_ckt_t &C, int nb)
+{
+    ngsf_wide_t *w = C.wide;
+    cuda::atomic_ref<int, cuda::thread_scope_device> done(w->done);
+    cuda::atomic_ref<int, cuda::thread_scope_device> err(w->err);
+    long long spins = 0;
+    while (done.load(cuda::memory_order_acquire) < nb - 1) {
+        if (++spins > NGSF_WIDE_SPIN_LIMIT || err.load(cuda::memory_order_relaxed)) {
+            err.store(1);
+            return 1;
+        }
+        __nanosleep(64);
+    }
+    return w->noncon;
+}
+
+/* worker blocks: serve block 0's commands until EXIT (or a timeout) */
+__device__ void wide_worker(const ngsf_ckt_t &C, Ctl &s)
+{
+    ngsf_wide_t *w = C.wide;
+    __shared__ int cmd;
+    int seen = 0;
+    for (;;) {
+        if (threadIdx.x == 0) {
+            cuda::atomic_ref<int, cuda::thread_scope_device> seq(w->seq);
+            long long spins = 0;
+            int v;
+            while ((v = seq.load(cuda::memory_order_acquire)) == seen) {
+                if (++spins > NGSF_WIDE_SPIN_LIMIT)
+                    break;
+                __nanosleep(128);
+            }
+            if (v == seen) {
+                cuda::atomic_ref<int, cuda::thread_scope_device>(w->err).store(1);
+                cmd = NGSF_WIDE_EXIT;
+            } else {
+                seen = v;
+                cmd = w->cmd;
+                unsigned long long *dst = (unsigned long long *)&s;
+                for (int k = 0; k < (int)((sizeof(Ctl) + 7) / 8); k++)
+                    dst[k] = w->ctl[k];
+            }
+        }
+        __syncthreads();
+        if (cmd == NGSF_WIDE_EXIT)
+            return;
+        Iter it = iter_ctx(C, s);
+        int nc = wide_transistors(C, s, it, blockIdx.x, gridDim.x);
+        nc = block_or(s, nc);
+        if (threadIdx.x == 0) {
+            if (nc)
+                atomicOr(&w->noncon, 1);
+            cuda::atomic_ref<int, cuda::thread_scope_device> done(w->done);
+            done.fetch_add(1, cuda::memory_order_release);
+        }
+        __syncthreads();
+    }
+}
+
 /* CKTload: zero, device loads, gather into matrix and rhs. */
 __device__ int ckt_load(const ngsf_ckt_t &C, Ctl &s, const Iter &it)
 {
     int nc = 0;
-    for (int i = threadIdx.x; i < C.bsim4.n; i += blockDim.x)
-        nc |= bsim4_load_one(C, s, it, i);
-    cap_load(C, s, it);
-    for (int i = threadIdx.x; i < C.mos1.n; i += blockDim.x)
-        nc |= mos1_load_one(C, s, it, i);
-    res_load(C);
-    src_load(C, s);
-    nc = block_or(s, nc);   /* includes __syncthreads: stamps visible */
+    __shared__ int wide_nc;
+    if (C.wide) {
+        if (threadIdx.x == 0)
+            wide_issue(C, s, NGSF_WIDE_LOAD);
+        nc = wide_transistors(C, s, it, 0, gridDim.x);
+        cap_load(C, s, it);
+        res_load(C);
+        src_load(C, s);
+        nc = block_or(s, nc);
+        if (threadIdx.x == 0) {
+            wide_nc = wide_collect(C, gridDim.x);
+            if (C.wide->err)
+                s.flag = NGSF_E_WATCHDOG;
+        }
+        __syncthreads();
+        nc |= wide_nc;
+    } else {
+        for (int i = threadIdx.x; i < C.bsim4.n; i += blockDim.x)
+            nc |= bsim4_load_one(C, s, it, i);
+        cap_load(C, s, it);
+        for (int i = threadIdx.x; i < C.mos1.n; i += blockDim.x)
+            nc |= mos1_load_one(C, s, it, i);
+        res_load(C);
+        src_load(C, s);
+        nc = block_or(s, nc);   /* includes __syncthreads: stamps visible */
+    }
+    /* Cells with up to NGSF_HEAVY contributions are summed by one thread
+     * in the reference's load order (bit-identical to CKTload).  The few
+     * cells that collect thousands of contributions (a supply node's
+     * diagonal) are summed by a warp: lane-strided partial sums in load
+     * order, then a fixed butterfly; the rounding then differs from the
+     * sequential sum by far less than the 1e-12 stamp tolerance. */
     for (int p = threadIdx.x; p < C.nnz; p += blockDim.x) {
+        const int q0 = C.gptr[p], q1 = C.gptr[p + 1];
+        if (q1 - q0 > NGSF_HEAVY)
+            continue;
         double acc = 0.0;
-        for (int q = C.gptr[p]; q < C.gptr[p + 1]; q++)
+        for (int q = q0; q < q1; q++)
             acc += C.stampv[C.gsrc[q]];
         C.ax[p] = acc;
     }
     for (int r = threadIdx.x; r <= C.n; r += blockDim.x) {
+        const int q0 = C.rptr[r], q1 = C.rptr[r + 1];
+        if (q1 - q0 > NGSF_HEAVY)
+            continue;
         double acc = 0.0;
-        for (int q = C.rptr[r]; q < C.rptr[r + 1]; q++)
+        for (int q = q0; q < q1; q++)
             acc += C.stampv[C.rsrc[q]];
         it.rhs[r] = acc;
+    }
+    {
+        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+        for (int h = warp; h < C.nheavy; h += NGSF_WARPS) {
+            const int p = C.heavy[h];
+            const bool isrhs = p < 0;
+            const int e = isrhs ? -p - 1 : p;
+            const int *ptr = isrhs ? C.rptr : C.gptr;
+            const int *src = isrhs ? C.rsrc : C.gsrc;
+            double acc = 0.0;
+            for (int q = ptr[e] + lane; q < ptr[e + 1]; q += 32)
+                acc += C.stampv[src[q]];
+            for (int o = 16; o > 0; o >>= 1)
+                acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == 0) {
+                if (isrhs)
+                    it.rhs[e] = acc;
+                else
+                    C.ax[e] = acc;
+            }
+        }
     }
     __syncthreads();
     return nc;
@@ -840,6 +990,32 @@ __device__ int lu_factor(const ngsf_ckt_t &C, Ctl &s)
     }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int bad = 0;
+    if (C.rl_levels > 0) {
+        /* right-looking, two barriers per level (large matrices) */
+        for (int l = 0; l < C.rl_levels; l++) {
+            for (int c = C.rl_ptr[l] + threadIdx.x; c < C.rl_ptr[l + 1]; c += blockDim.x) {
+                double piv = C.lux[C.cdiag[C.rl_col[c]]];
+                if (!(fabs(piv) > 0.0) || !isfinite(piv))
+                    bad = 1;
+            }
+            for (int e = C.sc_ptr[l] + threadIdx.x; e < C.sc_ptr[l + 1]; e += blockDim.x) {
+                double l_ik = C.lux[C.sc_pos[e]] / C.lux[C.sc_piv[e]];
+                C.lux[C.sc_pos[e]] = l_ik;
+                if (!(fabs(l_ik) <= NGSF_GROWTH))
+                    bad = 1;
+            }
+            __syncthreads();
+            for (int d = C.ud_ptr[l] + threadIdx.x; d < C.ud_ptr[l + 1]; d += blockDim.x) {
+                const int dst = C.ud_dst[d];
+                double acc = C.lux[dst];
+                for (int c = C.ud_cptr[d]; c < C.ud_cptr[d + 1]; c++)
+                    acc -= C.lux[C.ud_l[c]] * C.lux[C.ud_u[c]];
+                C.lux[dst] = acc;
+            }
+            __syncthreads();
+        }
+        return block_or(s, bad);
+    }
     for (int l = 0; l < C.nlevels; l++) {
         for (int c = C.lvl_ptr[l] + warp; c < C.lvl_ptr[l + 1]; c += NGSF_WARPS) {
             int k = C.lvl_col[c];
@@ -872,23 +1048,51 @@ __device__ void lu_solve(const ngsf_ckt_t &C, Ctl &s, double *rhs)
     for (int k = threadIdx.x; k < C.n; k += blockDim.x)
         w[k] = rhs[C.prow[k]];
     __syncthreads();
+    /* rows of up to 32 terms: one thread, terms in order; longer rows
+     * (listed per level in fh/bh): a warp, lane-strided partial sums and a
+     * fixed butterfly */
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     for (int l = 0; l < C.nflevels; l++) {
         for (int r = C.fl_ptr[l] + threadIdx.x; r < C.fl_ptr[l + 1]; r += blockDim.x) {
             int k = C.fl_row[r];
+            if (C.lr_ptr[k + 1] - C.lr_ptr[k] > 32)
+                continue;
             double acc = w[k];
             for (int q = C.lr_ptr[k]; q < C.lr_ptr[k + 1]; q++)
                 acc -= C.lux[C.lr_pos[q]] * w[C.lr_col[q]];
             w[k] = acc;
+        }
+        for (int h = C.fh_ptr[l] + warp; h < C.fh_ptr[l + 1]; h += NGSF_WARPS) {
+            int k = C.fh_row[h];
+            double acc = 0.0;
+            for (int q = C.lr_ptr[k] + lane; q < C.lr_ptr[k + 1]; q += 32)
+                acc += C.lux[C.lr_pos[q]] * w[C.lr_col[q]];
+            for (int o = 16; o > 0; o >>= 1)
+                acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == 0)
+                w[k] = w[k] - acc;
         }
         __syncthreads();
     }
     for (int l = 0; l < C.nblevels; l++) {
         for (int r = C.bl_ptr[l] + threadIdx.x; r < C.bl_ptr[l + 1]; r += blockDim.x) {
             int k = C.bl_row[r];
+            if (C.ur_ptr[k + 1] - C.ur_ptr[k] > 32)
+                continue;
             double acc = w[k];
             for (int q = C.ur_ptr[k]; q < C.ur_ptr[k + 1]; q++)
                 acc -= C.lux[C.ur_pos[q]] * w[C.ur_col[q]];
             w[k] = acc / C.lux[C.cdiag[k]];
+        }
+        for (int h = C.bh_ptr[l] + warp; h < C.bh_ptr[l + 1]; h += NGSF_WARPS) {
+            int k = C.bh_row[h];
+            double acc = 0.0;
+            for (int q = C.ur_ptr[k] + lane; q < C.ur_ptr[k + 1]; q += 32)
+                acc += C.lux[C.ur_pos[q]] * w[C.ur_col[q]];
+            for (int o = 16; o > 0; o >>= 1)
+                acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == 0)
+                w[k] = (w[k] - acc) / C.lux[C.cdiag[k]];
         }
         __syncthreads();
     }
@@ -1143,6 +1347,13 @@ __device__ int ni_iter(const ngsf_ckt_t &C, Ctl &s, int maxIter, bool resume)
         } else {
             noncon = ckt_load(C, s, it);
             iterno++;
+            if (C.wide && s.flag == NGSF_E_WATCHDOG) {
+                /* a worker block stopped answering: end the run */
+                if (threadIdx.x == 0)
+                    s.numIter += iterno;
+                __syncthreads();
+                return NGSF_E_WATCHDOG;
+            }
             if (C.capmax > 0)
                 capture(C, s, it);
             bool want = (s.mode & NGSF_MODEINITJCT) ||
@@ -1725,6 +1936,8 @@ __device__ int dc_tran(const ngsf_ckt_t &C, Ctl &s, long long maxSteps, bool res
 #define RUN_RESUME 1
 #define RUN_PROBE 2
 
+__device__ void run_circuit(const ngsf_ckt_t &C, Ctl &s, int runMode, long long maxSteps);
+
 __global__ void __launch_bounds__(NGSF_THREADS)
 tran_kernel(const ngsf_ckt_t *ckts, int nckt, int runMode, long long maxSteps)
 {
@@ -1740,7 +1953,36 @@ tran_kernel(const ngsf_ckt_t *ckts, int nckt, int runMode, long long maxSteps)
             dst[w] = src[w];
     }
     __syncthreads();
-    const ngsf_ckt_t &C = Cs;
+    Cs.wide = nullptr;
+    __syncthreads();
+    run_circuit(Cs, s, runMode, maxSteps);
+}
+
+/* One circuit over the whole (cooperative) grid: block 0 runs the
+ * transient, the other blocks evaluate transistors on its command. */
+__global__ void __launch_bounds__(NGSF_THREADS)
+tran_wide_kernel(const ngsf_ckt_t *ckt, int runMode, long long maxSteps)
+{
+    __shared__ Ctl s;
+    __shared__ __align__(16) ngsf_ckt_t Cs;
+    {
+        const unsigned long long *src = (const unsigned long long *)ckt;
+        unsigned long long *dst = (unsigned long long *)&Cs;
+        for (int w = threadIdx.x; w < (int)(sizeof(ngsf_ckt_t) / 8); w += blockDim.x)
+            dst[w] = src[w];
+    }
+    __syncthreads();
+    if (blockIdx.x != 0) {
+        wide_worker(Cs, s);
+        return;
+    }
+    run_circuit(Cs, s, runMode, maxSteps);
+    if (threadIdx.x == 0)
+        wide_issue(Cs, s, NGSF_WIDE_EXIT);
+}
+
+__device__ void run_circuit(const ngsf_ckt_t &C, Ctl &s, int runMode, long long maxSteps)
+{
     if (runMode == RUN_RESUME) {
         const int *src = (const int *)C.ctlsave;
         int *dst = (int *)&s;
@@ -1831,7 +2073,31 @@ tran_kernel(const ngsf_ckt_t *ckts, int nckt, int runMode, long long maxSteps)
 
 }  // namespace
 
+static_assert(sizeof(Ctl) <= NGSF_WIDE_CTL_BYTES, "control block does not fit the wide hand-over");
+
 extern "C" int ngsf_ctl_bytes(void) { return (int)sizeof(Ctl); }
+
+/* Blocks a cooperative wide launch can keep resident on this device. */
+extern "C" int ngsf_wide_blocks(void)
+{
+    int dev = 0, sms = 0, per = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess)
+        return 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, tran_wide_kernel, NGSF_THREADS, 0) !=
+        cudaSuccess)
+        return 0;
+    return sms * per;
+}
+
+extern "C" cudaError_t ngsf_launch_tran_wide(const ngsf_ckt_t *d_ckt, int nblocks, int runMode,
+                                             long long maxSteps, cudaStream_t stream)
+{
+    void *args[] = {(void *)&d_ckt, (void *)&runMode, (void *)&maxSteps};
+    return cudaLaunchCooperativeKernel((const void *)tran_wide_kernel, dim3(nblocks),
+                                       dim3(NGSF_THREADS), args, 0, stream);
+}
 
 extern "C" cudaError_t ngsf_launch_tran(const ngsf_ckt_t *d_ckts, int nckt, int runMode,
                                         long long maxSteps, cudaStream_t stream)

@@ -162,6 +162,22 @@ typedef struct {
     int itl1, itl4, maxord, method, uic, order_init;
 } ngsf_opts_t;
 
+/* -------- wide launch: one circuit over a cooperative grid ------------ *
+ * Block 0 runs the transient; the other blocks wait for its commands and
+ * evaluate their share of the device instances.  The words are handed over
+ * with device-scope release/acquire; every wait is bounded. */
+#define NGSF_WIDE_CTL_BYTES 1024
+enum { NGSF_WIDE_LOAD = 1, NGSF_WIDE_EXIT = 2 };
+typedef struct {
+    int seq;              /* command number, bumped by block 0 (release) */
+    int cmd;              /* NGSF_WIDE_* */
+    int done;             /* blocks that finished the current command */
+    int noncon;           /* OR of the workers' convergence flags */
+    int err;              /* 1: a bounded wait ran out */
+    int pad[3];
+    unsigned long long ctl[NGSF_WIDE_CTL_BYTES / 8];  /* block 0's control words */
+} ngsf_wide_t;
+
 typedef struct {
     /* sizes */
     int n;                /* unknowns (equations 1..n) */
@@ -192,6 +208,8 @@ typedef struct {
     double *stampv;       /* [nstamp] */
     double *ax;           /* [nnz] */
     const int *gptr, *gsrc;
+    int nheavy;           /* entries summed by a warp (more than 64 terms) */
+    const int *heavy;     /* matrix entry p >= 0, or rhs row r as -r-1 */
     const int *rptr, *rsrc;
     const int *a_lupos;   /* [nnz] position of each entry in lux */
     const int *a_diag;    /* [n] entry index of A(j,j), -1 when absent */
@@ -217,6 +235,14 @@ typedef struct {
     int nflevels, nblevels;
     const int *lr_ptr, *lr_col, *lr_pos;  /* L rows: (k, lux pos) for m<k */
     const int *ur_ptr, *ur_col, *ur_pos;  /* U rows: (m, lux pos) for m>k */
+    const int *fh_ptr, *fh_row;   /* per forward level: rows reduced by a warp */
+    const int *bh_ptr, *bh_row;   /* per backward level: rows reduced by a warp */
+    /* right-looking schedule (used when rl_levels > 0): per level, its
+     * pivot columns, the L entries to divide by their pivot, and the
+     * destinations with their lists of (L pos, U pos) products */
+    int rl_levels;
+    const int *rl_ptr, *rl_col, *sc_ptr, *sc_pos, *sc_piv;
+    const int *ud_ptr, *ud_dst, *ud_cptr, *ud_l, *ud_u;
     double *work;         /* [n] solve workspace */
 
     /* Newton / integration state */
@@ -246,6 +272,7 @@ typedef struct {
     /* results written by the engine */
     int *result;          /* see NGSF_R_* */
     double *fresult;      /* see NGSF_F_* */
+    ngsf_wide_t *wide;    /* set only for a wide (cooperative) launch */
 } ngsf_ckt_t;
 
 /* integer results */

@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include <chrono>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -27,6 +28,9 @@
 #include "bsim4.h"
 #include "sparse.h"
 
+extern "C" int ngsf_wide_blocks(void);
+extern "C" cudaError_t ngsf_launch_tran_wide(const ngsf_ckt_t *d_ckt, int nblocks, int runMode,
+                                             long long maxSteps, cudaStream_t stream);
 extern "C" cudaError_t ngsf_launch_tran(const ngsf_ckt_t *d_ckts, int nckt, int runMode,
                                         long long maxSteps, cudaStream_t stream);
 extern "C" int ngsf_ctl_bytes(void);
@@ -109,12 +113,12 @@ void DeviceCircuit::upload(const Image &img, const std::vector<int> &probes, int
         size_t res_node, res_g;
         size_t cap_node, cap_st, cap_c, cap_m, cap_ic;
         size_t vs[9], is[9];
-        size_t ntype, stampv, ax, gptr, gsrc, rptr, rsrc, a_diag, opsave_rhs, opsave_st;
+        size_t ntype, stampv, ax, gptr, gsrc, rptr, rsrc, heavy, a_diag, opsave_rhs, opsave_st;
         size_t lux, lvl_ptr, lvl_col, cdiag, cend, cbeg, kptr, kdep, kpos, kseg, upd_dst,
             upd_src, prow, pcol, fl_ptr, fl_row, bl_ptr, bl_row, lr_ptr, lr_col, lr_pos,
             ur_ptr, ur_col, ur_pos, work;
         size_t states, rhs, rhsOld, breaks, out, probe, cap_ax, cap_rhs, cap_meta, result,
-            fresult, ctlsave;
+            fresult, ctlsave, wide;
     } o{};
     o.b4_node = puti(img.b4_node);
     o.b4_st = puti(img.b4_st);
@@ -155,6 +159,7 @@ void DeviceCircuit::upload(const Image &img, const std::vector<int> &probes, int
     o.gsrc = puti(img.gsrc);
     o.rptr = puti(img.rptr);
     o.rsrc = puti(img.rsrc);
+    o.heavy = puti(img.heavy);
     o.a_diag = puti(img.a_diag);
     o.opsave_rhs = zero((size_t)(n + 1) * sizeof(double));
     o.opsave_st = zero((size_t)(img.nstates + 1) * sizeof(double));
@@ -173,6 +178,7 @@ void DeviceCircuit::upload(const Image &img, const std::vector<int> &probes, int
     o.ctlsave = zero((size_t)ngsf_ctl_bytes() + 64);
     o.result = zero(NGSF_R_COUNT * sizeof(int));
     o.fresult = zero(NGSF_F_COUNT * sizeof(double));
+    o.wide = zero(sizeof(ngsf_wide_t));
 
     if (impl->base)
         cudaFree(impl->base);
@@ -210,6 +216,8 @@ void DeviceCircuit::upload(const Image &img, const std::vector<int> &probes, int
     h.gsrc = I(o.gsrc);
     h.rptr = I(o.rptr);
     h.rsrc = I(o.rsrc);
+    h.nheavy = (int)img.heavy.size();
+    h.heavy = I(o.heavy);
     h.a_diag = I(o.a_diag);
     h.opsave_rhs = D(o.opsave_rhs);
     h.opsave_st = D(o.opsave_st);
@@ -230,6 +238,7 @@ void DeviceCircuit::upload(const Image &img, const std::vector<int> &probes, int
     h.ctlsave = (void *)(b + o.ctlsave);
     h.result = I(o.result);
     h.fresult = D(o.fresult);
+    h.wide = (ngsf_wide_t *)(b + o.wide);
     if (!impl->d_desc)
         ck(cudaMalloc(&impl->d_desc, sizeof(ngsf_ckt_t)), "cudaMalloc(desc)");
     ck(cudaMemcpy(impl->d_desc, &h, sizeof(h), cudaMemcpyHostToDevice), "cudaMemcpy(desc)");
@@ -270,7 +279,20 @@ void DeviceCircuit::upload_lu(const Image &img)
            o_fl_ptr = puti(img.fl_ptr), o_fl_row = puti(img.fl_row), o_bl_ptr = puti(img.bl_ptr),
            o_bl_row = puti(img.bl_row), o_lr_ptr = puti(img.lr_ptr), o_lr_col = puti(img.lr_col),
            o_lr_pos = puti(img.lr_pos), o_ur_ptr = puti(img.ur_ptr), o_ur_col = puti(img.ur_col),
-           o_ur_pos = puti(img.ur_pos);
+           o_ur_pos = puti(img.ur_pos), o_fh_ptr = puti(img.fh_ptr),
+           o_fh_row = puti(img.fh_row), o_bh_ptr = puti(img.bh_ptr), o_bh_row = puti(img.bh_row);
+    /* the right-looking schedule is used for large matrices (its two
+     * barriers per level beat a column's dependency chain); small ones keep
+     * the left-looking order.  NGSF_LU=rl / ll overrides. */
+    bool rl = img.n > 1000;
+    if (const char *e = getenv("NGSF_LU"))
+        rl = std::string(e) == "rl";
+    const std::vector<int> none;
+    size_t o_rl_ptr = puti(rl ? img.rl_ptr : none), o_rl_col = puti(rl ? img.rl_col : none),
+           o_sc_ptr = puti(rl ? img.sc_ptr : none), o_sc_pos = puti(rl ? img.sc_pos : none),
+           o_sc_piv = puti(rl ? img.sc_piv : none), o_ud_ptr = puti(rl ? img.ud_ptr : none),
+           o_ud_dst = puti(rl ? img.ud_dst : none), o_ud_cptr = puti(rl ? img.ud_cptr : none),
+           o_ud_l = puti(rl ? img.ud_l : none), o_ud_u = puti(rl ? img.ud_u : none);
     if (impl->lubase)
         cudaFree(impl->lubase);
     impl->lubase = nullptr;
@@ -311,6 +333,21 @@ void DeviceCircuit::upload_lu(const Image &img)
     h.ur_ptr = I(o_ur_ptr);
     h.ur_col = I(o_ur_col);
     h.ur_pos = I(o_ur_pos);
+    h.fh_ptr = I(o_fh_ptr);
+    h.fh_row = I(o_fh_row);
+    h.bh_ptr = I(o_bh_ptr);
+    h.bh_row = I(o_bh_row);
+    h.rl_levels = rl ? (int)img.rl_ptr.size() - 1 : 0;
+    h.rl_ptr = I(o_rl_ptr);
+    h.rl_col = I(o_rl_col);
+    h.sc_ptr = I(o_sc_ptr);
+    h.sc_pos = I(o_sc_pos);
+    h.sc_piv = I(o_sc_piv);
+    h.ud_ptr = I(o_ud_ptr);
+    h.ud_dst = I(o_ud_dst);
+    h.ud_cptr = I(o_ud_cptr);
+    h.ud_l = I(o_ud_l);
+    h.ud_u = I(o_ud_u);
     ck(cudaMemcpy(impl->d_desc, &h, sizeof(h), cudaMemcpyHostToDevice), "cudaMemcpy(desc)");
 }
 
@@ -384,6 +421,21 @@ void prepare(Prepared &p, const std::string &netlist, const std::vector<std::str
     p.probes = probes;
     p.dev = std::make_unique<DeviceCircuit>();
     p.dev->upload(p.img, probes, outcap, capmax);
+    /* large circuits spread their transistor evaluation over the whole
+     * device; NGSF_WIDE=0/1 overrides the size rule */
+    int transistors = p.img.nb4 + p.img.nmos1;
+    bool wide = transistors >= 1024;
+    if (const char *e = getenv("NGSF_WIDE"))
+        wide = atoi(e) != 0;
+    p.wide = false;
+    p.wide_blocks = 0;
+    if (wide) {
+        int nb = ngsf_wide_blocks();
+        if (nb >= 2) {
+            p.wide = true;
+            p.wide_blocks = nb;
+        }
+    }
     p.dev->upload_lu(p.img);     /* empty plan: the first iteration asks for one */
 }
 
@@ -407,18 +459,44 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
             if (nl > 64 + 8 * (int)cs.size())
                 throw std::runtime_error("too many re-pivot rounds");
             std::vector<ngsf_ckt_t> descs;
-            for (auto *c : pending)
-                descs.push_back(c->dev->desc());
-            ck(cudaMemcpy(d, descs.data(), descs.size() * sizeof(ngsf_ckt_t),
-                          cudaMemcpyHostToDevice), "cudaMemcpy(descs)");
-            cudaEventRecord(e0, 0);
-            ck(ngsf_launch_tran(d, (int)descs.size(), mode, maxSteps, 0), "launch(tran)");
-            cudaEventRecord(e1, 0);
-            ck(cudaEventSynchronize(e1), "tran");
-            float ms = 0;
-            cudaEventElapsedTime(&ms, e0, e1);
-            total += ms * 1e-3;
-            nl++;
+            std::vector<Prepared *> wide;
+            for (auto *c : pending) {
+                if (c->wide)
+                    wide.push_back(c);
+                else
+                    descs.push_back(c->dev->desc());
+            }
+            if (!descs.empty()) {
+                ck(cudaMemcpy(d, descs.data(), descs.size() * sizeof(ngsf_ckt_t),
+                              cudaMemcpyHostToDevice), "cudaMemcpy(descs)");
+                cudaEventRecord(e0, 0);
+                ck(ngsf_launch_tran(d, (int)descs.size(), mode, maxSteps, 0), "launch(tran)");
+                cudaEventRecord(e1, 0);
+                ck(cudaEventSynchronize(e1), "tran");
+                float ms = 0;
+                cudaEventElapsedTime(&ms, e0, e1);
+                total += ms * 1e-3;
+                nl++;
+            }
+            for (auto *c : wide) {
+                /* a fresh hand-over block per launch: command numbers start at 0 */
+                ck(cudaMemset(c->dev->desc().wide, 0, sizeof(ngsf_wide_t)), "cudaMemset(wide)");
+                int nb = c->wide_blocks;
+                cudaEventRecord(e0, 0);
+                ck(ngsf_launch_tran_wide(c->dev->device_desc(), nb, mode, maxSteps, 0),
+                   "launch(tran wide)");
+                cudaEventRecord(e1, 0);
+                ck(cudaEventSynchronize(e1), "tran wide");
+                float ms = 0;
+                cudaEventElapsedTime(&ms, e0, e1);
+                total += ms * 1e-3;
+                nl++;
+                int err = 0;
+                ck(cudaMemcpy(&err, &c->dev->desc().wide->err, sizeof(int),
+                              cudaMemcpyDeviceToHost), "cudaMemcpy(wide err)");
+                if (err)
+                    throw std::runtime_error("wide launch: a block hand-over wait ran out");
+            }
             std::vector<Prepared *> next;
             for (auto *c : pending) {
                 c->dev->read_results(c->ires, c->fres);

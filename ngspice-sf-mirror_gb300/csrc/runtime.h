@@ -45,6 +45,8 @@ struct Prepared {
     std::vector<int> ires;
     std::vector<double> fres;
     std::vector<double> points;   /* [npoints][1 + nprobe] */
+    bool wide = false;            /* run alone over a cooperative grid */
+    int wide_blocks = 0;
 };
 
 void prepare(Prepared &p, const std::string &netlist, const std::vector<std::string> &probes,

@@ -44,12 +44,39 @@ bool plan_lu(int n, const std::vector<int> &cp, const std::vector<int> &ri,
     std::vector<std::vector<int>> Lrows(n), Ucols(n);
     std::vector<char> rowDone(n, 0), colDone(n, 0);
 
+    /* rows holding a single entry: a zero-cost (Markowitz) pivot that the
+     * column-count search would reach late when its column is long, as for
+     * a supply node whose voltage source row is a singleton.  Taking it
+     * first keeps the supply's long row and column out of the fill. */
+    std::set<int> singles;
+    for (int i = 0; i < n; i++)
+        if (rows[i].size() == 1)
+            singles.insert(i);
+
     for (int k = 0; k < n; k++) {
         long bestCost = -1;
         int bp = -1, bq = -1;
         double bmag = 0;
         int examined = 0;
-        for (auto it = colq.begin(); it != colq.end(); ++it) {
+        while (!singles.empty()) {
+            int i = *singles.begin();
+            singles.erase(singles.begin());
+            if (rowDone[i] || rows[i].size() != 1)
+                continue;
+            int q = rows[i].begin()->first;
+            double a = std::fabs(rows[i].begin()->second);
+            double cmax = 0;
+            for (int r : cols[q])
+                cmax = std::max(cmax, std::fabs(rows[r][q]));
+            if (cmax > 0 && a >= pivrel * cmax && a > pivtol) {
+                bestCost = 0;
+                bp = i;
+                bq = q;
+                bmag = a;
+                break;
+            }
+        }
+        for (auto it = colq.begin(); bp < 0 && it != colq.end(); ++it) {
             int q = it->second;
             int cc = it->first;
             if (bestCost >= 0 && (examined >= 6 || (long)(cc - 1) * 0 >= bestCost))
@@ -123,8 +150,11 @@ bool plan_lu(int n, const std::vector<int> &cp, const std::vector<int> &ri,
             if (j != q)
                 colq.insert({(int)cols[j].size(), j});
         }
-        for (int i : Lrows[k])
+        for (int i : Lrows[k]) {
             rows[i].erase(q);
+            if (rows[i].size() == 1)
+                singles.insert(i);
+        }
         colq.erase({(int)cols[q].size(), q});
         cols[q].clear();
         rows[p].clear();
@@ -289,6 +319,99 @@ bool plan_lu(int n, const std::vector<int> &cp, const std::vector<int> &ri,
     };
     group(fl, img.fl_ptr, img.fl_row);
     group(bl, img.bl_ptr, img.bl_row);
+
+    /* Long rows of the triangular solves (a supply node's U row) are
+     * reduced by a warp: per solve level, the rows with more than 32 terms. */
+    auto heavy_rows = [&](const std::vector<int> &ptr, const std::vector<int> &rowsv,
+                          const std::vector<int> &rp, std::vector<int> &hptr,
+                          std::vector<int> &hrow) {
+        int nl = (int)ptr.size() - 1;
+        hptr.assign(nl + 1, 0);
+        hrow.clear();
+        for (int l = 0; l < nl; l++) {
+            for (int r = ptr[l]; r < ptr[l + 1]; r++) {
+                int k = rowsv[r];
+                if (rp[k + 1] - rp[k] > 32)
+                    hrow.push_back(k);
+            }
+            hptr[l + 1] = (int)hrow.size();
+        }
+    };
+    heavy_rows(img.fl_ptr, img.fl_row, img.lr_ptr, img.fh_ptr, img.fh_row);
+    heavy_rows(img.bl_ptr, img.bl_row, img.ur_ptr, img.bh_ptr, img.bh_row);
+
+    /* Right-looking schedule for large matrices: pivots grouped in levels
+     * (a pivot's level is one more than that of every pivot whose column or
+     * row it needs); per level, first the L entries of its pivots are
+     * divided by the pivots, then every later entry receives the products
+     * L(i,k) * U(k,j) of the level's pivots, grouped by destination so that
+     * one thread owns each destination.  The critical path is two barriers
+     * per level instead of a column's whole dependency chain. */
+    {
+        std::vector<int> rl(n, 0);
+        std::vector<std::vector<int>> lrows_of(n);   /* m with L(k,m) != 0 */
+        for (int m = 0; m < n; m++)
+            for (int i : lcol[m])
+                lrows_of[i].push_back(m);
+        for (int k = 0; k < n; k++) {
+            int lv = 0;
+            for (int m : ucol[k])
+                lv = std::max(lv, rl[m] + 1);
+            for (int m : lrows_of[k])
+                lv = std::max(lv, rl[m] + 1);
+            rl[k] = lv;
+        }
+        int nl = 0;
+        for (int k = 0; k < n; k++)
+            nl = std::max(nl, rl[k] + 1);
+        std::vector<std::vector<int>> piv(nl);
+        for (int k = 0; k < n; k++)
+            piv[rl[k]].push_back(k);
+        img.rl_ptr.assign(nl + 1, 0);
+        img.rl_col.clear();
+        img.sc_ptr.assign(nl + 1, 0);
+        img.sc_pos.clear();
+        img.sc_piv.clear();
+        img.ud_ptr.assign(nl + 1, 0);
+        img.ud_dst.clear();
+        img.ud_cptr.assign(1, 0);
+        img.ud_l.clear();
+        img.ud_u.clear();
+        for (int l = 0; l < nl; l++) {
+            std::map<int, std::vector<std::pair<int, int>>> dst;
+            for (int k : piv[l]) {
+                img.rl_col.push_back(k);
+                for (size_t s2 = 0; s2 < lcol[k].size(); s2++) {
+                    img.sc_pos.push_back(img.cdiag[k] + 1 + (int)s2);
+                    img.sc_piv.push_back(img.cdiag[k]);
+                }
+                for (size_t s2 = 0; s2 < lcol[k].size(); s2++) {
+                    int i = lcol[k][s2];
+                    int lpos = img.cdiag[k] + 1 + (int)s2;
+                    for (auto &e : urow[k]) {
+                        int j = e.first, upos = e.second;
+                        int d = posIn(j, i);
+                        if (d < 0) {
+                            err = "internal: fill closure violated (right-looking)";
+                            return false;
+                        }
+                        dst[d].push_back({lpos, upos});
+                    }
+                }
+            }
+            for (auto &de : dst) {
+                img.ud_dst.push_back(de.first);
+                for (auto &c : de.second) {
+                    img.ud_l.push_back(c.first);
+                    img.ud_u.push_back(c.second);
+                }
+                img.ud_cptr.push_back((int)img.ud_l.size());
+            }
+            img.rl_ptr[l + 1] = (int)img.rl_col.size();
+            img.sc_ptr[l + 1] = (int)img.sc_pos.size();
+            img.ud_ptr[l + 1] = (int)img.ud_dst.size();
+        }
+    }
 
     img.prow.resize(n);
     img.pcol.resize(n);

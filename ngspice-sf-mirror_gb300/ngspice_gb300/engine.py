@@ -19,6 +19,7 @@ LIB_PATH = os.path.join(PKG, "lib", "libngspice_gb300.so")
 R_STATUS, R_NPOINTS, R_ACCEPTED, R_REJECTED, R_NUMITER, R_TRANITER, R_TIMEPTS, \
     R_NCAP, R_OPITER, R_BADPIVOT, R_REORDERS = range(11)
 R_COUNT = 11
+F_COUNT = 3
 
 # C-ABI symbols declared in include/*.h
 EXPORTS = [
@@ -136,7 +137,7 @@ class Circuit:
 
     def results(self) -> np.ndarray:
         ires = np.zeros(R_COUNT, np.int32)
-        fres = np.zeros(2)
+        fres = np.zeros(F_COUNT)
         if lib().ngsf_results(self._h, _ptr(ires, C.c_int), _ptr(fres, C.c_double)):
             raise EngineError(last_error())
         return ires

@@ -101,6 +101,17 @@ int port_b4_load_one(int mode, int order, double gmin, double delta, double delt
                      const double *st2, const double *p, double *h, const int *node, int st,
                      double *sv);
 
+/* sparse mode for large circuits (sparse_port.cpp plans the pivots) */
+typedef struct {
+    int n, nnz, nlu, nlevels, nflevels, nblevels;
+    int *a_lupos, *cdiag, *cend, *kptr, *kpos, *kseg, *upd_dst, *upd_src, *prow, *pcol;
+    int *lvl_ptr, *lvl_col, *fl_ptr, *fl_row, *bl_ptr, *bl_row;
+    int *lr_ptr, *lr_col, *lr_pos, *ur_ptr, *ur_col, *ur_pos;
+} port_plan_t;
+int port_plan(int n, const int *cp, const int *ri, const double *ax, double pivrel,
+              double pivtol, port_plan_t *out);
+void port_plan_free(port_plan_t *p);
+
 typedef struct { int a, b; double g; } res_t;
 typedef struct { int a, b, st; double c, m, ic; } cap_t;
 typedef struct {
@@ -123,6 +134,12 @@ typedef struct {
     double tstep, tstop, tstart, tmax, delmin, minbreak;
     int itl1, itl4, maxord;
     /* run state */
+    int sparse;              /* 1: CSC matrix + planned sparse LU */
+    int recording, nrec, caprec, *rec;   /* pattern discovery (sparse) */
+    int *cp, *ri, nnz;       /* CSC pattern, 0-based rows/cols */
+    double *ax, *lux, *work, trash;
+    port_plan_t plan;
+    int havePlan;
     double *A, *LU;          /* dense (n+1)^2, row/col 0 = ground trash */
     int *perm;               /* row permutation of the factorization */
     int haveLU;
@@ -141,7 +158,36 @@ typedef struct {
     int dumpcap, ndump;
 } port_t;
 
-#define A_(c, r, k) ((c)->A[(size_t)(r) * ((c)->n + 1) + (k)])
+/* matrix element (r, k), 1-based; row or column 0 is the ground trash */
+static double *port_elt(port_t *c, int r, int k)
+{
+    if (!c->sparse)
+        return &c->A[(size_t)r * (c->n + 1) + k];
+    if (r == 0 || k == 0)
+        return &c->trash;
+    if (c->recording) {
+        if (c->nrec == c->caprec) {
+            c->caprec = c->caprec ? 2 * c->caprec : 1024;
+            c->rec = realloc(c->rec, sizeof(int) * 2 * (size_t)c->caprec);
+        }
+        c->rec[2 * c->nrec] = k - 1;
+        c->rec[2 * c->nrec + 1] = r - 1;
+        c->nrec++;
+        return &c->trash;
+    }
+    int lo = c->cp[k - 1], hi = c->cp[k] - 1;
+    while (lo <= hi) {
+        int mid = (lo + hi) >> 1;
+        if (c->ri[mid] < r - 1)
+            lo = mid + 1;
+        else if (c->ri[mid] > r - 1)
+            hi = mid - 1;
+        else
+            return &c->ax[mid];
+    }
+    return &c->trash;   /* not reached: every stamped cell is in the pattern */
+}
+#define A_(c, r, k) (*port_elt((c), (r), (k)))
 
 port_t *port_new(int n, int nstates)
 {
@@ -149,8 +195,13 @@ port_t *port_new(int n, int nstates)
     c->n = n;
     c->nstates = nstates;
     c->ntype = calloc((size_t)n + 1, sizeof(int));
-    c->A = calloc((size_t)(n + 1) * (n + 1), sizeof(double));
-    c->LU = calloc((size_t)(n + 1) * (n + 1), sizeof(double));
+    c->sparse = n > 400;
+    if (!c->sparse) {
+        c->A = calloc((size_t)(n + 1) * (n + 1), sizeof(double));
+        c->LU = calloc((size_t)(n + 1) * (n + 1), sizeof(double));
+    } else {
+        c->work = calloc((size_t)n + 1, sizeof(double));
+    }
     c->perm = calloc((size_t)n + 1, sizeof(int));
     c->rhs = calloc((size_t)n + 1, sizeof(double));
     c->rhsOld = calloc((size_t)n + 1, sizeof(double));
@@ -182,6 +233,13 @@ void port_free(port_t *c)
     free(c->mos1);
     free(c->b4);
     free(c->breaks);
+    free(c->rec);
+    free(c->cp);
+    free(c->ri);
+    free(c->ax);
+    free(c->lux);
+    free(c->work);
+    port_plan_free(&c->plan);
     free(c);
 }
 
@@ -913,11 +971,69 @@ static int b4_load(port_t *c)
     return nc;
 }
 
+static int ckt_load_devices(port_t *c);
+
+static int cmp_pair(const void *a, const void *b)
+{
+    const int *x = a, *y = b;
+    if (x[0] != y[0])
+        return x[0] < y[0] ? -1 : 1;
+    return x[1] < y[1] ? -1 : (x[1] > y[1]);
+}
+
+/* sparse mode: discover the matrix pattern from one recording load
+ * (every element a device touches), then keep it for the run */
+static void build_pattern(port_t *c)
+{
+    int n = c->n;
+    c->recording = 1;
+    c->nrec = 0;
+    ckt_load_devices(c);
+    c->recording = 0;
+    for (int j = 0; j < n; j++) {      /* every equation keeps its diagonal */
+        if (c->nrec == c->caprec) {
+            c->caprec = c->caprec ? 2 * c->caprec : 1024;
+            c->rec = realloc(c->rec, sizeof(int) * 2 * (size_t)c->caprec);
+        }
+        c->rec[2 * c->nrec] = j;
+        c->rec[2 * c->nrec + 1] = j;
+        c->nrec++;
+    }
+    qsort(c->rec, (size_t)c->nrec, 2 * sizeof(int), cmp_pair);
+    c->cp = calloc((size_t)n + 1, sizeof(int));
+    c->ri = malloc(sizeof(int) * (size_t)c->nrec);
+    int m = 0;
+    for (int t = 0; t < c->nrec; t++) {
+        if (t && c->rec[2 * t] == c->rec[2 * t - 2] && c->rec[2 * t + 1] == c->rec[2 * t - 1])
+            continue;
+        c->ri[m++] = c->rec[2 * t + 1];
+        c->cp[c->rec[2 * t] + 1]++;
+    }
+    for (int j = 0; j < n; j++)
+        c->cp[j + 1] += c->cp[j];
+    c->nnz = m;
+    c->ax = calloc((size_t)m, sizeof(double));
+}
+
 static int ckt_load(port_t *c)
 {
     int n = c->n;
+    if (c->sparse && !c->cp) {
+        /* the recording pass has the load's side effects (states of the
+         * first iteration); the real pass below repeats them identically */
+        memset(c->rhs, 0, sizeof(double) * (n + 1));
+        build_pattern(c);
+    }
     memset(c->rhs, 0, sizeof(double) * (n + 1));
-    memset(c->A, 0, sizeof(double) * (size_t)(n + 1) * (n + 1));
+    if (c->sparse)
+        memset(c->ax, 0, sizeof(double) * (size_t)c->nnz);
+    else
+        memset(c->A, 0, sizeof(double) * (size_t)(n + 1) * (n + 1));
+    return ckt_load_devices(c);
+}
+
+static int ckt_load_devices(port_t *c)
+{
     /* reference device-table order: bsim4, cap, dio, isrc, mos1, res, vsrc */
     int nc = b4_load(c);
     cap_load(c);
@@ -932,9 +1048,65 @@ static int ckt_load(port_t *c)
 /* dense LU standing in for KLU: pivoting factorization when the        */
 /* reference reorders, refactorization on the same pivots otherwise     */
 /* ------------------------------------------------------------------ */
+/* sparse refactorization on the planned pattern: left-looking, columns
+ * in dependency-level order; fails (asking for new pivots) on a zero or
+ * non-finite pivot or an L entry above 1e6 */
+static int sp_factor(port_t *c)
+{
+    port_plan_t *P = &c->plan;
+    int n = c->n;
+    double *lux = c->lux;
+    memset(lux, 0, sizeof(double) * (size_t)P->nlu);
+    for (int p = 0; p < c->nnz; p++)
+        lux[P->a_lupos[p]] = c->ax[p];
+    if (c->diagGmin != 0)
+        for (int j = 0; j < n; j++)
+            for (int p = c->cp[j]; p < c->cp[j + 1]; p++)
+                if (c->ri[p] == j)
+                    lux[P->a_lupos[p]] += c->diagGmin;
+    for (int l = 0; l < P->nlevels; l++)
+        for (int q = P->lvl_ptr[l]; q < P->lvl_ptr[l + 1]; q++) {
+            int k = P->lvl_col[q];
+            for (int t = P->kptr[k]; t < P->kptr[k + 1]; t++) {
+                double xk = lux[P->kpos[t]];
+                for (int u = P->kseg[t]; u < P->kseg[t + 1]; u++)
+                    lux[P->upd_dst[u]] -= lux[P->upd_src[u]] * xk;
+            }
+            double piv = lux[P->cdiag[k]];
+            if (!(fabs(piv) > 0.0) || !isfinite(piv))
+                return E_SINGULAR;
+            for (int q2 = P->cdiag[k] + 1; q2 < P->cend[k]; q2++) {
+                double lik = lux[q2] / piv;
+                lux[q2] = lik;
+                if (!(fabs(lik) <= 1e6))
+                    return E_SINGULAR;
+            }
+        }
+    return 0;
+}
+
 static int lu_factor(port_t *c, int repivot)
 {
     int n = c->n;
+    if (c->sparse) {
+        if (repivot || !c->havePlan) {
+            double *a = malloc(sizeof(double) * (size_t)c->nnz);
+            memcpy(a, c->ax, sizeof(double) * (size_t)c->nnz);
+            if (c->diagGmin != 0)
+                for (int j = 0; j < n; j++)
+                    for (int p = c->cp[j]; p < c->cp[j + 1]; p++)
+                        if (c->ri[p] == j)
+                            a[p] += c->diagGmin;
+            int rc = port_plan(n, c->cp, c->ri, a, c->pivrel, c->pivtol, &c->plan);
+            free(a);
+            if (rc != 0)
+                return E_SINGULAR;
+            c->havePlan = 1;
+            free(c->lux);
+            c->lux = malloc(sizeof(double) * (size_t)c->plan.nlu);
+        }
+        return sp_factor(c);
+    }
     double *L = c->LU;
     for (int r = 1; r <= n; r++)
         for (int k = 1; k <= n; k++)
@@ -997,9 +1169,40 @@ static int lu_factor(port_t *c, int repivot)
     return 0;
 }
 
+static void sp_solve(port_t *c, double *b)
+{
+    port_plan_t *P = &c->plan;
+    int n = c->n;
+    double *w = c->work, *lux = c->lux;
+    for (int k = 0; k < n; k++)
+        w[k] = b[P->prow[k]];
+    for (int l = 0; l < P->nflevels; l++)
+        for (int r = P->fl_ptr[l]; r < P->fl_ptr[l + 1]; r++) {
+            int k = P->fl_row[r];
+            double acc = w[k];
+            for (int q = P->lr_ptr[k]; q < P->lr_ptr[k + 1]; q++)
+                acc -= lux[P->lr_pos[q]] * w[P->lr_col[q]];
+            w[k] = acc;
+        }
+    for (int l = 0; l < P->nblevels; l++)
+        for (int r = P->bl_ptr[l]; r < P->bl_ptr[l + 1]; r++) {
+            int k = P->bl_row[r];
+            double acc = w[k];
+            for (int q = P->ur_ptr[k]; q < P->ur_ptr[k + 1]; q++)
+                acc -= lux[P->ur_pos[q]] * w[P->ur_col[q]];
+            w[k] = acc / lux[P->cdiag[k]];
+        }
+    for (int k = 0; k < n; k++)
+        b[P->pcol[k]] = w[k];
+}
+
 static void lu_solve(port_t *c, double *b)
 {
     int n = c->n;
+    if (c->sparse) {
+        sp_solve(c, b);
+        return;
+    }
     double *L = c->LU;
     double *y = malloc(sizeof(double) * (n + 1));
     for (int i = 1; i <= n; i++) {
@@ -1040,7 +1243,7 @@ static int conv_test(port_t *c)
 
 static void dump(port_t *c)
 {
-    if (c->ndump >= c->dumpcap)
+    if (c->ndump >= c->dumpcap || c->sparse)
         return;
     int n = c->n, k = c->ndump++;
     if (c->dump_ax)

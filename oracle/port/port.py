@@ -43,7 +43,8 @@ def build(force: bool = False) -> str:
     model arithmetic (g++) into oracle/_port/libngport.so, without
     floating-point contraction."""
     src = os.path.join(HERE, "port.c")
-    cxx = [os.path.join(HERE, "b4port.cpp"), os.path.join(CSRC, "bsim4_setup.cpp")]
+    cxx = [os.path.join(HERE, "b4port.cpp"), os.path.join(HERE, "sparse_port.cpp"),
+           os.path.join(CSRC, "bsim4_setup.cpp"), os.path.join(CSRC, "sparse.cpp")]
     deps = [src] + cxx + [os.path.join(CSRC, f) for f in os.listdir(CSRC)
                           if f.endswith((".h", ".cuh", ".def"))]
     os.makedirs(OUT, exist_ok=True)
