@@ -81,6 +81,39 @@ NGSF_API int ngsf_workload(const ngsf_handle *h, long long *counts);
 /* device bytes held by the circuit */
 NGSF_API long long ngsf_device_bytes(const ngsf_handle *h);
 
+/* First-iteration stamps of an opened circuit, with no allocation.
+ *
+ * No reference counterpart: it evaluates what the reference's first Newton
+ * iteration hands to the factorization -- CKTload in MODETRANOP |
+ * MODEINITJCT from zero state -- and copies the stamped matrix (ax[nnz], CSC
+ * order of ngsf_pattern) and right-hand side (rhs[n+1], rhs[0] = ground) to
+ * the caller's host buffers.  The result equals the first matrix and
+ * right-hand side ngsf_capture records for the same circuit.
+ *
+ * Why it exists: the call allocates nothing -- no cudaMalloc/cudaFree and
+ * no allocating library routine.  Every array the launch writes lives in one
+ * file-scope static device array of the library (8 MiB); the circuit's own
+ * device memory is only read.  Callers that cannot allocate device memory
+ * when they need the stamps can use it: a process whose device memory is
+ * already handed out to a framework's pool, a loop that must not pay for the
+ * device-wide synchronisation cudaFree implies, an embedder with a fixed
+ * memory budget.
+ *
+ * Limits and rules:
+ * - a circuit whose arrays need more than the 8 MiB is refused: -1, and
+ *   ngsf_last_error() names the size it would need;
+ * - nothing in the static array has to start at zero: the launch clears the
+ *   state vectors, right-hand sides and per-instance memories itself, and
+ *   every device rewrites all of its stamp slots;
+ * - the first call on a device looks the static array up
+ *   (cudaGetSymbolAddress, with that device current) and keeps the address;
+ *   make that first call before any stream capture begins;
+ * - there is one static array per device: calls that overlap in time (from
+ *   several threads, or while an earlier call's work is still running)
+ *   race on it and must be serialised by the caller.
+ * Returns 0, or -1 with ngsf_last_error() set. */
+NGSF_API int ngsf_stamp_initial_static(const ngsf_handle *h, double *ax, double *rhs);
+
 #ifdef __cplusplus
 }
 #endif

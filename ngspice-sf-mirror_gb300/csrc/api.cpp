@@ -34,6 +34,17 @@ struct ngsf_handle {
 namespace {
 thread_local std::string g_err;
 thread_local int g_launches = 0;
+}  // namespace
+
+/* internal (not exported): engine.cu entry points reach a handle's device
+ * descriptor and report errors through ngsf_last_error() */
+extern "C" const ngsf_ckt_t *ngsf_internal_desc(const ngsf_handle *h)
+{
+    return (h && h->p.dev) ? &h->p.dev->desc() : nullptr;
+}
+extern "C" void ngsf_internal_set_error(const char *msg) { g_err = msg ? msg : ""; }
+
+namespace {
 
 int fail(const std::string &msg, int code = -1)
 {

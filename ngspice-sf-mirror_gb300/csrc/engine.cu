@@ -23,9 +23,12 @@
  */
 #include <cuda_runtime.h>
 #include <cuda/atomic>
+#include <mutex>
+#include <string>
 #include <math.h>
 #include <stdint.h>
 
+#include "../../include/ngspice_gb300.h"
 #include "ngsf_types.h"
 #include "devsup.cuh"
 
@@ -2073,6 +2076,29 @@ __device__ void run_circuit(const ngsf_ckt_t &C, Ctl &s, int runMode, long long 
 
 }  // namespace
 
+/* ---------------------------------------------------------------- */
+/* First-iteration stamps without allocation                          */
+/* ---------------------------------------------------------------- */
+/* The operating-point initialisation load of one circuit (CKTload in
+ * MODETRANOP | MODEINITJCT from zero state: the matrix and right-hand side
+ * that the first Newton iteration hands to the factorization), with every
+ * mutable array of the launch -- state vectors, right-hand sides, stamp
+ * slots, matrix values, per-instance memories, result words -- placed in
+ * this file-scope device array instead of device memory owned by the
+ * circuit.  8 MiB: a few thousand transistors; larger circuits are refused. */
+#define NGSF_STATIC_SCRATCH_BYTES (8u << 20)
+static __device__ __align__(256) unsigned char g_static_scratch[NGSF_STATIC_SCRATCH_BYTES];
+
+__global__ void __launch_bounds__(NGSF_THREADS) stamp_static_kernel(ngsf_ckt_t C)
+{
+    __shared__ Ctl s;
+    __shared__ __align__(16) ngsf_ckt_t Cs;
+    if (threadIdx.x == 0)
+        Cs = C;
+    __syncthreads();
+    run_circuit(Cs, s, RUN_PROBE, 0);
+}
+
 static_assert(sizeof(Ctl) <= NGSF_WIDE_CTL_BYTES, "control block does not fit the wide hand-over");
 
 extern "C" int ngsf_ctl_bytes(void) { return (int)sizeof(Ctl); }
@@ -2089,6 +2115,110 @@ extern "C" int ngsf_wide_blocks(void)
         cudaSuccess)
         return 0;
     return sms * per;
+}
+
+extern "C" const ngsf_ckt_t *ngsf_internal_desc(const ngsf_handle *h);
+extern "C" void ngsf_internal_set_error(const char *msg);
+
+namespace {
+
+/* Device address of g_static_scratch, looked up once per device (with
+ * that device current) and kept for later calls. */
+void *static_scratch(int dev, std::string &err)
+{
+    static std::mutex mu;
+    static void *addr[64] = {nullptr};
+    if (dev < 0 || dev >= 64) {
+        err = "device ordinal out of range";
+        return nullptr;
+    }
+    std::lock_guard<std::mutex> lock(mu);
+    if (!addr[dev]) {
+        void *p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+        if (e != cudaSuccess) {
+            err = std::string("cudaGetSymbolAddress(static scratch): ") + cudaGetErrorString(e);
+            return nullptr;
+        }
+        addr[dev] = p;
+    }
+    return addr[dev];
+}
+
+}  // namespace
+
+extern "C" NGSF_API int ngsf_stamp_initial_static(const ngsf_handle *h, double *ax, double *rhs)
+{
+    const ngsf_ckt_t *d = ngsf_internal_desc(h);
+    if (!d) {
+        ngsf_internal_set_error("ngsf_stamp_initial_static: null or host-only handle");
+        return -1;
+    }
+    /* layout of the mutable arrays, each on a 256-byte boundary */
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        size_t o = off;
+        off += (bytes + 255) & ~(size_t)255;
+        return o;
+    };
+    const size_t n1 = (size_t)d->n + 1;
+    size_t o_states = take(4 * ((size_t)d->nstates + 1) * sizeof(double));
+    size_t o_rhs = take(n1 * sizeof(double));
+    size_t o_rhsOld = take(n1 * sizeof(double));
+    size_t o_stampv = take((size_t)d->nstamp * sizeof(double));
+    size_t o_ax = take((size_t)d->nnz * sizeof(double));
+    size_t o_m1h = take((size_t)M1H_COUNT * d->mos1.n * sizeof(double));
+    size_t o_b4h = take((size_t)B4H_COUNT * d->bsim4.n * sizeof(double));
+    size_t o_vbrk = take((size_t)d->vsrc.n * sizeof(double));
+    size_t o_ibrk = take((size_t)d->isrc.n * sizeof(double));
+    size_t o_res = take(NGSF_R_COUNT * sizeof(int));
+    size_t o_fres = take(NGSF_F_COUNT * sizeof(double));
+    if (off > NGSF_STATIC_SCRATCH_BYTES) {
+        std::string m = "ngsf_stamp_initial_static: the circuit needs " + std::to_string(off) +
+                        " bytes of scratch, more than the static " +
+                        std::to_string((size_t)NGSF_STATIC_SCRATCH_BYTES) + " bytes";
+        ngsf_internal_set_error(m.c_str());
+        return -1;
+    }
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) {
+        ngsf_internal_set_error(cudaGetErrorString(e));
+        return -1;
+    }
+    std::string err;
+    unsigned char *base = (unsigned char *)static_scratch(dev, err);
+    if (!base) {
+        ngsf_internal_set_error(err.c_str());
+        return -1;
+    }
+    ngsf_ckt_t c = *d;
+    c.states = (double *)(base + o_states);
+    c.rhs = (double *)(base + o_rhs);
+    c.rhsOld = (double *)(base + o_rhsOld);
+    c.stampv = (double *)(base + o_stampv);
+    c.ax = (double *)(base + o_ax);
+    c.mos1.h = (double *)(base + o_m1h);
+    c.bsim4.h = (double *)(base + o_b4h);
+    c.vsrc.brk = (double *)(base + o_vbrk);
+    c.isrc.brk = (double *)(base + o_ibrk);
+    c.result = (int *)(base + o_res);
+    c.fresult = (double *)(base + o_fres);
+    c.capmax = 0;
+    c.wide = nullptr;
+    stamp_static_kernel<<<1, NGSF_THREADS>>>(c);
+    e = cudaGetLastError();
+    if (e == cudaSuccess && ax)
+        e = cudaMemcpy(ax, c.ax, (size_t)d->nnz * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess && rhs)
+        e = cudaMemcpy(rhs, c.rhs, n1 * sizeof(double), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess)
+        e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        ngsf_internal_set_error(cudaGetErrorString(e));
+        return -1;
+    }
+    return 0;
 }
 
 extern "C" cudaError_t ngsf_launch_tran_wide(const ngsf_ckt_t *d_ckt, int nblocks, int runMode,

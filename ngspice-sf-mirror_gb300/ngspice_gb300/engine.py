@@ -26,7 +26,7 @@ EXPORTS = [
     "ngsf_open", "ngsf_compile", "ngsf_close", "ngsf_last_error", "ngsf_info",
     "ngsf_eq_name", "ngsf_pattern", "ngsf_probes", "ngsf_run", "ngsf_results",
     "ngsf_points", "ngsf_capture", "ngsf_lu_flops", "ngsf_device_bytes",
-    "ngsf_last_launches", "ngsf_workload",
+    "ngsf_last_launches", "ngsf_workload", "ngsf_stamp_initial_static",
     "ngSpice_Init", "ngSpice_Init_Sync", "ngSpice_Command", "ngGet_Vec_Info",
     "ngSpice_Circ", "ngSpice_CurPlot", "ngSpice_AllPlots", "ngSpice_AllVecs",
     "ngSpice_running", "ngSpice_SetBkpt", "ngSpice_nospinit", "ngSpice_nospiceinit",
