@@ -123,28 +123,7 @@ NGSF_HD inline void b4_tat(double vts, double Nvtmr, double v, double &T, double
  * (const.h CONSTboltz * REFTEMP / CHARGE), the pnjlim scale of BSIM4. */
 #define B4_CONSTVT0 (1.38064852e-23 * (27.0 + 273.15) / 1.6021766208e-19)
 
-/* Iteration context of one BSIM4 load: what BSIM4load reads from the
- * circuit besides its own instance (CKTmode, CKTgmin, CKTdelta,
- * CKTdeltaOld[1], CKTag[0..1], CKTorder, CKTrhsOld, CKTstate0..2). */
-struct B4Ctx {
-    int mode;
-    int order;
-    double gmin, delta, deltaOld1, ag0, ag1;
-    const double *rhsOld;
-    double *st0;
-    double *st1;
-    const double *st2;
-};
-
-/* NIintegrate, trapezoidal (src/maths/ni/niinteg.c:18-80) for a charge at
- * state offset q whose current lives at q+1 */
-NGSF_HD inline void b4_integrate(const B4Ctx &x, double *st0, const double *st1, int q)
-{
-    if (x.order == 1)
-        st0[q + 1] = x.ag0 * st0[q] + x.ag1 * st1[q];
-    else
-        st0[q + 1] = -st1[q + 1] * x.ag1 + x.ag0 * (st0[q] - st1[q]);
-}
+typedef DevCtx B4Ctx;
 
 #include "bsim4_eval.cuh"
 

@@ -159,6 +159,10 @@ struct Image {
 void bsim4_params(const Circuit &c, const Model &m, const Instance &in, double *p,
                   bool &needDp, bool &needSp);
 
+/* Junction diode resolution (dio_setup.cpp): fills DIP_COUNT values. */
+void dio_params(const Circuit &c, const Model &m, const Instance &in, double *p,
+                bool &needPosPrime);
+
 /* CKTsetup + CKTtemp + SMPpreOrder equivalent. */
 void compile(Circuit &c, Image &img);
 

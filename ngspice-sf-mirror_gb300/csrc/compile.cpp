@@ -20,6 +20,7 @@
 #include <numeric>
 
 #include "bsim4.h"
+#include "dio.h"
 #include "circuit.h"
 
 namespace ngsf {
@@ -297,6 +298,7 @@ void compile(Circuit &c, Image &img)
     /* ---------------- setup: internal nodes, branches, states -------- */
     std::vector<std::array<double, M1P_COUNT>> m1p;
     std::vector<std::array<double, B4P_COUNT>> b4p;
+    std::vector<std::array<double, DIP_COUNT>> dip;
     int states = 0;
     for (int kind = 0; kind < K_COUNT; kind++) {
         for (int idx : c.order[kind]) {
@@ -317,8 +319,21 @@ void compile(Circuit &c, Image &img)
                 b4p.push_back(p);
                 break;
             }
-            case K_DIO:
-                throw NetlistError("diode instance " + in.name + ": device kind not built");
+            case K_DIO: {
+                /* DIOsetup: states, then the series-resistance node */
+                in.states = states;
+                states += DIS_COUNT;
+                if (in.model < 0)
+                    throw NetlistError("diode " + in.name + " needs a model");
+                std::array<double, DIP_COUNT> p{};
+                bool needPP;
+                dio_params(c, c.models[in.model], in, p.data(), needPP);
+                int pos = in.nodes[0], neg = in.nodes[1];
+                int pp = needPP ? mk_internal(c, in.name + "#internal", true) : pos;
+                in.inodes = {pos, neg, pp};
+                dip.push_back(p);
+                break;
+            }
             case K_CAP:
                 in.states = states;
                 states += 2;
@@ -451,6 +466,38 @@ void compile(Circuit &c, Image &img)
             }
         });
     }
+    /* DIO: DIOload order (dioload.c:785-815) */
+    {
+        const auto &ord = c.order[K_DIO];
+        int nk = (int)ord.size();
+        img.ndio = nk;
+        img.dio_node.assign(DIN_COUNT * nk, 0);
+        img.dio_st.assign(nk, 0);
+        img.dio_p.assign((size_t)DIP_COUNT * nk, 0.0);
+        for (int i = 0; i < nk; i++) {
+            const Instance &in = c.inst[ord[i]];
+            for (int t = 0; t < DIN_COUNT; t++)
+                img.dio_node[t * nk + i] = in.inodes[t];
+            img.dio_st[i] = in.states;
+            for (int t = 0; t < DIP_COUNT; t++)
+                img.dio_p[(size_t)t * nk + i] = dip[i][t];
+        }
+        img.dio_stamp0 = add_kind(nk, DIO_NSTAMP, [&](int i, int k) -> Stamp {
+            int P = img.dio_node[DIN_POS * nk + i], N = img.dio_node[DIN_NEG * nk + i];
+            int PP = img.dio_node[DIN_POSP * nk + i];
+            switch (k) {
+            case 0: return {-1, N};
+            case 1: return {-1, PP};
+            case 2: return {P, P};
+            case 3: return {N, N};
+            case 4: return {PP, PP};
+            case 5: return {P, PP};
+            case 6: return {N, PP};
+            case 7: return {PP, P};
+            default: return {PP, N};
+            }
+        });
+    }
     /* ISRC */
     auto fill_src = [&](int kind, std::vector<int> &node, std::vector<int> &wk,
                         std::vector<int> &nc, std::vector<double> &coef,
@@ -467,8 +514,12 @@ void compile(Circuit &c, Image &img)
         mv.assign(nk, 1.0);
         for (int i = 0; i < nk; i++) {
             const Instance &in = c.inst[ord[i]];
-            node[i] = in.nodes[0];
-            node[nk + i] = in.nodes[1];
+            /* the current source's instance struct lists its negative node
+             * first (isrcdefs.h:30-31), so the first netlist node binds to
+             * ISRCnegNode; the voltage source lists the positive node first */
+            bool isrc = kind == K_ISRC;
+            node[i] = in.nodes[isrc ? 1 : 0];
+            node[nk + i] = in.nodes[isrc ? 0 : 1];
             node[2 * nk + i] = in.branch;
             wk[i] = in.wf.kind;
             nc[i] = (int)in.wf.coef.size();

@@ -114,4 +114,35 @@ NGSF_HD inline double dev_fetlim(double vnew, double vold, double vto)
 
 /* DEVqmeyer: Meyer gate capacitances (devsup.c:674-736) */
 
+/* Iteration context a device load reads besides its own instance:
+ * CKTmode, CKTorder, CKTgmin, CKTdelta, CKTdeltaOld[1], CKTag[0..1],
+ * CKTrhsOld and the state vectors CKTstate0..2. */
+struct DevCtx {
+    int mode;
+    int order;
+    double gmin, delta, deltaOld1, ag0, ag1;
+    const double *rhsOld;
+    double *st0;
+    double *st1;
+    const double *st2;
+};
+
+/* NIintegrate, trapezoidal (src/maths/ni/niinteg.c:18-80) for a charge at
+ * state offset q whose current lives at q+1 */
+NGSF_HD inline void dev_integrate(const DevCtx &x, double *st0, const double *st1, int q)
+{
+    if (x.order == 1)
+        st0[q + 1] = x.ag0 * st0[q] + x.ag1 * st1[q];
+    else
+        st0[q + 1] = -st1[q + 1] * x.ag1 + x.ag0 * (st0[q] - st1[q]);
+}
+
+/* DEVpred (src/spicelib/devices/devsup.c:815-827): linear extrapolation of
+ * a state from the two previous time points */
+NGSF_HD inline double dev_pred(const DevCtx &x, const double *st1, const double *st2, int q)
+{
+    double xfact = x.delta / x.deltaOld1;
+    return ((1 + xfact) * st1[q]) - (xfact * st2[q]);
+}
+
 #endif

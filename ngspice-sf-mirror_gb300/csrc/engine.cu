@@ -770,6 +770,29 @@ __device__ int mos1_conv_one(const ngsf_ckt_t &C, const Iter &it, int i)
 }
 
 #include "bsim4_load.cuh"
+#include "dio_eval.cuh"
+
+__device__ int dio_load_one(const ngsf_ckt_t &C, const Ctl &s, const Iter &it, int i)
+{
+    const ngsf_dio_t &K = C.dio;
+    const int n = K.n;
+    DevCtx x;
+    x.mode = s.mode;
+    x.order = s.order;
+    x.gmin = s.gmin;
+    x.delta = s.delta;
+    x.deltaOld1 = s.deltaOld[1];
+    x.ag0 = s.ag[0];
+    x.ag1 = s.ag[1];
+    x.rhsOld = it.rhsOld;
+    x.st0 = it.st0;
+    x.st1 = const_cast<double *>(it.st1);
+    x.st2 = it.st2;
+    int node[DIN_COUNT];
+    for (int t = 0; t < DIN_COUNT; t++)
+        node[t] = K.node[t * n + i];
+    return dio_eval(x, K.p + i, (size_t)n, node, K.st[i], C.stampv + K.stamp0 + i, (size_t)n);
+}
 
 __device__ int bsim4_load_one(const ngsf_ckt_t &C, const Ctl &s, const Iter &it, int i)
 {
@@ -900,6 +923,8 @@ __device__ int ckt_load(const ngsf_ckt_t &C, Ctl &s, const Iter &it)
             wide_issue(C, s, NGSF_WIDE_LOAD);
         nc = wide_transistors(C, s, it, 0, gridDim.x);
         cap_load(C, s, it);
+        for (int i = threadIdx.x; i < C.dio.n; i += blockDim.x)
+            nc |= dio_load_one(C, s, it, i);
         res_load(C);
         src_load(C, s);
         nc = block_or(s, nc);
@@ -914,6 +939,8 @@ __device__ int ckt_load(const ngsf_ckt_t &C, Ctl &s, const Iter &it)
         for (int i = threadIdx.x; i < C.bsim4.n; i += blockDim.x)
             nc |= bsim4_load_one(C, s, it, i);
         cap_load(C, s, it);
+        for (int i = threadIdx.x; i < C.dio.n; i += blockDim.x)
+            nc |= dio_load_one(C, s, it, i);
         for (int i = threadIdx.x; i < C.mos1.n; i += blockDim.x)
             nc |= mos1_load_one(C, s, it, i);
         res_load(C);
@@ -1169,6 +1196,8 @@ __device__ double ckt_trunc(const ngsf_ckt_t &C, Ctl &s, double timeStep)
     double t = 1e300;   /* HUGE */
     for (int i = threadIdx.x; i < C.cap.n; i += blockDim.x)
         t = ckt_terr(C, s, C.cap.st[i], t);
+    for (int i = threadIdx.x; i < C.dio.n; i += blockDim.x)
+        t = ckt_terr(C, s, C.dio.st[i] + DIS_CAPCHARGE, t);
     for (int i = threadIdx.x; i < C.bsim4.n; i += blockDim.x) {
         int b = C.bsim4.st[i];
         t = ckt_terr(C, s, b + B4S_QB, t);

@@ -96,27 +96,13 @@ typedef struct {
     int stamp0;           /* first stamp slot; slot = stamp0 + k*n + i */
 } ngsf_bsim4_t;
 
-/* -------- diode ------------------------------------------------------- */
-enum { DN_POS, DN_NEG, DN_POSP, DN_COUNT };
-enum {
-    DP_VT, DP_VTE, DP_TSAT, DP_TSATSW, DP_VCRIT, DP_TBRKDWN, DP_BVGIVEN,
-    DP_GSPR, DP_TJCTCAP, DP_TJCTSWCAP, DP_TDEPCAP, DP_TJCTPOT, DP_TJCTSWPOT,
-    DP_TGRADE, DP_TGRADESW, DP_F1, DP_F2, DP_F3, DP_F2SW, DP_F3SW, DP_TTT,
-    DP_AREA_M, DP_M, DP_GMIN_EXTRA, DP_OFF, DP_INITCOND, DP_TDEPSWCAP,
-    DP_F1SW, DP_COUNT
-};
-enum { DH_CAP, DH_COUNT };
-enum { DS_VOLTAGE, DS_CURRENT, DS_CONDUCT, DS_CAPCHARGE, DS_CAPCURRENT, DS_COUNT };
-#define D_NSTAMP_MAT 7
-#define D_NSTAMP_RHS 2
-#define D_NSTAMP (D_NSTAMP_MAT + D_NSTAMP_RHS)
-
+/* -------- diode (field enums in dio.h) --------------------------------- */
 typedef struct {
     int n;
-    const int *node;      /* [DN_COUNT][n] */
+    const int *node;      /* [DIN_COUNT][n] */
     const int *st;
-    const double *p;      /* [DP_COUNT][n] */
-    double *h;            /* [DH_COUNT][n] */
+    const double *p;      /* [DIP_COUNT][n] */
+    double *h;            /* unused */
     int stamp0;
 } ngsf_dio_t;
 

@@ -109,6 +109,7 @@ void DeviceCircuit::upload(const Image &img, const std::vector<int> &probes, int
     const int nnz = (int)img.a_ri.size();
     struct Off {
         size_t b4_node, b4_st, b4_p, b4_h;
+        size_t dio_node, dio_st, dio_p;
         size_t mos1_node, mos1_st, mos1_p, mos1_h;
         size_t res_node, res_g;
         size_t cap_node, cap_st, cap_c, cap_m, cap_ic;
@@ -124,6 +125,9 @@ void DeviceCircuit::upload(const Image &img, const std::vector<int> &probes, int
     o.b4_st = puti(img.b4_st);
     o.b4_p = putd(img.b4_p);
     o.b4_h = zero((size_t)B4H_COUNT * img.nb4 * sizeof(double));
+    o.dio_node = puti(img.dio_node);
+    o.dio_st = puti(img.dio_st);
+    o.dio_p = putd(img.dio_p);
     o.mos1_node = puti(img.mos1_node);
     o.mos1_st = puti(img.mos1_st);
     o.mos1_p = putd(img.mos1_p);
@@ -200,6 +204,7 @@ void DeviceCircuit::upload(const Image &img, const std::vector<int> &probes, int
     h.nnz = nnz;
     h.opt = img.opt;
     h.bsim4 = {img.nb4, I(o.b4_node), I(o.b4_st), D(o.b4_p), D(o.b4_h), img.b4_stamp0};
+    h.dio = {img.ndio, I(o.dio_node), I(o.dio_st), D(o.dio_p), nullptr, img.dio_stamp0};
     h.mos1 = {img.nmos1, I(o.mos1_node), I(o.mos1_st), D(o.mos1_p), D(o.mos1_h),
               img.mos1_stamp0};
     h.res = {img.nres, I(o.res_node), D(o.res_g), img.res_stamp0};

@@ -13,6 +13,7 @@
 #include <string>
 
 #include "../../ngspice-sf-mirror_gb300/csrc/bsim4_load.cuh"
+#include "../../ngspice-sf-mirror_gb300/csrc/dio_eval.cuh"
 #include "../../ngspice-sf-mirror_gb300/csrc/circuit.h"
 
 extern "C" int port_b4_nparam(void) { return B4P_COUNT; }
@@ -93,4 +94,61 @@ extern "C" void port_b4_pattern(int *rows, int *cols)
         rows[k] = pat[k][0];
         cols[k] = pat[k][1];
     }
+}
+
+/* ---------------- junction diode (shared evaluation, as above) -------- */
+extern "C" int port_dio_nparam(void) { return DIP_COUNT; }
+extern "C" int port_dio_nstate(void) { return DIS_COUNT; }
+
+extern "C" int port_dio_params(const char *mname, int nm, const char **mkeys, const double *mvals,
+                               const char *iname, int ni, const char **ikeys, const double *ivals,
+                               double temp, double tnom, double reltol, double *out,
+                               int *needPosPrime, char *err, int errlen)
+{
+    try {
+        ngsf::Circuit c;
+        c.opt.temp = temp;
+        c.opt.tnom = tnom;
+        c.opt.reltol = reltol;
+        ngsf::Model m;
+        m.name = mname;
+        m.kind = ngsf::K_DIO;
+        for (int k = 0; k < nm; k++)
+            m.p.v[mkeys[k]] = mvals[k];
+        ngsf::Instance in;
+        in.name = iname;
+        in.kind = ngsf::K_DIO;
+        for (int k = 0; k < ni; k++)
+            in.p.v[ikeys[k]] = ivals[k];
+        bool pp = false;
+        ngsf::dio_params(c, m, in, out, pp);
+        *needPosPrime = pp;
+        return 0;
+    } catch (const std::exception &e) {
+        if (err && errlen > 0) {
+            std::strncpy(err, e.what(), (size_t)errlen - 1);
+            err[errlen - 1] = 0;
+        }
+        return -1;
+    }
+}
+
+extern "C" int port_dio_load_one(int mode, int order, double gmin, double delta,
+                                 double deltaOld1, double ag0, double ag1, const double *rhsOld,
+                                 double *st0, double *st1, const double *st2, const double *p,
+                                 const int *node, int st, double *sv)
+{
+    DevCtx x;
+    x.mode = mode;
+    x.order = order;
+    x.gmin = gmin;
+    x.delta = delta;
+    x.deltaOld1 = deltaOld1;
+    x.ag0 = ag0;
+    x.ag1 = ag1;
+    x.rhsOld = rhsOld;
+    x.st0 = st0;
+    x.st1 = st1;
+    x.st2 = st2;
+    return dio_eval(x, p, 1, node, st, sv, 1);
 }

@@ -112,6 +112,18 @@ int port_plan(int n, const int *cp, const int *ri, const double *ax, double pivr
               double pivtol, port_plan_t *out);
 void port_plan_free(port_plan_t *p);
 
+/* junction diode through the shared evaluation (b4port.cpp) */
+#define DIO_MAXPARAM 64
+typedef struct {
+    int node[3];        /* pos neg pos' */
+    int st;
+    double p[DIO_MAXPARAM];
+} dio_t;
+int port_dio_nparam(void);
+int port_dio_load_one(int mode, int order, double gmin, double delta, double deltaOld1,
+                      double ag0, double ag1, const double *rhsOld, double *st0, double *st1,
+                      const double *st2, const double *p, const int *node, int st, double *sv);
+
 typedef struct { int a, b; double g; } res_t;
 typedef struct { int a, b, st; double c, m, ic; } cap_t;
 typedef struct {
@@ -123,12 +135,13 @@ typedef struct {
     int n, nstates;
     int *ntype;
     /* devices in reference iteration order */
-    int nres, ncap, nvsrc, nisrc, nmos1, nb4;
+    int nres, ncap, nvsrc, nisrc, nmos1, nb4, ndio;
     res_t *res;
     cap_t *cap;
     src_t *vsrc, *isrc;
     mos1_t *mos1;
     b4_t *b4;
+    dio_t *dio;
     /* options */
     double reltol, abstol, vntol, chgtol, trtol, gmin0, pivtol, pivrel, xmu;
     double tstep, tstop, tstart, tmax, delmin, minbreak;
@@ -232,6 +245,7 @@ void port_free(port_t *c)
     free(c->isrc);
     free(c->mos1);
     free(c->b4);
+    free(c->dio);
     free(c->breaks);
     free(c->rec);
     free(c->cp);
@@ -304,6 +318,17 @@ void port_add_b4(port_t *c, const int *nodes, int st, const double *p)
     memcpy(m.p, p, sizeof(double) * port_b4_nparam());
     c->b4 = realloc(c->b4, sizeof(b4_t) * (c->nb4 + 1));
     c->b4[c->nb4++] = m;
+}
+
+void port_add_dio(port_t *c, const int *nodes, int st, const double *p)
+{
+    dio_t d;
+    memset(&d, 0, sizeof d);
+    memcpy(d.node, nodes, sizeof d.node);
+    d.st = st;
+    memcpy(d.p, p, sizeof(double) * port_dio_nparam());
+    c->dio = realloc(c->dio, sizeof(dio_t) * (c->ndio + 1));
+    c->dio[c->ndio++] = d;
 }
 
 void port_set_output(port_t *c, double *out, int outcap)
@@ -1015,6 +1040,30 @@ static void build_pattern(port_t *c)
     c->ax = calloc((size_t)m, sizeof(double));
 }
 
+/* DIOload (src/spicelib/devices/dio/dioload.c:785-815 stamp order) */
+static int dio_load(port_t *c)
+{
+    int nc = 0;
+    double sv[9];
+    for (int i = 0; i < c->ndio; i++) {
+        dio_t *d = &c->dio[i];
+        nc |= port_dio_load_one(c->mode, c->order, c->gmin, c->delta, c->deltaOld[1], c->ag[0],
+                                c->ag[1], c->rhsOld, c->states[0], c->states[1], c->states[2],
+                                d->p, d->node, d->st, sv);
+        int P = d->node[0], N = d->node[1], PP = d->node[2];
+        c->rhs[N] += sv[0];
+        c->rhs[PP] += sv[1];
+        A_(c, P, P) += sv[2];
+        A_(c, N, N) += sv[3];
+        A_(c, PP, PP) += sv[4];
+        A_(c, P, PP) += sv[5];
+        A_(c, N, PP) += sv[6];
+        A_(c, PP, P) += sv[7];
+        A_(c, PP, N) += sv[8];
+    }
+    return nc;
+}
+
 static int ckt_load(port_t *c)
 {
     int n = c->n;
@@ -1037,6 +1086,7 @@ static int ckt_load_devices(port_t *c)
     /* reference device-table order: bsim4, cap, dio, isrc, mos1, res, vsrc */
     int nc = b4_load(c);
     cap_load(c);
+    nc |= dio_load(c);
     src_load(c);
     nc |= mos1_load(c);
     res_load(c);
@@ -1617,6 +1667,8 @@ static double trunc_step(port_t *c, double timeStep)
     }
     for (int i = 0; i < c->ncap; i++)
         t = terr(c, c->cap[i].st, t);
+    for (int i = 0; i < c->ndio; i++)
+        t = terr(c, c->dio[i].st + 6, t);   /* capCharge */
     for (int i = 0; i < c->nmos1; i++) {
         t = terr(c, c->mos1[i].st + S_QGS, t);
         t = terr(c, c->mos1[i].st + S_QGD, t);

@@ -44,7 +44,8 @@ def build(force: bool = False) -> str:
     floating-point contraction."""
     src = os.path.join(HERE, "port.c")
     cxx = [os.path.join(HERE, "b4port.cpp"), os.path.join(HERE, "sparse_port.cpp"),
-           os.path.join(CSRC, "bsim4_setup.cpp"), os.path.join(CSRC, "sparse.cpp")]
+           os.path.join(CSRC, "bsim4_setup.cpp"), os.path.join(CSRC, "dio_setup.cpp"),
+           os.path.join(CSRC, "sparse.cpp")]
     deps = [src] + cxx + [os.path.join(CSRC, f) for f in os.listdir(CSRC)
                           if f.endswith((".h", ".cuh", ".def"))]
     os.makedirs(OUT, exist_ok=True)
@@ -85,6 +86,15 @@ def lib():
                                    C.POINTER(C.c_double), C.c_double, C.c_int, C.c_double]
         L.port_add_mos1.argtypes = [vp, C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_double)]
         L.port_add_b4.argtypes = [vp, C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_double)]
+        L.port_add_dio.argtypes = [vp, C.POINTER(C.c_int), C.c_int, C.POINTER(C.c_double)]
+        L.port_dio_nparam.restype = C.c_int
+        L.port_dio_nstate.restype = C.c_int
+        L.port_dio_params.restype = C.c_int
+        L.port_dio_params.argtypes = [C.c_char_p, C.c_int, C.POINTER(C.c_char_p),
+                                      C.POINTER(C.c_double), C.c_char_p, C.c_int,
+                                      C.POINTER(C.c_char_p), C.POINTER(C.c_double), C.c_double,
+                                      C.c_double, C.c_double, C.POINTER(C.c_double),
+                                      C.POINTER(C.c_int), C.c_char_p, C.c_int]
         L.port_b4_nparam.restype = C.c_int
         L.port_b4_nstate.restype = C.c_int
         cp = C.POINTER(C.c_char_p)
@@ -267,6 +277,23 @@ class Circuit:
                 wf = self.source(t)
                 inst.append((kind, t[0], nodes, None, {}, wf))
                 key = ("default", kind)
+            elif k == "d":
+                nodes = [self.node(t[1]), self.node(t[2])]
+                mname = t[3]
+                p = {}
+                i = 4
+                while i < len(t):           # optional area value, then key=value
+                    if i + 1 < len(t) and t[i + 1] == "=":
+                        p[t[i]] = evaluate(t[i + 2])
+                        i += 3
+                    elif evaluate(t[i]) is not None and "area" not in p:
+                        p["area"] = evaluate(t[i])
+                        i += 1
+                    else:
+                        p[t[i]] = 1.0
+                        i += 1
+                inst.append((K_DIO, t[0], nodes, mname, p, None))
+                key = mname
             elif k == "m":
                 nodes = [self.node(x) for x in t[1:5]]
                 mname = t[5]
@@ -287,7 +314,7 @@ class Circuit:
         self.order = {kk: [] for kk in range(7)}
         groups = {}
         for idx, e in enumerate(inst):
-            key = ("default", e[0]) if e[0] not in (K_MOS1, K_BSIM4) else e[3]
+            key = ("default", e[0]) if e[0] not in (K_MOS1, K_BSIM4, K_DIO) else e[3]
             groups.setdefault(key, []).append(idx)
         for kk in range(7):
             keys = [key for key in groups if (inst[groups[key][0]][0] == kk)]
@@ -350,6 +377,13 @@ class Circuit:
                     sp = self.mk(name + "#source", True) if need_sp else s
                     self.dev[kk].append(([d, g, s, b, dp, sp], st, par))
                     st += lib().port_b4_nstate()
+                elif kind == K_DIO:
+                    mtype, mp = self.models[extra]
+                    par, need_pp = dio_params(extra, mp, name, p, self.opts)
+                    pos, neg = nodes
+                    pp = self.mk(name + "#internal", True) if need_pp else pos
+                    self.dev[kk].append(([pos, neg, pp], st, par))
+                    st += lib().port_dio_nstate()
                 elif kind == K_MOS1:
                     mtype, mp = self.models[extra]
                     par, need_dp, need_sp = mos1_params(mtype, mp, p, self.opts)
@@ -395,10 +429,15 @@ class Circuit:
             for kk, isv in ((K_ISRC, 0), (K_VSRC, 1)):
                 for nodes, wf in self.dev[kk]:
                     cf = (C.c_double * 64)(*wf["coef"])
-                    L.port_add_src(h, isv, nodes[0], nodes[1], nodes[2], wf["kind"],
+                    # ISRC binds its first netlist node as the negative node
+                    # (isrcdefs.h:30-31); VSRC binds it as the positive node
+                    p_, n_ = (nodes[1], nodes[0]) if kk == K_ISRC else (nodes[0], nodes[1])
+                    L.port_add_src(h, isv, p_, n_, nodes[2], wf["kind"],
                                    len(wf["coef"]), cf, wf["dc"], wf["dcgiven"], 1.0)
             for nodes, st, par in self.dev[K_MOS1]:
                 L.port_add_mos1(h, (C.c_int * 6)(*nodes), st, (C.c_double * len(par))(*par))
+            for nodes, st, par in self.dev[K_DIO]:
+                L.port_add_dio(h, (C.c_int * 3)(*nodes), st, (C.c_double * len(par))(*par))
             for nodes, st, par in self.dev[K_BSIM4]:
                 L.port_add_b4(h, (C.c_int * 6)(*nodes), st, (C.c_double * len(par))(*par))
             for nodes, r, p in self.dev[K_RES]:
@@ -605,6 +644,30 @@ def bsim4_params(mname: str, mtype: str, mp: dict, iname: str, ip: dict, opts: d
     if rc != 0:
         raise ValueError("oracle port: " + err.value.decode())
     return list(out), bool(ndp.value), bool(nsp.value)
+
+
+def dio_params(mname: str, mp: dict, iname: str, ip: dict, opts: dict):
+    """DIOsetup + DIOtemp for one diode through the shared arithmetic
+    (b4port.cpp); returns the parameter vector and whether the series
+    resistance needs an internal node."""
+    L = lib()
+    mk = list(mp)
+    ik = list(ip)
+    temp, tnom = _temps(opts)
+    reltol = evaluate(opts["reltol"]) if "reltol" in opts else 1e-3
+    out = (C.c_double * L.port_dio_nparam())()
+    npp = C.c_int()
+    err = C.create_string_buffer(512)
+    rc = L.port_dio_params(mname.encode(), len(mk),
+                           (C.c_char_p * max(1, len(mk)))(*[k.encode() for k in mk]),
+                           (C.c_double * max(1, len(mk)))(*[float(mp[k]) for k in mk]),
+                           iname.encode(), len(ik),
+                           (C.c_char_p * max(1, len(ik)))(*[k.encode() for k in ik]),
+                           (C.c_double * max(1, len(ik)))(*[float(ip[k]) for k in ik]),
+                           temp, tnom, reltol, out, C.byref(npp), err, 512)
+    if rc != 0:
+        raise ValueError("oracle port: " + err.value.decode())
+    return list(out), bool(npp.value)
 
 
 def simulate(text: str, **kw) -> dict:

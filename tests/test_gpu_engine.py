@@ -11,6 +11,7 @@ pytestmark = pytest.mark.gpu
 
 CASES = ["rc_ladder", "inverter_chain32"]
 BSIM4_CASES = ["bsim4_chain8", "bsim4_logic_s3"]
+DIODE_CASES = ["diode_rectifier", "mos1_mix"]
 
 
 @pytest.fixture(scope="module")
@@ -71,6 +72,23 @@ def test_newton_iterations_stamp_like_reference(E, name):
         assert rhs_violation(g["it_rhs"][kr][1:n + 1], cap["rhs"][km][1:n + 1]) <= 1.0
         checked += 1
     assert checked > 20
+
+
+@pytest.mark.parametrize("name", DIODE_CASES)
+def test_diode_decks_match_reference(E, name):
+    """Junction diodes and the mixed MOS1 deck (current source, series
+    resistances): the reference's Newton and step counts, time points equal
+    to rounding, waveforms within the option tolerances."""
+    g = golden(name)
+    c = run_one(E, str(g["netlist"]))
+    r = c.results()
+    ref = g["stats"]
+    assert r[E.R_STATUS] == 0
+    assert (r[E.R_ACCEPTED], r[E.R_REJECTED], r[E.R_TRANITER]) == (ref[3], ref[4], ref[1])
+    t, v = c.points()
+    assert len(t) == len(g["times"])
+    assert np.max(np.abs(t - g["times"])) <= 1e-9 * g["times"][-1]
+    assert waveform_violation(c.names(), g["times"], g["values"], t, v) < 1.0
 
 
 @pytest.mark.parametrize("name", BSIM4_CASES)

@@ -31,6 +31,25 @@ def test_port_matches_reference(name):
     assert waveform_violation(r["names"], g["times"], g["values"], r["times"], r["values"]) < 0.01
 
 
+@pytest.mark.parametrize("name", ["diode_rectifier", "mos1_mix"])
+def test_port_diode_decks_match_reference(name):
+    """Junction diodes (series resistance, depletion and transit-time
+    charge) and the mixed MOS1 deck with a current source: identical
+    Newton and step counts, time points equal to rounding, waveforms within
+    the option tolerances."""
+    g = golden(name)
+    r = port.simulate(str(g["netlist"]))
+    st, ref = r["stats"], g["stats"]
+    assert st["status"] == 0
+    assert (st["numIter"], st["tranIter"], st["accepted"], st["rejected"]) == \
+        (ref[0], ref[1], ref[3], ref[4])
+    assert np.max(np.abs(r["times"] - g["times"])) <= 1e-9 * g["times"][-1]
+    names = list(g["names"])
+    idx = [r["names"].index(x) for x in names]
+    assert waveform_violation(names, g["times"], g["values"], r["times"],
+                              r["values"][:, idx]) < 0.1
+
+
 def test_port_bsim4_logic_matches_reference():
     """Random BSIM4 logic (seed 3, ~120 transistors): identical Newton and
     step counts; the accepted time points agree to rounding (the dense LU
