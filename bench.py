@@ -1,15 +1,21 @@
 """Benchmark: accepted transient timesteps per second on one GB300.
 
-Engine arm (default): the GPU transient engine runs `.tran` on a batch of
-independent circuit instances in one launch; a step is one complete
-transient of the whole batch.  `value` is device-timed (inputs resident in
-HBM, CUDA events around the launches, L2 flushed between steps); `e2e` is
-the same metric through the public C ABI starting from host netlist text
-(compile, upload, run, read back the accepted points).
+Workloads: c1 (default) one 10,000-transistor BSIM4 random-logic netlist,
+the plain drop-in at scale, over the first 500 ps of its transient; c2
+1024 Monte Carlo instances of uneven size (100-3000 transistors, device
+mismatch) in one launch, first 200 ps; c0 the 32-stage MOS1 inverter chain,
+1216 instances, full 20 ns.
+
+Engine arm (default): the GPU transient engine runs `.tran` on the step's
+circuits in one launch; a step is one complete transient window of every
+circuit.  `value` is device-timed (inputs resident in HBM, CUDA events
+around the launches, L2 flushed between steps); `e2e` is the same metric
+through the public C ABI starting from host netlist text (compile, upload,
+run, read back the accepted points).
 
 Reference arm (--impl reference): the CPU oracle restatement of the
-reference transient path (oracle/port), on all host cores, one process per
-core, over a bounded sample of the same instances.
+reference transient path (oracle/port) on the host cores, on a bounded
+sample of the same workload (see cpu_measure).
 
 Prints one JSON line.
 """
@@ -33,27 +39,61 @@ UNIT = "timesteps/s"
 # Algorithmic bytes per Newton iteration (8 B per double, 4 B per index):
 # distinct fields each device load reads and writes, the matrix and LU
 # values the refactorization touches, the solve and convergence vectors.
+# BSIM4: 8 x (4 node V + 29 state0 read + 29 state0 write + 15 state1/2 +
+# 143 size-dependent parameters + 30 instance scalars + 22 slots + 4 rhs)
+# + 4 x 22 slot indices.  Diode: 8 x (3 node V + 22 state0 read/write x 2
+# + 4 state1/2 + 27 parameters + 9 slots + 2 rhs) + 4 x 9.
 BYTES_MOS1 = 920
 BYTES_RES = 72
 BYTES_CAP = 136
 BYTES_SRC = 120
 
 
-def workload_text(name: str, tstop: str | None = None) -> tuple[str, dict]:
+BYTES_BSIM4 = 2296
+BYTES_DIO = 748
+
+DEFAULT_INSTANCES = {"c0": 1216, "c1": 1, "c2": 1024}
+DEFAULT_WINDOW = {"c0": "20n", "c1": "500p", "c2": "200p"}
+
+
+def c2_sizes(instances: int) -> list[int]:
+    """Transistor counts of the Monte Carlo instances: U[100, 3000], seeded."""
+    import random
+    rng = random.Random(20240)
+    return [rng.randint(100, 3000) for _ in range(instances)]
+
+
+def workload_texts(name: str, tstop: str | None, instances: int) -> tuple[list[str], dict]:
+    """Netlists of one bench step and their description."""
     from ngspice_gb300 import netlists
+    tstop = tstop or DEFAULT_WINDOW[name]
     if name == "c0":
-        tstop = tstop or "20n"
-        return netlists.inverter_chain(tstop=tstop), {
+        return [netlists.inverter_chain(tstop=tstop)] * instances, {
             "circuit": "32-stage MOS1 CMOS inverter chain (level 1, VTO +-0.7 V, KP 110/50 uA/V^2,"
                        " LAMBDA 0.04, W/L 2u/1u and 4u/1u, VDD 3.3 V, 20 fF loads,"
                        " PULSE(0 3.3 0 100p 100p 2n 4n))",
             "tran": f".tran 10p {tstop}"}
+    if name == "c1":
+        return [netlists.random_logic(n_transistors=10000, seed=1, tstop=tstop)] * instances, {
+            "circuit": "seeded random CMOS logic, 10,000 BSIM4 (level 54) transistors, gate mix"
+                       " INV/NAND2/NOR2 40/35/25 %, RC pi nets, 64 PULSE inputs, VDD 1.0 V",
+            "tran": f".tran 1p {tstop} (the first {tstop} of the 5n transient)"}
+    if name == "c2":
+        sizes = c2_sizes(instances)
+        texts = [netlists.random_logic(n_transistors=n, seed=i, tstop=tstop, mismatch=True)
+                 for i, n in enumerate(sizes)]
+        return texts, {
+            "circuit": f"{instances} Monte Carlo instances of seeded random BSIM4 logic,"
+                       f" {min(sizes)}-{max(sizes)} transistors ({sum(sizes)} total), per-device"
+                       " mismatch vth0 N(nom, 15 mV), toxe N(nom, 2 %), W N(nom, 3 %)",
+            "tran": f".tran 1p {tstop} (the first {tstop} of the 2n transient)"}
     raise SystemExit(f"unknown workload {name}")
 
 
 def bytes_per_iteration(w: dict) -> int:
     n, nnz, nlu = w["n"], w["nnz"], w["nlu"]
-    return (BYTES_MOS1 * w["mos1"] + BYTES_RES * w["res"] + BYTES_CAP * w["cap"]
+    return (BYTES_BSIM4 * w["bsim4"] + BYTES_MOS1 * w["mos1"] + BYTES_DIO * w["dio"]
+            + BYTES_RES * w["res"] + BYTES_CAP * w["cap"]
             + BYTES_SRC * (w["vsrc"] + w["isrc"])
             + 8 * nnz + 12 * nlu          # refactorization
             + 12 * nlu + 24 * n           # forward/backward substitution
@@ -124,43 +164,77 @@ def peaks() -> dict:
 # ---------------------------------------------------------------------------
 # CPU oracle (reference arm and cpu_baseline)
 # ---------------------------------------------------------------------------
-def _cpu_one(text: str) -> int:
+def _cpu_one(text: str) -> tuple[int, float]:
     sys.path.insert(0, os.path.join(ROOT, "oracle", "port"))
     import port
+    t0 = time.perf_counter()
     r = port.simulate(text)
-    return int(r["stats"]["accepted"])
+    return int(r["stats"]["accepted"]), time.perf_counter() - t0
 
 
-def cpu_sample(text: str, instances: int, procs: int) -> tuple[float, int]:
+def cpu_pool(texts: list[str], procs: int) -> tuple[int, float]:
+    """Run the oracle port on every netlist, `procs` processes (spawned);
+    returns (accepted steps, makespan seconds)."""
     ctx = mp.get_context("spawn")
     t0 = time.perf_counter()
     with ctx.Pool(procs) as pool:
-        acc = sum(pool.map(_cpu_one, [text] * instances, chunksize=1))
-    return acc, time.perf_counter() - t0
+        res = pool.map(_cpu_one, texts, chunksize=1)
+    return sum(a for a, _ in res), time.perf_counter() - t0
 
 
-def cpu_arm(args, text, wdesc) -> dict:
+def cpu_measure(args) -> dict:
+    """One bounded CPU sample of the workload on the host cores.
+
+    c0/c2: independent instances, one port process per core over a sample
+    of the instances (throughput = accepted steps / makespan).  c1: one
+    circuit; the port is single-threaded, so one core; the rate is the
+    marginal one between a 20p and a 50p window of the same netlist
+    (accepted steps and seconds of the difference), which leaves out the
+    operating point and favours the CPU."""
     sys.path.insert(0, os.path.join(ROOT, "oracle", "port"))
     import port
     port.build()
     procs = os.cpu_count() or 1
-    sample = args.cpu_sample or 8 * procs
-    for _ in range(max(0, min(args.warmup, 1))):
-        cpu_sample(text, procs, procs)
-    times, accs = [], []
+    if args.workload == "c1":
+        from ngspice_gb300 import netlists
+        short = netlists.random_logic(n_transistors=10000, seed=1, tstop="20p")
+        long_ = netlists.random_logic(n_transistors=10000, seed=1, tstop="50p")
+        a1, t1 = _cpu_one(short)
+        a2, t2 = _cpu_one(long_)
+        return {"value": (a2 - a1) / max(t2 - t1, 1e-9), "cores": 1, "seconds": t1 + t2,
+                "sample": f"C1 netlist on 1 core (single-threaded port): accepted steps between the"
+                          f" 20p and 50p windows ({a2 - a1} steps in {t2 - t1:.1f} s; operating"
+                          f" point excluded)"}
+    texts, _ = workload_texts(args.workload, args.tstop, args.instances)
+    if args.workload == "c0":
+        sample = args.cpu_sample or 4 * procs
+        batch = [texts[0]] * sample
+    else:
+        sample = args.cpu_sample or 2 * procs
+        step = max(1, len(texts) // sample)
+        batch = texts[::step][:sample]
+    a, dt = cpu_pool(batch, procs)
+    return {"value": a / dt, "cores": procs, "seconds": dt,
+            "sample": f"{len(batch)} of the step's instances across {procs} processes"
+                      f" ({a} accepted steps in {dt:.1f} s)"}
+
+
+def cpu_arm(args, wdesc) -> dict:
+    times, vals, desc = [], [], ""
     for _ in range(args.steps):
-        a, dt = cpu_sample(text, sample, procs)
-        times.append(dt)
-        accs.append(a)
-    value = sum(accs) / sum(times)
-    desc = f"{sample} instances per step across {procs} processes (oracle restatement, oracle/port)"
+        m = cpu_measure(args)
+        vals.append(m["value"])
+        times.append(m["seconds"])
+        desc = m["sample"]
+        cores = m["cores"]
+    value = statistics.mean(vals)
     return {"metric": METRIC, "value": value, "unit": UNIT, "impl": "reference",
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * statistics.mean(times), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": wdesc,
-            "cpu_baseline": {"value": value, "unit": UNIT, "cores": procs, "kind": "port",
-                             "sample": desc},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": desc + " (oracle restatement, oracle/port)"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
 
@@ -168,28 +242,30 @@ def cpu_arm(args, text, wdesc) -> dict:
 # ---------------------------------------------------------------------------
 # engine arm
 # ---------------------------------------------------------------------------
-def engine_arm(args, text, wdesc, rank, world) -> dict | None:
+def engine_arm(args, texts, wdesc, rank, world) -> dict | None:
     from ngspice_gb300 import engine as E
-    B = args.instances
     probes = ["n32"] if args.workload == "c0" else None
-    circuits = [E.Circuit(text, probes=probes, outcap=8192) for _ in range(B)]
-    w = circuits[0].workload()
+    circuits = [E.Circuit(t, probes=probes, outcap=8192) for t in texts]
+    wls = [c.workload() for c in circuits]
     for _ in range(args.warmup):
         E.run(circuits)
     clocks = Clocks()
-    dev_times, accepted, iters, launches = [], 0, 0, 0
+    dev_times, accepted, launches, moved = [], 0, 0, 0
+    iters_of = [0] * len(circuits)
     for _ in range(args.steps):
         flush_l2()
         sec = E.run(circuits)
         dev_times.append(sec)
         launches += E.last_launches()
-        for c in circuits:
+        for i, c in enumerate(circuits):
             r = c.results()
             if r[E.R_STATUS] != 0:
-                raise SystemExit(f"engine status {r[E.R_STATUS]}")
+                raise SystemExit(f"engine status {r[E.R_STATUS]} on instance {i}")
             accepted += int(r[E.R_ACCEPTED])
-            iters += int(r[E.R_NUMITER])
+            iters_of[i] += int(r[E.R_NUMITER])
     clk = clocks.stop()
+    iters = sum(iters_of)
+    moved = sum(bytes_per_iteration(w) * k for w, k in zip(wls, iters_of))
     total = sum(dev_times)
     if world > 1:
         import torch
@@ -204,12 +280,12 @@ def engine_arm(args, text, wdesc, rank, world) -> dict | None:
     value = accepted_all / total
 
     # e2e: host netlist text -> compile/upload -> run -> accepted points on host
-    e2e_steps = max(1, min(args.steps, 2))
+    e2e_steps = 1
     t0 = time.perf_counter()
     h2d = d2h = 0
     e2e_acc = 0
     for _ in range(e2e_steps):
-        cs = [E.Circuit(text, probes=probes, outcap=8192) for _ in range(B)]
+        cs = [E.Circuit(t, probes=probes, outcap=8192) for t in texts]
         E.run(cs)
         for c in cs:
             tt, vv = c.points()
@@ -219,30 +295,29 @@ def engine_arm(args, text, wdesc, rank, world) -> dict | None:
         del cs
     e2e_time = time.perf_counter() - t0
     e2e = {"value": world * e2e_acc / e2e_time, "unit": UNIT,
-           "h2d_bytes_per_step": h2d // e2e_steps, "d2h_bytes_per_step": d2h // e2e_steps}
+           "h2d_bytes_per_step": h2d // e2e_steps, "d2h_bytes_per_step": d2h // e2e_steps,
+           "includes": "netlist compile, symbolic analysis, upload, run, read-back"}
 
     pk = peaks()
-    bpi = bytes_per_iteration(w)
-    achieved = bpi * iters / total / 1e9
+    achieved = moved / total / 1e9
+    kernel = "tran_wide_kernel" if (len(texts) <= 4 and wls[0]["bsim4"] + wls[0]["mos1"] >= 1024) \
+        else "tran_kernel"
     roof = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
             "frac": achieved / pk["hbm_gbs"], "traffic": None,
-            "peak_source": pk["src"], "kernel": "tran_kernel",
-            "algorithmic_bytes_per_newton_iteration": bpi}
+            "peak_source": pk["src"], "kernel": kernel,
+            "algorithmic_bytes_per_newton_iteration": moved // max(iters, 1)}
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup,
-           "ms_per_step": 1e3 * max(dev_times) if args.steps == 1 else 1e3 * total / args.steps,
+           "ms_per_step": 1e3 * total / args.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic", "config": wdesc, "clocks": clk, "e2e": e2e,
            "gpu_launches": launches, "roofline": roof,
            "newton_iterations_per_s": iters * world / total,
            "newton_iterations_per_accepted_step": iters / max(accepted, 1)}
     if rank == 0 and not args.no_cpu_baseline:
-        procs = os.cpu_count() or 1
-        sample = args.cpu_sample or 4 * procs
-        a, dt = cpu_sample(text, sample, procs)
-        out["cpu_baseline"] = {"value": a / dt, "unit": UNIT, "cores": procs, "kind": "port",
-                               "sample": f"{sample} instances of the same circuit across {procs}"
-                                         f" processes ({dt:.1f} s of CPU work)"}
+        m = cpu_measure(args)
+        out["cpu_baseline"] = {"value": m["value"], "unit": UNIT, "cores": m["cores"],
+                               "kind": "port", "sample": m["sample"]}
     return out
 
 
@@ -252,8 +327,9 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--workload", default="c0")
-    ap.add_argument("--instances", type=int, default=1216)
+    ap.add_argument("--workload", default="c1", choices=["c0", "c1", "c2"])
+    ap.add_argument("--instances", type=int, default=0,
+                    help="instances per launch (default: 1216 for c0, 1 for c1, 1024 for c2)")
     ap.add_argument("--cpu-sample", type=int, default=0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--tstop", default=None,
@@ -261,15 +337,16 @@ def main():
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
-    text, tdesc = workload_text(args.workload, args.tstop)
+    args.instances = args.instances or DEFAULT_INSTANCES[args.workload]
+    texts, tdesc = workload_texts(args.workload, args.tstop, args.instances)
     wdesc = {"workload": f"{args.workload.upper()}: {tdesc['circuit']}, {tdesc['tran']},"
-                         f" {args.instances} independent instances per launch",
+                         f" {args.instances} independent instance(s) per launch",
              "instances_per_gpu": args.instances, "l2": "flushed between timed steps",
              "parallelism": f"replicas x{world}"}
     if args.impl == "reference":
         if rank != 0:
             return
-        print(json.dumps(cpu_arm(args, text, wdesc)))
+        print(json.dumps(cpu_arm(args, wdesc)))
         return
     if world > 1:
         import torch
@@ -277,7 +354,7 @@ def main():
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("nccl")
         dist.barrier()
-    out = engine_arm(args, text, wdesc, rank, world)
+    out = engine_arm(args, texts, wdesc, rank, world)
     if world > 1:
         import torch.distributed as dist
         dist.barrier()

@@ -60,8 +60,10 @@ NGSF_API int ngsf_probes(const ngsf_handle *h, int *eqs, int max);
 NGSF_API int ngsf_run(ngsf_handle *const *hs, int count, long long max_steps,
                       double *seconds);
 
-/* results: ires[11] (status, npoints, accepted, rejected, numIter,
- * tranIter, timePts, ncap, opIter, badPivot, reorders), fres[3] (time
+/* results: ires[14] (status, npoints, accepted, rejected, numIter,
+ * tranIter, timePts, ncap, opIter, badPivot, reorders, and with a Newton
+ * predictor: steps started from its guess, of those accepted after the
+ * first iteration, and retried from the plain start), fres[3] (time
  * reached, last step, diagonal gmin in force) */
 NGSF_API int ngsf_results(const ngsf_handle *h, int *ires, double *fres);
 /* accepted points: buf[np][1 + nprobe] = time, probe values; returns np */
@@ -113,6 +115,61 @@ NGSF_API long long ngsf_device_bytes(const ngsf_handle *h);
  *   race on it and must be serialised by the caller.
  * Returns 0, or -1 with ngsf_last_error() set. */
 NGSF_API int ngsf_stamp_initial_static(const ngsf_handle *h, double *ax, double *rhs);
+
+/* ---------------------------------------------------------------------- *
+ * Learned Newton predictor: the network kernels (no reference counterpart;
+ * the reference's Newton starts from the previous solution and the devices'
+ * INITPRED extrapolation, src/maths/ni/niiter.c:29-367).
+ *
+ * A shared-weight message-passing network over a circuit's node graph (3
+ * layers, width 64, BF16 tensor-core products with FP32 accumulation)
+ * predicting per node a correction to the linear extrapolation of the node
+ * voltage to the next timepoint.  Parameters are an FP32 master copy in a
+ * flat layout of ngsf_gnn_param_count() floats: Win[16][64], bin[64],
+ * three times (W[128][64], b[64]), Wout[64][16], bout[1].
+ * ---------------------------------------------------------------------- */
+typedef struct ngsf_gnn ngsf_gnn;
+
+NGSF_API int ngsf_gnn_param_count(void);
+/* A network state for one graph of nnodes nodes; neighbour lists in CSR
+ * (nbr_ptr[nnodes+1], nbr_idx), symmetric.  NULL on error. */
+NGSF_API ngsf_gnn *ngsf_gnn_create(int nnodes, const int *nbr_ptr, const int *nbr_idx);
+NGSF_API void ngsf_gnn_destroy(ngsf_gnn *g);
+/* set the FP32 master parameters (resets the optimiser); read them back */
+NGSF_API int ngsf_gnn_set_params(ngsf_gnn *g, const float *flat);
+NGSF_API int ngsf_gnn_get_params(const ngsf_gnn *g, float *flat);
+/* X: host [nnodes][16] features; pred: host [nnodes] */
+NGSF_API int ngsf_gnn_forward(ngsf_gnn *g, const float *X, float *pred);
+/* Forward, loss sum_i w_i (pred_i - y_i)^2 / (2 sum_i w_i), backward and,
+ * when lr > 0, one Adam step.  loss and grads (flat layout) are optional
+ * host outputs. */
+NGSF_API int ngsf_gnn_train_step(ngsf_gnn *g, const float *X, const float *y, const float *w,
+                                 float lr, float *loss, float *grads);
+/* The tensor-core product on its own: C[M][N] = bf16(A)[M][K] bf16(B)[N][K]^T
+ * with FP32 accumulation (host arrays); M % 128 == 0, N % 16 == 0 and
+ * N <= 128, K % 16 == 0; the K range split over `splits` blocks. */
+NGSF_API int ngsf_gnn_gemm_test(const float *A, const float *B, float *C, int M, int N, int K,
+                                int splits);
+
+/* The predictor's view of a circuit: the voltage unknowns (equation
+ * indices 1..n, *nv of them), their neighbour lists from the matrix
+ * pattern (CSR gptr[nv+1], gidx[*nedges], symmetric), and per node
+ * log(1 + count) of incident MOSFET gate, drain/source, bulk, capacitor,
+ * resistor and source terminals (stat[nv][6]).  Array arguments may be
+ * NULL (sizes first). */
+NGSF_API int ngsf_node_graph(const ngsf_handle *h, int *nv, int *nedges, int *vnode, int *gptr,
+                             int *gidx, float *stat);
+/* Newton predictor for the circuit's next runs: kind 0 off (the
+ * reference's start), 1 linear extrapolation of the last two accepted
+ * points, 2 that plus the network's correction of the node voltages
+ * (params: flat layout above).  With a predictor, Newton at each new
+ * timestep starts from its guess, may be accepted after the first
+ * iteration when NIconvTest passes, and a start that misses itl4 is
+ * retried from the plain start.  Features per node at step n: v_n,
+ * (v_n - v_{n-1})/0.05, (v_{n-1} - v_{n-2})/0.05, r1 = h_{n+1}/h_n and
+ * r2 = h_n/h_{n-1} (each at most 4), r1 (v_n - v_{n-1})/0.05, stat[6], 1,
+ * 0, 0, 0; the guess is v_n + r1 (v_n - v_{n-1}) + 0.05 pred. */
+NGSF_API int ngsf_set_predictor(ngsf_handle *h, int kind, const float *params);
 
 #ifdef __cplusplus
 }

@@ -236,6 +236,41 @@ NGSF_API long long ngsf_device_bytes(const ngsf_handle *h)
     return (h && h->p.dev) ? (long long)h->p.dev->bytes() : 0;
 }
 
+NGSF_API int ngsf_node_graph(const ngsf_handle *h, int *nv, int *nedges, int *vnode, int *gptr,
+                             int *gidx, float *stat)
+{
+    if (!h)
+        return fail("null handle");
+    ngsf::PredGraph g = ngsf::pred_graph(h->p.img);
+    if (nv)
+        *nv = (int)g.vnode.size();
+    if (nedges)
+        *nedges = (int)g.gidx.size();
+    if (vnode)
+        memcpy(vnode, g.vnode.data(), g.vnode.size() * sizeof(int));
+    if (gptr)
+        memcpy(gptr, g.gptr.data(), g.gptr.size() * sizeof(int));
+    if (gidx)
+        memcpy(gidx, g.gidx.data(), g.gidx.size() * sizeof(int));
+    if (stat)
+        memcpy(stat, g.stat.data(), g.stat.size() * sizeof(float));
+    return 0;
+}
+
+NGSF_API int ngsf_set_predictor(ngsf_handle *h, int kind, const float *params)
+{
+    if (!h || !h->p.dev)
+        return fail("ngsf_set_predictor: null or host-only handle");
+    if (kind < 0 || kind > 2 || (kind == 2 && !params))
+        return fail("ngsf_set_predictor: kind 0, 1, or 2 with parameters");
+    try {
+        h->p.dev->set_pred(h->p.img, kind, params);
+    } catch (const std::exception &e) {
+        return fail(e.what());
+    }
+    return 0;
+}
+
 }  // extern "C"
 
 /* ====================================================================== */

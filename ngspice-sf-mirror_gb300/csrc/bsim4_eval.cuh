@@ -83,7 +83,10 @@ NGSF_HD inline int bsim4_eval(const B4Ctx &x, const double *P, size_t ps, double
             B4PRED(B4S_VDES, vdes)
             st0[B4S_QDEF] = st1[B4S_QDEF];
 #undef B4PRED
-        } else {
+        }
+        if (!(mode & NGSF_MODEINITPRED) || (mode & NGSF_MODEGUESS)) {
+            /* INITFLOAT, or a predictor guess in rhsOld (after the
+             * INITPRED state copies above) */
             const double *ro = x.rhsOld;
             vds = type * (ro[dpN] - ro[spN]);
             vgs = type * (ro[gN] - ro[spN]);

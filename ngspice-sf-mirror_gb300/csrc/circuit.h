@@ -150,7 +150,7 @@ struct Image {
     std::vector<int> fh_ptr, fh_row, bh_ptr, bh_row;   /* solve rows reduced by a warp */
     /* right-looking level schedule (large matrices) */
     std::vector<int> rl_ptr, rl_col, sc_ptr, sc_pos, sc_piv;
-    std::vector<int> ud_ptr, ud_dst, ud_cptr, ud_l, ud_u;
+    std::vector<int> ud_ptr, ud_dst, ud_cptr, ud_l, ud_u, ud_p;
     double lu_flops = 0;   /* multiply-adds of one refactorization */
     std::vector<std::string> names;  /* equation names 1..n */
 };

@@ -56,6 +56,8 @@ NGSF_HD inline int dio_eval(const DevCtx &x, const double *P, size_t ps, const i
             st0[DIS_RESCONDUCT] = st1[DIS_RESCONDUCT];
             st0[DIS_CQCSR] = st1[DIS_CQCSR];
             st0[DIS_GQCSR] = st1[DIS_GQCSR];
+            if (mode & NGSF_MODEGUESS)   /* predictor guess in rhsOld */
+                vd = x.rhsOld[node[DIN_POSP]] - x.rhsOld[node[DIN_NEG]];
         } else {
             vd = x.rhsOld[node[DIN_POSP]] - x.rhsOld[node[DIN_NEG]];
             st0[DIS_QTH] = 0.0;   /* cth0 * delTemp, no self-heating */

@@ -22,7 +22,9 @@
  * (NGSF_E_WATCHDOG), so a kernel always returns with a status word.
  */
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <cuda/atomic>
+#include <cuda_bf16.h>
 #include <mutex>
 #include <string>
 #include <math.h>
@@ -36,6 +38,8 @@
 #define NGSF_WARPS (NGSF_THREADS / 32)
 /* a matrix cell or rhs entry with more contributions is summed by a warp */
 #define NGSF_HEAVY 64
+/* largest dynamic shared memory a launch asks for (solve buffers) */
+#define NGSF_SOLVE_SMEM_MAX (160 * 1024)
 
 namespace {
 
@@ -55,6 +59,11 @@ struct Ctl {
      * host re-pivot, and the loop locals it needs to continue */
     int phase, shouldReorder, savedIter, savedNoncon, iters0, reorders;
     long long steps;
+    /* Newton predictor: accepted times of cur/h0/h1, accepted points in
+     * the history, plain start forced for the retry of this step, the
+     * current step started from a guess; counters */
+    double tcur, th0, th1;
+    int histCount, guessOff, guessUsed, guessSteps, guessFirst, guessFalls;
     double delta0;
     /* CKTop fallbacks: gmin stepping and source stepping (cktop.c) */
     int opPhase, gi, itersBefore;
@@ -191,6 +200,8 @@ __device__ Iter iter_ctx(const ngsf_ckt_t &C, const Ctl &s)
     return it;
 }
 
+#include "predict.cuh"
+
 /* ---------------------------------------------------------------- */
 /* independent source value at the current time (VSRCload/ISRCload)   */
 /* ---------------------------------------------------------------- */
@@ -281,26 +292,26 @@ __device__ double src_value(const ngsf_src_t &S, int i, const Ctl &s, const ngsf
 /* device loads                                                      */
 /* ---------------------------------------------------------------- */
 /* CAPload (src/spicelib/devices/cap/capload.c:15-87) */
-__device__ void cap_load(const ngsf_ckt_t &C, const Ctl &s, const Iter &it)
+__device__ void cap_load(const ngsf_ckt_t &C, const Ctl &s, const Iter &it, int t0, int T)
 {
     const ngsf_cap_t &K = C.cap;
     int n = K.n, mode = s.mode;
     if (!(mode & (NGSF_MODETRAN | NGSF_MODETRANOP))) {
-        for (int i = threadIdx.x; i < n; i += blockDim.x)
+        for (int i = t0; i < n; i += T)
             for (int k = 0; k < 6; k++)
                 C.stampv[K.stamp0 + k * n + i] = 0.0;
         return;
     }
     bool cond1 = ((mode & NGSF_MODEDC) && (mode & NGSF_MODEINITJCT)) ||
                  ((mode & NGSF_MODEUIC) && (mode & NGSF_MODEINITTRAN));
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    for (int i = t0; i < n; i += T) {
         int p = K.node[i], q = K.node[n + i], st = K.st[i];
         double m = K.m[i], cap = K.c[i];
         double vcap = cond1 ? K.ic[i] : it.rhsOld[p] - it.rhsOld[q];
         double g = 0.0, ceqv = 0.0;
         double *sv = C.stampv + K.stamp0 + i;
         if (mode & NGSF_MODETRAN) {
-            if (mode & NGSF_MODEINITPRED) {
+            if ((mode & NGSF_MODEINITPRED) && !(mode & NGSF_MODEGUESS)) {
                 it.st0[st] = it.st1[st];
             } else {
                 it.st0[st] = cap * vcap;
@@ -328,11 +339,11 @@ __device__ void cap_load(const ngsf_ckt_t &C, const Ctl &s, const Iter &it)
 }
 
 /* RESload (src/spicelib/devices/res/resload.c:15-40) */
-__device__ void res_load(const ngsf_ckt_t &C)
+__device__ void res_load(const ngsf_ckt_t &C, int t0, int T)
 {
     const ngsf_res_t &K = C.res;
     int n = K.n;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    for (int i = t0; i < n; i += T) {
         double g = K.g[i];
         double *sv = C.stampv + K.stamp0 + i;
         sv[0] = g;
@@ -418,6 +429,12 @@ __device__ int mos1_load_one(const ngsf_ckt_t &C, const Ctl &s, const Iter &it, 
             st0[M1S_VDS] = st1[M1S_VDS];
             vds = (1 + xfact) * (st1[M1S_VDS]) - (xfact * (st2[M1S_VDS]));
             st0[M1S_VBD] = st0[M1S_VBS] - st0[M1S_VDS];
+            if (mode & NGSF_MODEGUESS) {
+                /* predictor guess: state copies as above, voltages from rhsOld */
+                vbs = type * (it.rhsOld[bN] - it.rhsOld[spN]);
+                vgs = type * (it.rhsOld[gN] - it.rhsOld[spN]);
+                vds = type * (it.rhsOld[dpN] - it.rhsOld[spN]);
+            }
         } else {
             vbs = type * (it.rhsOld[bN] - it.rhsOld[spN]);
             vgs = type * (it.rhsOld[gN] - it.rhsOld[spN]);
@@ -820,22 +837,45 @@ __device__ int bsim4_load_one(const ngsf_ckt_t &C, const Ctl &s, const Iter &it,
 /* ---------------------------------------------------------------- */
 /* wide launch: hand-over between block 0 and the worker blocks        */
 /* ---------------------------------------------------------------- */
-#define NGSF_WIDE_SPIN_LIMIT (1LL << 26)   /* x ~100 ns sleeps: a few seconds */
+#define NGSF_WIDE_SPIN_LIMIT (1LL << 26)   /* polls: a few seconds */
 
-/* the transistor share of block b out of nb: contiguous chunks */
-__device__ int wide_transistors(const ngsf_ckt_t &C, const Ctl &s, const Iter &it, int b, int nb)
+/* grid barriers this block has passed in the current launch */
+__shared__ unsigned long long g_barGen;
+
+/* Barrier over the nb blocks of a wide launch (every block calls the same
+ * sequence of barriers); with nb == 1 a block barrier.  Arrivals count up
+ * in one 64-bit word; the block that completes generation g publishes g in
+ * a second word, which the others poll (so the polls do not contend with
+ * the arrivals).  The wait is bounded and gives up at once after any
+ * block's wait ran out (err). */
+__device__ void grid_sync(const ngsf_ckt_t &C, int nb)
 {
-    int nc = 0;
-    int chunk = (C.bsim4.n + nb - 1) / nb;
-    int lo = b * chunk, hi = min(C.bsim4.n, lo + chunk);
-    for (int i = lo + threadIdx.x; i < hi; i += blockDim.x)
-        nc |= bsim4_load_one(C, s, it, i);
-    chunk = (C.mos1.n + nb - 1) / nb;
-    lo = b * chunk;
-    hi = min(C.mos1.n, lo + chunk);
-    for (int i = lo + threadIdx.x; i < hi; i += blockDim.x)
-        nc |= mos1_load_one(C, s, it, i);
-    return nc;
+    __syncthreads();
+    if (nb <= 1)
+        return;
+    if (threadIdx.x == 0) {
+        ngsf_wide_t *w = C.wide;
+        const unsigned long long g = g_barGen + 1;
+        cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> bar(w->bar);
+        cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> gen(w->gen);
+        cuda::atomic_ref<int, cuda::thread_scope_device> err(w->err);
+        __threadfence();
+        const unsigned long long old = bar.fetch_add(1ull, cuda::memory_order_acq_rel);
+        if (old + 1 == g * (unsigned long long)nb) {
+            gen.store(g, cuda::memory_order_release);
+        } else {
+            long long spins = 0;
+            while (gen.load(cuda::memory_order_acquire) < g) {
+                if (++spins > NGSF_WIDE_SPIN_LIMIT || err.load(cuda::memory_order_relaxed)) {
+                    err.store(1);
+                    break;
+                }
+            }
+        }
+        __threadfence();
+        g_barGen = g;
+    }
+    __syncthreads();
 }
 
 /* block 0: publish the control words and a command (thread 0 only) */
@@ -844,6 +884,7 @@ __device__ void wide_issue(const ngsf_ckt_t &C, const Ctl &s, int cmd)
     ngsf_wide_t *w = C.wide;
     w->done = 0;
     w->noncon = 0;
+    w->bad = 0;
     const unsigned long long *src = (const unsigned long long *)&s;
     for (int k = 0; k < (int)((sizeof(Ctl) + 7) / 8); k++)
         w->ctl[k] = src[k];
@@ -852,23 +893,100 @@ __device__ void wide_issue(const ngsf_ckt_t &C, const Ctl &s, int cmd)
     seq.fetch_add(1, cuda::memory_order_release);
 }
 
-/* block 0: wait until the other nb-1 blocks finished (thread 0 only);
- * returns their convergence flag, or 1 with err set when the wait ran out */
-__device__ int wide_collect(const ngsf_ckt_t &C, int nb)
+/* Sum of the contributions to every matrix cell and rhs row.  Cells with
+ * up to NGSF_HEAVY contributions are summed by one thread in the
+ * reference's load order (bit-identical to CKTload).  The few that collect
+ * thousands (a supply node's diagonal) are cut into chunks of NGSF_HCHUNK
+ * contributions: one warp per chunk, lane-strided partial sums in load
+ * order and a fixed butterfly, then the chunk sums in chunk order
+ * (gather_heavy_combine).  The rounding then differs from the sequential
+ * sum by far less than the 1e-12 stamp tolerance, and is the same for any
+ * number of blocks.  Thread t of T, warp gw of GW. */
+__device__ void gather(const ngsf_ckt_t &C, const Iter &it, int t, int T, int gw, int GW)
 {
-    ngsf_wide_t *w = C.wide;
-    cuda::atomic_ref<int, cuda::thread_scope_device> done(w->done);
-    cuda::atomic_ref<int, cuda::thread_scope_device> err(w->err);
-    long long spins = 0;
-    while (done.load(cuda::memory_order_acquire) < nb - 1) {
-        if (++spins > NGSF_WIDE_SPIN_LIMIT || err.load(cuda::memory_order_relaxed)) {
-            err.store(1);
-            return 1;
-        }
-        __nanosleep(64);
+    for (int p = t; p < C.nnz; p += T) {
+        const int q0 = C.gptr[p], q1 = C.gptr[p + 1];
+        if (q1 - q0 > NGSF_HEAVY)
+            continue;
+        double acc = 0.0;
+        for (int q = q0; q < q1; q++)
+            acc += C.stampv[C.gsrc[q]];
+        C.ax[p] = acc;
     }
-    return w->noncon;
+    for (int r = t; r <= C.n; r += T) {
+        const int q0 = C.rptr[r], q1 = C.rptr[r + 1];
+        if (q1 - q0 > NGSF_HEAVY)
+            continue;
+        double acc = 0.0;
+        for (int q = q0; q < q1; q++)
+            acc += C.stampv[C.rsrc[q]];
+        it.rhs[r] = acc;
+    }
+    const int lane = threadIdx.x & 31;
+    for (int c = gw; c < C.nhchunk; c += GW) {
+        const int h = C.hch_cell[c];
+        const int p = C.heavy[h];
+        const bool isrhs = p < 0;
+        const int e = isrhs ? -p - 1 : p;
+        const int *ptr = isrhs ? C.rptr : C.gptr;
+        const int *src = isrhs ? C.rsrc : C.gsrc;
+        const int q0 = ptr[e] + (c - C.hch_ptr[h]) * NGSF_HCHUNK;
+        const int q1 = min(ptr[e + 1], q0 + NGSF_HCHUNK);
+        double acc = 0.0;
+        for (int q = q0 + lane; q < q1; q += 32)
+            acc += C.stampv[src[q]];
+        for (int o = 16; o > 0; o >>= 1)
+            acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0)
+            C.hpart[c] = acc;
+    }
 }
+
+/* one block, after every chunk sum is visible */
+__device__ void gather_heavy_combine(const ngsf_ckt_t &C, const Iter &it)
+{
+    for (int h = threadIdx.x; h < C.nheavy; h += blockDim.x) {
+        double acc = 0.0;
+        for (int c = C.hch_ptr[h]; c < C.hch_ptr[h + 1]; c++)
+            acc += C.hpart[c];
+        const int p = C.heavy[h];
+        if (p < 0)
+            it.rhs[-p - 1] = acc;
+        else
+            C.ax[p] = acc;
+    }
+}
+
+/* The device loads and the gather of one CKTload, shared by nb blocks
+ * (this is block b): every instance to one thread of the grid, then the
+ * cell sums.  Block 0 (master) also loads the sources.  Ends after a grid
+ * barrier; the heavy chunk sums still need gather_heavy_combine.  Returns
+ * this block's convergence flag; the others' are ORed into wide->noncon. */
+__device__ int load_phase(const ngsf_ckt_t &C, Ctl &s, const Iter &it, int b, int nb, bool master)
+{
+    const int t = b * blockDim.x + threadIdx.x, T = nb * blockDim.x;
+    int nc = 0;
+    for (int i = t; i < C.bsim4.n; i += T)
+        nc |= bsim4_load_one(C, s, it, i);
+    cap_load(C, s, it, t, T);
+    for (int i = t; i < C.dio.n; i += T)
+        nc |= dio_load_one(C, s, it, i);
+    for (int i = t; i < C.mos1.n; i += T)
+        nc |= mos1_load_one(C, s, it, i);
+    res_load(C, t, T);
+    if (master)
+        src_load(C, s);
+    nc = block_or(s, nc);   /* includes __syncthreads: stamps visible */
+    if (nb > 1 && threadIdx.x == 0 && nc && !master)
+        atomicOr(&C.wide->noncon, 1);
+    grid_sync(C, nb);
+    const int warp = threadIdx.x >> 5;
+    gather(C, it, t, T, b * NGSF_WARPS + warp, nb * NGSF_WARPS);
+    grid_sync(C, nb);
+    return nc;
+}
+
+__device__ int lu_factor_rl(const ngsf_ckt_t &C, Ctl &s, int b, int nb);
 
 /* worker blocks: serve block 0's commands until EXIT (or a timeout) */
 __device__ void wide_worker(const ngsf_ckt_t &C, Ctl &s)
@@ -900,100 +1018,36 @@ __device__ void wide_worker(const ngsf_ckt_t &C, Ctl &s)
         __syncthreads();
         if (cmd == NGSF_WIDE_EXIT)
             return;
-        Iter it = iter_ctx(C, s);
-        int nc = wide_transistors(C, s, it, blockIdx.x, gridDim.x);
-        nc = block_or(s, nc);
-        if (threadIdx.x == 0) {
-            if (nc)
-                atomicOr(&w->noncon, 1);
-            cuda::atomic_ref<int, cuda::thread_scope_device> done(w->done);
-            done.fetch_add(1, cuda::memory_order_release);
+        if (cmd == NGSF_WIDE_LOAD) {
+            Iter it = iter_ctx(C, s);
+            load_phase(C, s, it, blockIdx.x, gridDim.x, false);
+        } else if (cmd == NGSF_WIDE_FACTOR) {
+            lu_factor_rl(C, s, blockIdx.x, gridDim.x);
         }
         __syncthreads();
     }
 }
 
-/* CKTload: zero, device loads, gather into matrix and rhs. */
+/* CKTload: zero, device loads, gather into matrix and rhs; in a wide
+ * launch the worker blocks take their share of both. */
 __device__ int ckt_load(const ngsf_ckt_t &C, Ctl &s, const Iter &it)
 {
-    int nc = 0;
+    const int nb = C.wide ? gridDim.x : 1;
+    if (C.wide && threadIdx.x == 0)
+        wide_issue(C, s, NGSF_WIDE_LOAD);
+    int nc = load_phase(C, s, it, 0, nb, true);
+    gather_heavy_combine(C, it);
     __shared__ int wide_nc;
-    if (C.wide) {
-        if (threadIdx.x == 0)
-            wide_issue(C, s, NGSF_WIDE_LOAD);
-        nc = wide_transistors(C, s, it, 0, gridDim.x);
-        cap_load(C, s, it);
-        for (int i = threadIdx.x; i < C.dio.n; i += blockDim.x)
-            nc |= dio_load_one(C, s, it, i);
-        res_load(C);
-        src_load(C, s);
-        nc = block_or(s, nc);
-        if (threadIdx.x == 0) {
-            wide_nc = wide_collect(C, gridDim.x);
-            if (C.wide->err)
+    if (threadIdx.x == 0) {
+        wide_nc = 0;
+        if (C.wide) {
+            wide_nc = *(volatile int *)&C.wide->noncon;
+            if (*(volatile int *)&C.wide->err)
                 s.flag = NGSF_E_WATCHDOG;
-        }
-        __syncthreads();
-        nc |= wide_nc;
-    } else {
-        for (int i = threadIdx.x; i < C.bsim4.n; i += blockDim.x)
-            nc |= bsim4_load_one(C, s, it, i);
-        cap_load(C, s, it);
-        for (int i = threadIdx.x; i < C.dio.n; i += blockDim.x)
-            nc |= dio_load_one(C, s, it, i);
-        for (int i = threadIdx.x; i < C.mos1.n; i += blockDim.x)
-            nc |= mos1_load_one(C, s, it, i);
-        res_load(C);
-        src_load(C, s);
-        nc = block_or(s, nc);   /* includes __syncthreads: stamps visible */
-    }
-    /* Cells with up to NGSF_HEAVY contributions are summed by one thread
-     * in the reference's load order (bit-identical to CKTload).  The few
-     * cells that collect thousands of contributions (a supply node's
-     * diagonal) are summed by a warp: lane-strided partial sums in load
-     * order, then a fixed butterfly; the rounding then differs from the
-     * sequential sum by far less than the 1e-12 stamp tolerance. */
-    for (int p = threadIdx.x; p < C.nnz; p += blockDim.x) {
-        const int q0 = C.gptr[p], q1 = C.gptr[p + 1];
-        if (q1 - q0 > NGSF_HEAVY)
-            continue;
-        double acc = 0.0;
-        for (int q = q0; q < q1; q++)
-            acc += C.stampv[C.gsrc[q]];
-        C.ax[p] = acc;
-    }
-    for (int r = threadIdx.x; r <= C.n; r += blockDim.x) {
-        const int q0 = C.rptr[r], q1 = C.rptr[r + 1];
-        if (q1 - q0 > NGSF_HEAVY)
-            continue;
-        double acc = 0.0;
-        for (int q = q0; q < q1; q++)
-            acc += C.stampv[C.rsrc[q]];
-        it.rhs[r] = acc;
-    }
-    {
-        const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-        for (int h = warp; h < C.nheavy; h += NGSF_WARPS) {
-            const int p = C.heavy[h];
-            const bool isrhs = p < 0;
-            const int e = isrhs ? -p - 1 : p;
-            const int *ptr = isrhs ? C.rptr : C.gptr;
-            const int *src = isrhs ? C.rsrc : C.gsrc;
-            double acc = 0.0;
-            for (int q = ptr[e] + lane; q < ptr[e + 1]; q += 32)
-                acc += C.stampv[src[q]];
-            for (int o = 16; o > 0; o >>= 1)
-                acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (lane == 0) {
-                if (isrhs)
-                    it.rhs[e] = acc;
-                else
-                    C.ax[e] = acc;
-            }
         }
     }
     __syncthreads();
-    return nc;
+    return nc | wide_nc;
 }
 
 /* SMPluFac: left-looking refactorization on the fixed pivot sequence.
@@ -1003,8 +1057,111 @@ __device__ int ckt_load(const ngsf_ckt_t &C, Ctl &s, const Iter &it)
  * chooses new pivots from this matrix (the reference re-factors with
  * pivoting when refactoring fails, src/maths/ni/niiter.c:161-195). */
 #define NGSF_GROWTH 1e6
+
+/* Right-looking refactorization on the fixed pivot sequence, level by
+ * level of the column dependency graph (large matrices).  Phase p applies
+ * the updates of level p's pivot columns, each L entry divided by its
+ * pivot where it is used, and stores the scaled L entries of level p-1
+ * (which no update of level p reads or writes); one barrier per phase.
+ * The quotient and products are the ones a divide-then-update sweep
+ * computes, in the same order.  Over nb blocks of a wide launch (this is
+ * block b) a phase with little work runs in block 0 alone and only the
+ * change to a grid-wide phase costs a grid barrier. */
+#define NGSF_RL_SMALL 1024
+__device__ __forceinline__ int rl_phase_work(const ngsf_ckt_t &C, int p)
+{
+    int w = 0;
+    if (p < C.rl_levels)
+        w += C.ud_ptr[p + 1] - C.ud_ptr[p] + C.rl_ptr[p + 1] - C.rl_ptr[p];
+    if (p > 0)
+        w += C.sc_ptr[p] - C.sc_ptr[p - 1];
+    return w;
+}
+
+__device__ int rl_phase(const ngsf_ckt_t &C, int p, int t, int T)
+{
+    int bad = 0;
+    if (p < C.rl_levels) {
+        for (int c = C.rl_ptr[p] + t; c < C.rl_ptr[p + 1]; c += T) {
+            double piv = C.lux[C.cdiag[C.rl_col[c]]];
+            if (!(fabs(piv) > 0.0) || !isfinite(piv))
+                bad = 1;
+        }
+        for (int d = C.ud_ptr[p] + t; d < C.ud_ptr[p + 1]; d += T) {
+            const int dst = C.ud_dst[d];
+            double acc = C.lux[dst];
+            for (int c = C.ud_cptr[d]; c < C.ud_cptr[d + 1]; c++)
+                acc -= (C.lux[C.ud_l[c]] / C.lux[C.ud_p[c]]) * C.lux[C.ud_u[c]];
+            C.lux[dst] = acc;
+        }
+    }
+    if (p > 0) {
+        for (int e = C.sc_ptr[p - 1] + t; e < C.sc_ptr[p]; e += T) {
+            double l_ik = C.lux[C.sc_pos[e]] / C.lux[C.sc_piv[e]];
+            C.lux[C.sc_pos[e]] = l_ik;
+            if (!(fabs(l_ik) <= NGSF_GROWTH))
+                bad = 1;
+        }
+    }
+    return bad;
+}
+
+__device__ int lu_factor_rl(const ngsf_ckt_t &C, Ctl &s, int b, int nb)
+{
+    const int t = b * blockDim.x + threadIdx.x, T = nb * blockDim.x;
+    for (int q = t; q < C.nlu; q += T)
+        C.lux[q] = 0.0;
+    grid_sync(C, nb);
+    for (int p = t; p < C.nnz; p += T)
+        C.lux[C.a_lupos[p]] = C.ax[p];
+    grid_sync(C, nb);
+    if (s.diagGmin != 0.0) {
+        /* LoadGmin: gmin on every structural diagonal (klusmp.c:587-589) */
+        for (int j = t; j < C.n; j += T)
+            if (C.a_diag[j] >= 0)
+                C.lux[C.a_lupos[C.a_diag[j]]] += s.diagGmin;
+        grid_sync(C, nb);
+    }
+    int bad = 0;
+    const int L = C.rl_levels;
+    bool small = nb > 1 && rl_phase_work(C, 0) <= NGSF_RL_SMALL;
+    for (int p = 0; p <= L; p++) {
+        const bool nextSmall = p < L && nb > 1 && rl_phase_work(C, p + 1) <= NGSF_RL_SMALL;
+        if (small) {
+            if (b == 0) {
+                bad |= rl_phase(C, p, threadIdx.x, blockDim.x);
+                __syncthreads();
+            }
+            if (!nextSmall)
+                grid_sync(C, nb);
+        } else {
+            bad |= rl_phase(C, p, t, T);
+            grid_sync(C, nb);
+        }
+        small = nextSmall;
+    }
+    bad = block_or(s, bad);
+    if (nb > 1) {
+        if (threadIdx.x == 0 && bad)
+            atomicOr(&C.wide->bad, 1);
+        grid_sync(C, nb);
+        __shared__ int allbad;
+        if (threadIdx.x == 0)
+            allbad = *(volatile int *)&C.wide->bad;
+        __syncthreads();
+        bad = allbad;
+    }
+    return bad;
+}
+
 __device__ int lu_factor(const ngsf_ckt_t &C, Ctl &s)
 {
+    if (C.rl_levels > 0) {
+        const int nb = C.wide ? gridDim.x : 1;
+        if (C.wide && threadIdx.x == 0)
+            wide_issue(C, s, NGSF_WIDE_FACTOR);
+        return lu_factor_rl(C, s, 0, nb);
+    }
     for (int q = threadIdx.x; q < C.nlu; q += blockDim.x)
         C.lux[q] = 0.0;
     __syncthreads();
@@ -1020,32 +1177,6 @@ __device__ int lu_factor(const ngsf_ckt_t &C, Ctl &s)
     }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     int bad = 0;
-    if (C.rl_levels > 0) {
-        /* right-looking, two barriers per level (large matrices) */
-        for (int l = 0; l < C.rl_levels; l++) {
-            for (int c = C.rl_ptr[l] + threadIdx.x; c < C.rl_ptr[l + 1]; c += blockDim.x) {
-                double piv = C.lux[C.cdiag[C.rl_col[c]]];
-                if (!(fabs(piv) > 0.0) || !isfinite(piv))
-                    bad = 1;
-            }
-            for (int e = C.sc_ptr[l] + threadIdx.x; e < C.sc_ptr[l + 1]; e += blockDim.x) {
-                double l_ik = C.lux[C.sc_pos[e]] / C.lux[C.sc_piv[e]];
-                C.lux[C.sc_pos[e]] = l_ik;
-                if (!(fabs(l_ik) <= NGSF_GROWTH))
-                    bad = 1;
-            }
-            __syncthreads();
-            for (int d = C.ud_ptr[l] + threadIdx.x; d < C.ud_ptr[l + 1]; d += blockDim.x) {
-                const int dst = C.ud_dst[d];
-                double acc = C.lux[dst];
-                for (int c = C.ud_cptr[d]; c < C.ud_cptr[d + 1]; c++)
-                    acc -= C.lux[C.ud_l[c]] * C.lux[C.ud_u[c]];
-                C.lux[dst] = acc;
-            }
-            __syncthreads();
-        }
-        return block_or(s, bad);
-    }
     for (int l = 0; l < C.nlevels; l++) {
         for (int c = C.lvl_ptr[l] + warp; c < C.lvl_ptr[l + 1]; c += NGSF_WARPS) {
             int k = C.lvl_col[c];
@@ -1071,10 +1202,22 @@ __device__ int lu_factor(const ngsf_ckt_t &C, Ctl &s)
     return block_or(s, bad);
 }
 
+/* Triangular-solve workspace of this block: n+1 doubles of dynamic shared
+ * memory when they fit the launch's allocation, else C.work. */
+__shared__ double *g_sw;
+
+__device__ void solve_buffers_init(const ngsf_ckt_t &C, unsigned char *dyn, int dynBytes)
+{
+    if (threadIdx.x == 0)
+        g_sw = (dyn && (size_t)(C.n + 1) * sizeof(double) <= (size_t)dynBytes) ? (double *)dyn
+                                                                               : nullptr;
+    __syncthreads();
+}
+
 /* SMPsolve: x = A^-1 b, in place on rhs (row-oriented, level scheduled). */
 __device__ void lu_solve(const ngsf_ckt_t &C, Ctl &s, double *rhs)
 {
-    double *w = C.work;
+    double *w = g_sw ? g_sw : C.work;
     for (int k = threadIdx.x; k < C.n; k += blockDim.x)
         w[k] = rhs[C.prow[k]];
     __syncthreads();
@@ -1368,7 +1511,9 @@ __device__ void capture(const ngsf_ckt_t &C, Ctl &s, const Iter &it)
  * MODEINITTRAN: niiter.c:107-111, :328-346). */
 __device__ int ni_iter(const ngsf_ckt_t &C, Ctl &s, int maxIter, bool resume)
 {
-    if (maxIter < 100)
+    /* niiter.c raises the limit to 100; a start from the predictor's guess
+     * keeps itl4, after which the step is retried from the plain start */
+    if (maxIter < 100 && !(s.mode & NGSF_MODEGUESS))
         maxIter = 100;
     int iterno = resume ? s.savedIter : 0;
     for (;;) {
@@ -1432,11 +1577,15 @@ __device__ int ni_iter(const ngsf_ckt_t &C, Ctl &s, int maxIter, bool resume)
             __syncthreads();
             return NGSF_E_ITERLIM;
         }
-        if (noncon == 0 && iterno != 1)
+        /* NIconvTest from the second iteration (niiter.c), or already after
+         * the first when it started from the predictor's guess (every
+         * unknown against its guessed value, the same test) */
+        const bool guess1 = (s.mode & NGSF_MODEGUESS) && iterno == 1;
+        if (noncon == 0 && (iterno != 1 || guess1))
             noncon = conv_test(C, s, it);
         else
             noncon = 1;
-        int mode = s.mode;
+        int mode = s.mode & ~NGSF_MODEGUESS;
         int ret = -1, reorder = 0;
         if (mode & NGSF_MODEINITFLOAT) {
             if (noncon == 0)
@@ -1452,10 +1601,15 @@ __device__ int ni_iter(const ngsf_ckt_t &C, Ctl &s, int maxIter, bool resume)
                 reorder = 1;
             mode = (mode & ~NGSF_INITF) | NGSF_MODEINITFLOAT;
         } else if (mode & NGSF_MODEINITPRED) {
+            if (guess1 && noncon == 0)
+                ret = NGSF_OK;
             mode = (mode & ~NGSF_INITF) | NGSF_MODEINITFLOAT;
         }
         __syncthreads();
         if (threadIdx.x == 0) {
+            if (guess1 && ret == NGSF_OK)
+                s.guessFirst++;
+            s.mode &= ~NGSF_MODEGUESS;
             if (ret == NGSF_OK)
                 s.numIter += iterno;
             else {
@@ -1834,6 +1988,7 @@ __device__ int dc_tran(const ngsf_ckt_t &C, Ctl &s, long long maxSteps, bool res
                 return s.flag;
             if (s.time >= o.tstart)
                 dump_point(C, s);
+            pred_accept(C, s);
             if (almost_equal_ulps(s.time, o.tstop, 100))
                 return NGSF_OK;
             if (s.steps + 1 > maxSteps)
@@ -1878,14 +2033,33 @@ __device__ int dc_tran(const ngsf_ckt_t &C, Ctl &s, long long maxSteps, bool res
                 ni_comcof(C, s);
                 s.iters0 = s.numIter;
                 s.phase = PH_STEP_NIITER;
+                s.guessUsed = 0;
             }
             __syncthreads();
+            if (C.pred.kind && s.histCount >= 3 && (s.mode & NGSF_MODEINITPRED) && !s.guessOff)
+                pred_guess(C, s);
         }
         /* PH_STEP_NIITER */
         int converged = ni_iter(C, s, o.itl4, resume);
         resume = false;
         if (converged == NGSF_NEED_REORDER)
             return converged;
+        if (s.guessUsed && converged != 0 && converged != NGSF_E_SINGULAR &&
+            converged != NGSF_E_WATCHDOG) {
+            /* Newton from the predictor's guess missed itl4: the same step
+             * again from the plain start (INITPRED) */
+            if (threadIdx.x == 0) {
+                s.tranIter += s.numIter - s.iters0;
+                s.time -= s.delta;
+                s.guessOff = 1;
+                s.guessUsed = 0;
+                s.guessFalls++;
+                s.mode = NGSF_MODETRAN | NGSF_MODEINITPRED;
+                s.phase = PH_STEP;
+            }
+            __syncthreads();
+            continue;
+        }
         if (threadIdx.x == 0) {
             s.tranIter += s.numIter - s.iters0;
             s.timePts++;
@@ -1970,33 +2144,55 @@ __device__ int dc_tran(const ngsf_ckt_t &C, Ctl &s, long long maxSteps, bool res
 
 __device__ void run_circuit(const ngsf_ckt_t &C, Ctl &s, int runMode, long long maxSteps);
 
+/* Batched launch: a persistent grid (as many blocks as stay resident)
+ * takes circuits from a queue, largest first (order[]), and runs each
+ * circuit's transient in one block; a block that finishes a circuit takes
+ * the next one, so uneven circuits keep every SM busy until the queue is
+ * empty.  *queue starts at 0. */
 __global__ void __launch_bounds__(NGSF_THREADS)
-tran_kernel(const ngsf_ckt_t *ckts, int nckt, int runMode, long long maxSteps)
+tran_kernel(const ngsf_ckt_t *ckts, const int *order, int nckt, int *queue, int runMode,
+            long long maxSteps, int solveCap, int gnnBytes)
 {
+    extern __shared__ __align__(16) unsigned char ngsf_dyn[];
     __shared__ Ctl s;
     __shared__ __align__(16) ngsf_ckt_t Cs;
-    int b = blockIdx.x;
-    if (b >= nckt)
-        return;
-    {
-        const unsigned long long *src = (const unsigned long long *)(ckts + b);
-        unsigned long long *dst = (unsigned long long *)&Cs;
-        for (int w = threadIdx.x; w < (int)(sizeof(ngsf_ckt_t) / 8); w += blockDim.x)
-            dst[w] = src[w];
+    __shared__ int next;
+    pred_block_init(gnnBytes >= PRED_STAGE_BYTES ? ngsf_dyn + solveCap : nullptr);
+    for (;;) {
+        if (threadIdx.x == 0)
+            next = atomicAdd(queue, 1);
+        __syncthreads();
+        const int q = next;
+        if (q >= nckt)
+            break;
+        {
+            const unsigned long long *src = (const unsigned long long *)(ckts + order[q]);
+            unsigned long long *dst = (unsigned long long *)&Cs;
+            for (int w = threadIdx.x; w < (int)(sizeof(ngsf_ckt_t) / 8); w += blockDim.x)
+                dst[w] = src[w];
+        }
+        __syncthreads();
+        if (threadIdx.x == 0)
+            Cs.wide = nullptr;
+        __syncthreads();
+        solve_buffers_init(Cs, ngsf_dyn, solveCap);
+        run_circuit(Cs, s, runMode, maxSteps);
+        __syncthreads();
     }
-    __syncthreads();
-    Cs.wide = nullptr;
-    __syncthreads();
-    run_circuit(Cs, s, runMode, maxSteps);
+    pred_block_fini();
 }
 
 /* One circuit over the whole (cooperative) grid: block 0 runs the
  * transient, the other blocks evaluate transistors on its command. */
 __global__ void __launch_bounds__(NGSF_THREADS)
-tran_wide_kernel(const ngsf_ckt_t *ckt, int runMode, long long maxSteps)
+tran_wide_kernel(const ngsf_ckt_t *ckt, int runMode, long long maxSteps, int solveCap,
+                 int gnnBytes)
 {
+    extern __shared__ __align__(16) unsigned char ngsf_dyn[];
     __shared__ Ctl s;
     __shared__ __align__(16) ngsf_ckt_t Cs;
+    if (threadIdx.x == 0)
+        g_barGen = 0;
     {
         const unsigned long long *src = (const unsigned long long *)ckt;
         unsigned long long *dst = (unsigned long long *)&Cs;
@@ -2008,7 +2204,10 @@ tran_wide_kernel(const ngsf_ckt_t *ckt, int runMode, long long maxSteps)
         wide_worker(Cs, s);
         return;
     }
+    solve_buffers_init(Cs, ngsf_dyn, solveCap);
+    pred_block_init(gnnBytes >= PRED_STAGE_BYTES ? ngsf_dyn + solveCap : nullptr);
     run_circuit(Cs, s, runMode, maxSteps);
+    pred_block_fini();
     if (threadIdx.x == 0)
         wide_issue(Cs, s, NGSF_WIDE_EXIT);
 }
@@ -2037,6 +2236,9 @@ __device__ void run_circuit(const ngsf_ckt_t &C, Ctl &s, int runMode, long long 
             s.shouldReorder = 0;
             s.savedIter = s.savedNoncon = s.iters0 = s.reorders = 0;
             s.steps = 0;
+            s.tcur = s.th0 = s.th1 = 0.0;
+            s.histCount = s.guessOff = s.guessUsed = 0;
+            s.guessSteps = s.guessFirst = s.guessFalls = 0;
             s.gmin = C.opt.gmin;
             s.diagGmin = 0.0;
             s.srcFact = 1.0;
@@ -2097,6 +2299,9 @@ __device__ void run_circuit(const ngsf_ckt_t &C, Ctl &s, int runMode, long long 
         C.result[NGSF_R_OPITER] = s.opiter;
         C.result[NGSF_R_BADPIVOT] = s.badpivot;
         C.result[NGSF_R_REORDERS] = s.reorders;
+        C.result[NGSF_R_GUESSES] = s.guessSteps;
+        C.result[NGSF_R_GUESS1] = s.guessFirst;
+        C.result[NGSF_R_FALLBACKS] = s.guessFalls;
         C.fresult[NGSF_F_TIME] = s.time;
         C.fresult[NGSF_F_DELTA] = s.delta;
         C.fresult[NGSF_F_DIAGGMIN] = s.diagGmin;
@@ -2125,6 +2330,10 @@ __global__ void __launch_bounds__(NGSF_THREADS) stamp_static_kernel(ngsf_ckt_t C
     if (threadIdx.x == 0)
         Cs = C;
     __syncthreads();
+    if (threadIdx.x == 0) {      /* RUN_PROBE stamps only: no solve buffers */
+        g_sw = nullptr;
+        g_psm = nullptr;
+    }
     run_circuit(Cs, s, RUN_PROBE, 0);
 }
 
@@ -2140,7 +2349,8 @@ extern "C" int ngsf_wide_blocks(void)
         return 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
         return 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, tran_wide_kernel, NGSF_THREADS, 0) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, tran_wide_kernel, NGSF_THREADS,
+                                                      NGSF_SOLVE_SMEM_MAX + PRED_STAGE_BYTES) !=
         cudaSuccess)
         return 0;
     return sms * per;
@@ -2202,6 +2412,7 @@ extern "C" NGSF_API int ngsf_stamp_initial_static(const ngsf_handle *h, double *
     size_t o_ibrk = take((size_t)d->isrc.n * sizeof(double));
     size_t o_res = take(NGSF_R_COUNT * sizeof(int));
     size_t o_fres = take(NGSF_F_COUNT * sizeof(double));
+    size_t o_hpart = take((size_t)d->nhchunk * sizeof(double));
     if (off > NGSF_STATIC_SCRATCH_BYTES) {
         std::string m = "ngsf_stamp_initial_static: the circuit needs " + std::to_string(off) +
                         " bytes of scratch, more than the static " +
@@ -2232,9 +2443,11 @@ extern "C" NGSF_API int ngsf_stamp_initial_static(const ngsf_handle *h, double *
     c.vsrc.brk = (double *)(base + o_vbrk);
     c.isrc.brk = (double *)(base + o_ibrk);
     c.result = (int *)(base + o_res);
+    c.hpart = (double *)(base + o_hpart);
     c.fresult = (double *)(base + o_fres);
     c.capmax = 0;
     c.wide = nullptr;
+    c.pred.kind = 0;
     stamp_static_kernel<<<1, NGSF_THREADS>>>(c);
     e = cudaGetLastError();
     if (e == cudaSuccess && ax)
@@ -2250,19 +2463,88 @@ extern "C" NGSF_API int ngsf_stamp_initial_static(const ngsf_handle *h, double *
     return 0;
 }
 
-extern "C" cudaError_t ngsf_launch_tran_wide(const ngsf_ckt_t *d_ckt, int nblocks, int runMode,
-                                             long long maxSteps, cudaStream_t stream)
+/* Dynamic shared memory for the solve workspace of circuits with n
+ * unknowns: (n+1) doubles rounded to 128 bytes, or 0 when that exceeds
+ * NGSF_SOLVE_SMEM_MAX (the solve then works in global memory). */
+extern "C" int ngsf_solve_smem_bytes(int n)
 {
-    void *args[] = {(void *)&d_ckt, (void *)&runMode, (void *)&maxSteps};
-    return cudaLaunchCooperativeKernel((const void *)tran_wide_kernel, dim3(nblocks),
-                                       dim3(NGSF_THREADS), args, 0, stream);
+    size_t b = (size_t)(n + 1) * sizeof(double);
+    b = (b + 127) & ~(size_t)127;
+    return b <= (size_t)NGSF_SOLVE_SMEM_MAX ? (int)b : 0;
 }
 
-extern "C" cudaError_t ngsf_launch_tran(const ngsf_ckt_t *d_ckts, int nckt, int runMode,
-                                        long long maxSteps, cudaStream_t stream)
+/* staging of the predictor's network tiles (0 when no circuit has one) */
+extern "C" int ngsf_pred_smem_bytes(int any) { return any ? PRED_STAGE_BYTES : 0; }
+
+namespace {
+cudaError_t allow_dyn_smem(const void *fn)
+{
+    static std::mutex mu;
+    static const void *doneFn[16] = {nullptr};
+    static int doneDev[16];
+    static int ndone = 0;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess)
+        return e;
+    std::lock_guard<std::mutex> lock(mu);
+    for (int i = 0; i < ndone; i++)
+        if (doneFn[i] == fn && doneDev[i] == dev)
+            return cudaSuccess;
+    e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             NGSF_SOLVE_SMEM_MAX + PRED_STAGE_BYTES);
+    if (e == cudaSuccess && ndone < 16) {
+        doneFn[ndone] = fn;
+        doneDev[ndone++] = dev;
+    }
+    return e;
+}
+}  // namespace
+
+extern "C" cudaError_t ngsf_launch_tran_wide(const ngsf_ckt_t *d_ckt, int nblocks, int runMode,
+                                             long long maxSteps, int solveCap, int gnnBytes,
+                                             cudaStream_t stream)
+{
+    cudaError_t e = allow_dyn_smem((const void *)tran_wide_kernel);
+    if (e != cudaSuccess)
+        return e;
+    void *args[] = {(void *)&d_ckt, (void *)&runMode, (void *)&maxSteps, (void *)&solveCap,
+                    (void *)&gnnBytes};
+    return cudaLaunchCooperativeKernel((const void *)tran_wide_kernel, dim3(nblocks),
+                                       dim3(NGSF_THREADS), args,
+                                       (size_t)solveCap + (size_t)gnnBytes, stream);
+}
+
+/* Resident blocks of the batched kernel for a dynamic shared allocation. */
+extern "C" int ngsf_batch_blocks(int dynBytes)
+{
+    int dev = 0, sms = 0, per = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return 0;
+    if (allow_dyn_smem((const void *)tran_kernel) != cudaSuccess)
+        return 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, tran_kernel, NGSF_THREADS,
+                                                      (size_t)dynBytes) != cudaSuccess)
+        return 0;
+    return sms * per;
+}
+
+extern "C" cudaError_t ngsf_launch_tran(const ngsf_ckt_t *d_ckts, const int *d_order, int nckt,
+                                        int *d_queue, int nblocks, int runMode,
+                                        long long maxSteps, int solveCap, int gnnBytes,
+                                        cudaStream_t stream)
 {
     if (nckt <= 0)
         return cudaSuccess;
-    tran_kernel<<<nckt, NGSF_THREADS, 0, stream>>>(d_ckts, nckt, runMode, maxSteps);
+    cudaError_t e = allow_dyn_smem((const void *)tran_kernel);
+    if (e != cudaSuccess)
+        return e;
+    e = cudaMemsetAsync(d_queue, 0, sizeof(int), stream);
+    if (e != cudaSuccess)
+        return e;
+    tran_kernel<<<std::max(1, std::min(nblocks, nckt)), NGSF_THREADS,
+                  (size_t)solveCap + (size_t)gnnBytes, stream>>>(
+        d_ckts, d_order, nckt, d_queue, runMode, maxSteps, solveCap, gnnBytes);
     return cudaGetLastError();
 }

@@ -35,6 +35,10 @@ extern "C" {
 #define NGSF_MODEINITTRAN    0x1000
 #define NGSF_MODEINITPRED    0x2000
 #define NGSF_MODEUIC         0x10000
+/* engine-only bit (no reference counterpart): the first Newton iteration of
+ * a timestep starts from the predictor's guess in rhsOld (INITPRED state
+ * copies, terminal voltages from rhsOld) */
+#define NGSF_MODEGUESS       0x100000
 
 /* error codes, same values as src/include/ngspice/sperror.h */
 #define NGSF_OK         0
@@ -153,16 +157,41 @@ typedef struct {
  * evaluate their share of the device instances.  The words are handed over
  * with device-scope release/acquire; every wait is bounded. */
 #define NGSF_WIDE_CTL_BYTES 1024
-enum { NGSF_WIDE_LOAD = 1, NGSF_WIDE_EXIT = 2 };
+#define NGSF_HCHUNK 1024
+enum { NGSF_WIDE_LOAD = 1, NGSF_WIDE_EXIT = 2, NGSF_WIDE_FACTOR = 3 };
 typedef struct {
     int seq;              /* command number, bumped by block 0 (release) */
     int cmd;              /* NGSF_WIDE_* */
     int done;             /* blocks that finished the current command */
     int noncon;           /* OR of the workers' convergence flags */
     int err;              /* 1: a bounded wait ran out */
-    int pad[3];
+    int bad;              /* OR of the blocks' pivot checks (factor command) */
+    unsigned long long bar;  /* grid barrier: arrivals since the launch */
+    unsigned long long gen;  /* grid barrier: generations completed (last arriver) */
     unsigned long long ctl[NGSF_WIDE_CTL_BYTES / 8];  /* block 0's control words */
 } ngsf_wide_t;
+
+/* -------- learned Newton predictor (engine addition) ------------------ *
+ * Per circuit: the voltage unknowns, their neighbour graph and terminal
+ * counts, the last three accepted solutions, activations, and BF16 copies
+ * of the network (kind 2).  kind 0: off; 1: linear extrapolation guess;
+ * 2: linear extrapolation plus the network's correction. */
+#define NGSF_PRED_VSCALE 0.05
+#define NGSF_PRED_RATIO_MAX 4.0
+typedef struct {
+    int kind;
+    int nv;                       /* voltage unknowns */
+    const int *vnode;             /* [nv] equation index 1..n */
+    const int *gptr, *gidx;       /* neighbour CSR over 0..nv-1 */
+    const float *dinv;            /* [nv] 1 / degree */
+    const float *stat;            /* [nv][6] log(1 + terminal counts) */
+    float *Ha, *Hb;               /* [nv rounded to 128][64] activations */
+    double *cur, *h0, *h1;        /* [n+1] v_n, v_n-1, v_n-2 */
+    const unsigned short *WinT;   /* bf16 [64][16] */
+    const unsigned short *WT[3];  /* bf16 [64][128] */
+    const unsigned short *WoutT;  /* bf16 [16][64] */
+    const float *bin, *bl[3], *bout;
+} ngsf_pred_t;
 
 typedef struct {
     /* sizes */
@@ -228,8 +257,15 @@ typedef struct {
      * destinations with their lists of (L pos, U pos) products */
     int rl_levels;
     const int *rl_ptr, *rl_col, *sc_ptr, *sc_pos, *sc_piv;
-    const int *ud_ptr, *ud_dst, *ud_cptr, *ud_l, *ud_u;
+    const int *ud_ptr, *ud_dst, *ud_cptr, *ud_l, *ud_u, *ud_p;  /* ud_p: pivot pos */
     double *work;         /* [n] solve workspace */
+    /* matrix cells / rhs rows with more than NGSF_HEAVY contributions
+     * (heavy[]) are summed in chunks of NGSF_HCHUNK contributions: chunk c
+     * belongs to heavy entry hch_cell[c]; hch_ptr[h] is entry h's first
+     * chunk; hpart[c] holds the chunk's partial sum */
+    int nhchunk;
+    const int *hch_ptr, *hch_cell;
+    double *hpart;
 
     /* Newton / integration state */
     double *states;       /* [4][nstates] ring of CKTstates[0..3] */
@@ -259,13 +295,15 @@ typedef struct {
     int *result;          /* see NGSF_R_* */
     double *fresult;      /* see NGSF_F_* */
     ngsf_wide_t *wide;    /* set only for a wide (cooperative) launch */
+    ngsf_pred_t pred;     /* learned Newton predictor (kind 0: off) */
 } ngsf_ckt_t;
 
 /* integer results */
 enum {
     NGSF_R_STATUS, NGSF_R_NPOINTS, NGSF_R_ACCEPTED, NGSF_R_REJECTED,
     NGSF_R_NUMITER, NGSF_R_TRANITER, NGSF_R_TIMEPTS, NGSF_R_NCAP,
-    NGSF_R_OPITER, NGSF_R_BADPIVOT, NGSF_R_REORDERS, NGSF_R_COUNT
+    NGSF_R_OPITER, NGSF_R_BADPIVOT, NGSF_R_REORDERS, NGSF_R_GUESSES, NGSF_R_GUESS1,
+    NGSF_R_FALLBACKS, NGSF_R_COUNT
 };
 /* floating results */
 enum { NGSF_F_TIME, NGSF_F_DELTA, NGSF_F_DIAGGMIN, NGSF_F_COUNT };

@@ -19,6 +19,8 @@
 
 #include <chrono>
 #include <cstdlib>
+#include <algorithm>
+#include <cmath>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -26,13 +28,20 @@
 #include "circuit.h"
 #include "runtime.h"
 #include "bsim4.h"
+#include "dio.h"
 #include "sparse.h"
 
 extern "C" int ngsf_wide_blocks(void);
+extern "C" int ngsf_solve_smem_bytes(int n);
+extern "C" int ngsf_pred_smem_bytes(int any);
 extern "C" cudaError_t ngsf_launch_tran_wide(const ngsf_ckt_t *d_ckt, int nblocks, int runMode,
-                                             long long maxSteps, cudaStream_t stream);
-extern "C" cudaError_t ngsf_launch_tran(const ngsf_ckt_t *d_ckts, int nckt, int runMode,
-                                        long long maxSteps, cudaStream_t stream);
+                                             long long maxSteps, int solveCap, int gnnBytes,
+                                             cudaStream_t stream);
+extern "C" int ngsf_batch_blocks(int dynBytes);
+extern "C" cudaError_t ngsf_launch_tran(const ngsf_ckt_t *d_ckts, const int *d_order, int nckt,
+                                        int *d_queue, int nblocks, int runMode,
+                                        long long maxSteps, int solveCap, int gnnBytes,
+                                        cudaStream_t stream);
 extern "C" int ngsf_ctl_bytes(void);
 
 namespace ngsf {
@@ -66,6 +75,8 @@ struct DeviceCircuit::Impl {
     size_t bytes = 0;
     char *lubase = nullptr;
     size_t lubytes = 0;
+    char *predbase = nullptr;  /* Newton predictor arrays */
+    size_t predbytes = 0;
     ngsf_ckt_t h{};            /* device pointers */
     ngsf_ckt_t *d_desc = nullptr;
 };
@@ -77,6 +88,8 @@ DeviceCircuit::~DeviceCircuit()
         cudaFree(impl->base);
     if (impl->lubase)
         cudaFree(impl->lubase);
+    if (impl->predbase)
+        cudaFree(impl->predbase);
     if (impl->d_desc)
         cudaFree(impl->d_desc);
     delete impl;
@@ -114,7 +127,7 @@ void DeviceCircuit::upload(const Image &img, const std::vector<int> &probes, int
         size_t res_node, res_g;
         size_t cap_node, cap_st, cap_c, cap_m, cap_ic;
         size_t vs[9], is[9];
-        size_t ntype, stampv, ax, gptr, gsrc, rptr, rsrc, heavy, a_diag, opsave_rhs, opsave_st;
+        size_t ntype, stampv, ax, gptr, gsrc, rptr, rsrc, heavy, hch_ptr, hch_cell, hpart, a_diag, opsave_rhs, opsave_st;
         size_t lux, lvl_ptr, lvl_col, cdiag, cend, cbeg, kptr, kdep, kpos, kseg, upd_dst,
             upd_src, prow, pcol, fl_ptr, fl_row, bl_ptr, bl_row, lr_ptr, lr_col, lr_pos,
             ur_ptr, ur_col, ur_pos, work;
@@ -164,6 +177,20 @@ void DeviceCircuit::upload(const Image &img, const std::vector<int> &probes, int
     o.rptr = puti(img.rptr);
     o.rsrc = puti(img.rsrc);
     o.heavy = puti(img.heavy);
+    std::vector<int> hch_ptr(1, 0), hch_cell;
+    for (size_t h = 0; h < img.heavy.size(); h++) {
+        const int p = img.heavy[h];
+        const bool isrhs = p < 0;
+        const int e = isrhs ? -p - 1 : p;
+        const std::vector<int> &ptr = isrhs ? img.rptr : img.gptr;
+        const int m = ptr[e + 1] - ptr[e];
+        for (int c = 0; c < (m + NGSF_HCHUNK - 1) / NGSF_HCHUNK; c++)
+            hch_cell.push_back((int)h);
+        hch_ptr.push_back((int)hch_cell.size());
+    }
+    o.hch_ptr = puti(hch_ptr);
+    o.hch_cell = puti(hch_cell);
+    o.hpart = zero((size_t)std::max<size_t>(1, hch_cell.size()) * sizeof(double));
     o.a_diag = puti(img.a_diag);
     o.opsave_rhs = zero((size_t)(n + 1) * sizeof(double));
     o.opsave_st = zero((size_t)(img.nstates + 1) * sizeof(double));
@@ -223,6 +250,10 @@ void DeviceCircuit::upload(const Image &img, const std::vector<int> &probes, int
     h.rsrc = I(o.rsrc);
     h.nheavy = (int)img.heavy.size();
     h.heavy = I(o.heavy);
+    h.nhchunk = (int)hch_cell.size();
+    h.hch_ptr = I(o.hch_ptr);
+    h.hch_cell = I(o.hch_cell);
+    h.hpart = D(o.hpart);
     h.a_diag = I(o.a_diag);
     h.opsave_rhs = D(o.opsave_rhs);
     h.opsave_st = D(o.opsave_st);
@@ -255,7 +286,193 @@ void DeviceCircuit::upload(const Image &img, const std::vector<int> &probes, int
 
 const ngsf_ckt_t &DeviceCircuit::desc() const { return impl->h; }
 ngsf_ckt_t *DeviceCircuit::device_desc() const { return impl->d_desc; }
-size_t DeviceCircuit::bytes() const { return impl->bytes + impl->lubytes; }
+size_t DeviceCircuit::bytes() const
+{
+    return impl->bytes + impl->lubytes + impl->predbytes;
+}
+
+namespace {
+uint16_t to_bf16(float f)
+{
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    if ((u & 0x7fffffffu) > 0x7f800000u)
+        return (uint16_t)((u >> 16) | 0x40);      /* quiet NaN */
+    u += 0x7fffu + ((u >> 16) & 1u);              /* round to nearest even */
+    return (uint16_t)(u >> 16);
+}
+}  // namespace
+
+PredGraph pred_graph(const Image &img)
+{
+    PredGraph g;
+    const int n = img.n;
+    std::vector<int> pos(n + 1, -1);
+    for (int k = 1; k <= n; k++)
+        if (img.names[k - 1].find("#branch") == std::string::npos) {
+            pos[k] = (int)g.vnode.size();
+            g.vnode.push_back(k);
+        }
+    const int nv = (int)g.vnode.size();
+    std::vector<std::vector<int>> nb(nv);
+    for (int j = 0; j < n; j++) {
+        const int pj = pos[j + 1];
+        if (pj < 0)
+            continue;
+        for (int q = img.a_cp[j]; q < img.a_cp[j + 1]; q++) {
+            const int pi = pos[img.a_ri[q] + 1];
+            if (pi >= 0 && pi != pj) {
+                nb[pi].push_back(pj);
+                nb[pj].push_back(pi);
+            }
+        }
+    }
+    g.gptr.assign(nv + 1, 0);
+    g.dinv.assign(nv, 0.0f);
+    for (int v = 0; v < nv; v++) {
+        std::sort(nb[v].begin(), nb[v].end());
+        nb[v].erase(std::unique(nb[v].begin(), nb[v].end()), nb[v].end());
+        g.gidx.insert(g.gidx.end(), nb[v].begin(), nb[v].end());
+        g.gptr[v + 1] = (int)g.gidx.size();
+        if (!nb[v].empty())
+            g.dinv[v] = 1.0f / (float)nb[v].size();
+    }
+    std::vector<int> cnt((size_t)nv * 6, 0);
+    auto add = [&](int node, int col) {
+        if (node > 0 && node <= n && pos[node] >= 0)
+            cnt[(size_t)pos[node] * 6 + col]++;
+    };
+    for (int i = 0; i < img.nb4; i++) {
+        add(img.b4_node[B4N_G * img.nb4 + i], 0);
+        add(img.b4_node[B4N_D * img.nb4 + i], 1);
+        add(img.b4_node[B4N_S * img.nb4 + i], 1);
+        add(img.b4_node[B4N_B * img.nb4 + i], 2);
+    }
+    for (int i = 0; i < img.nmos1; i++) {
+        add(img.mos1_node[M1N_G * img.nmos1 + i], 0);
+        add(img.mos1_node[M1N_D * img.nmos1 + i], 1);
+        add(img.mos1_node[M1N_S * img.nmos1 + i], 1);
+        add(img.mos1_node[M1N_B * img.nmos1 + i], 2);
+    }
+    for (int i = 0; i < img.ndio; i++) {
+        add(img.dio_node[DIN_POS * img.ndio + i], 1);
+        add(img.dio_node[DIN_NEG * img.ndio + i], 1);
+    }
+    for (int i = 0; i < img.ncap; i++) {
+        add(img.cap_node[i], 3);
+        add(img.cap_node[img.ncap + i], 3);
+    }
+    for (int i = 0; i < img.nres; i++) {
+        add(img.res_node[i], 4);
+        add(img.res_node[img.nres + i], 4);
+    }
+    for (int i = 0; i < img.nvsrc; i++) {
+        add(img.vsrc_node[i], 5);
+        add(img.vsrc_node[img.nvsrc + i], 5);
+    }
+    for (int i = 0; i < img.nisrc; i++) {
+        add(img.isrc_node[i], 5);
+        add(img.isrc_node[img.nisrc + i], 5);
+    }
+    g.stat.resize(cnt.size());
+    for (size_t i = 0; i < cnt.size(); i++)
+        g.stat[i] = (float)std::log1p((double)cnt[i]);
+    return g;
+}
+
+/* Newton predictor: kind 0 off, 1 linear extrapolation, 2 with the network
+ * (params: the flat FP32 layout of ngsf_gnn_param_count() floats). */
+void DeviceCircuit::set_pred(const Image &img, int kind, const float *params)
+{
+    if (impl->predbase) {
+        cudaFree(impl->predbase);
+        impl->predbase = nullptr;
+        impl->predbytes = 0;
+    }
+    ngsf_pred_t &P = impl->h.pred;
+    memset(&P, 0, sizeof(P));
+    if (kind) {
+        PredGraph g = pred_graph(img);
+        const int nv = (int)g.vnode.size(), nvpad = (nv + 127) / 128 * 128, n1 = img.n + 1;
+        Arena a;
+        struct Plan {
+            size_t off;
+            const void *src;
+            size_t bytes;
+        };
+        std::vector<Plan> plans;
+        auto put = [&](const void *src, size_t bytes) {
+            size_t o = a.take(std::max<size_t>(bytes, 16));
+            if (bytes)
+                plans.push_back({o, src, bytes});
+            return o;
+        };
+        /* the network, BF16 transposed copies and FP32 biases */
+        std::vector<uint16_t> winT(64 * 16), wT[3], woutT(16 * 64);
+        std::vector<float> bias(64 * 4 + 1, 0.0f);
+        if (kind == 2) {
+            const float *Win = params, *bin = Win + 16 * 64;
+            for (int o = 0; o < 64; o++)
+                for (int i = 0; i < 16; i++)
+                    winT[o * 16 + i] = to_bf16(Win[i * 64 + o]);
+            memcpy(&bias[0], bin, 64 * 4);
+            const float *L = bin + 64;
+            for (int l = 0; l < 3; l++) {
+                const float *W = L + l * (128 * 64 + 64);
+                wT[l].resize(64 * 128);
+                for (int o = 0; o < 64; o++)
+                    for (int i = 0; i < 128; i++)
+                        wT[l][o * 128 + i] = to_bf16(W[i * 64 + o]);
+                memcpy(&bias[64 * (l + 1)], W + 128 * 64, 64 * 4);
+            }
+            const float *Wout = L + 3 * (128 * 64 + 64);
+            for (int o = 0; o < 16; o++)
+                for (int i = 0; i < 64; i++)
+                    woutT[o * 64 + i] = to_bf16(Wout[i * 16 + o]);
+            bias[256] = Wout[64 * 16];
+        }
+        size_t o_vnode = put(g.vnode.data(), nv * 4), o_gptr = put(g.gptr.data(), (nv + 1) * 4),
+               o_gidx = put(g.gidx.data(), g.gidx.size() * 4),
+               o_dinv = put(g.dinv.data(), nv * 4), o_stat = put(g.stat.data(), g.stat.size() * 4);
+        size_t o_ha = a.take((size_t)nvpad * 64 * 4), o_hb = a.take((size_t)nvpad * 64 * 4);
+        size_t o_cur = a.take(n1 * 8), o_h0 = a.take(n1 * 8), o_h1 = a.take(n1 * 8);
+        size_t o_win = put(winT.data(), kind == 2 ? winT.size() * 2 : 0), o_w[3];
+        for (int l = 0; l < 3; l++)
+            o_w[l] = put(wT[l].data(), wT[l].size() * 2);
+        size_t o_wout = put(woutT.data(), kind == 2 ? woutT.size() * 2 : 0);
+        size_t o_bias = put(bias.data(), bias.size() * 4);
+        ck(cudaMalloc(&impl->predbase, a.used), "cudaMalloc(predictor)");
+        ck(cudaMemset(impl->predbase, 0, a.used), "cudaMemset(predictor)");
+        impl->predbytes = a.used;
+        for (auto &pl : plans)
+            ck(cudaMemcpy(impl->predbase + pl.off, pl.src, pl.bytes, cudaMemcpyHostToDevice),
+               "cudaMemcpy(predictor)");
+        char *b = impl->predbase;
+        P.kind = kind;
+        P.nv = nv;
+        P.vnode = (const int *)(b + o_vnode);
+        P.gptr = (const int *)(b + o_gptr);
+        P.gidx = (const int *)(b + o_gidx);
+        P.dinv = (const float *)(b + o_dinv);
+        P.stat = (const float *)(b + o_stat);
+        P.Ha = (float *)(b + o_ha);
+        P.Hb = (float *)(b + o_hb);
+        P.cur = (double *)(b + o_cur);
+        P.h0 = (double *)(b + o_h0);
+        P.h1 = (double *)(b + o_h1);
+        P.WinT = (const unsigned short *)(b + o_win);
+        for (int l = 0; l < 3; l++)
+            P.WT[l] = (const unsigned short *)(b + o_w[l]);
+        P.WoutT = (const unsigned short *)(b + o_wout);
+        const float *bb = (const float *)(b + o_bias);
+        P.bin = bb;
+        for (int l = 0; l < 3; l++)
+            P.bl[l] = bb + 64 * (l + 1);
+        P.bout = bb + 256;
+    }
+    ck(cudaMemcpy(impl->d_desc, &impl->h, sizeof(impl->h), cudaMemcpyHostToDevice),
+       "cudaMemcpy(desc)");
+}
 
 /* Upload the LU plan (pivot sequence, layout, update lists, levels) into
  * its own allocation, replacing the previous plan. */
@@ -297,7 +514,8 @@ void DeviceCircuit::upload_lu(const Image &img)
            o_sc_ptr = puti(rl ? img.sc_ptr : none), o_sc_pos = puti(rl ? img.sc_pos : none),
            o_sc_piv = puti(rl ? img.sc_piv : none), o_ud_ptr = puti(rl ? img.ud_ptr : none),
            o_ud_dst = puti(rl ? img.ud_dst : none), o_ud_cptr = puti(rl ? img.ud_cptr : none),
-           o_ud_l = puti(rl ? img.ud_l : none), o_ud_u = puti(rl ? img.ud_u : none);
+           o_ud_l = puti(rl ? img.ud_l : none), o_ud_u = puti(rl ? img.ud_u : none),
+           o_ud_p = puti(rl ? img.ud_p : none);
     if (impl->lubase)
         cudaFree(impl->lubase);
     impl->lubase = nullptr;
@@ -353,6 +571,7 @@ void DeviceCircuit::upload_lu(const Image &img)
     h.ud_cptr = I(o_ud_cptr);
     h.ud_l = I(o_ud_l);
     h.ud_u = I(o_ud_u);
+    h.ud_p = I(o_ud_p);
     ck(cudaMemcpy(impl->d_desc, &h, sizeof(h), cudaMemcpyHostToDevice), "cudaMemcpy(desc)");
 }
 
@@ -426,8 +645,8 @@ void prepare(Prepared &p, const std::string &netlist, const std::vector<std::str
     p.probes = probes;
     p.dev = std::make_unique<DeviceCircuit>();
     p.dev->upload(p.img, probes, outcap, capmax);
-    /* large circuits spread their transistor evaluation over the whole
-     * device; NGSF_WIDE=0/1 overrides the size rule */
+    /* large circuits may take the whole device (a wide launch) when they
+     * run in a small batch; NGSF_WIDE=0/1 overrides the size rule */
     int transistors = p.img.nb4 + p.img.nmos1;
     bool wide = transistors >= 1024;
     if (const char *e = getenv("NGSF_WIDE"))
@@ -452,30 +671,62 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
 {
     std::vector<Prepared *> pending(cs.begin(), cs.end());
     int mode = 0;   /* RUN_FRESH */
+    /* a batch of many circuits fills the device with one block per
+     * circuit; only a batch of a few runs its large circuits wide */
+    bool allowWide = cs.size() <= 4;
+    if (const char *e = getenv("NGSF_WIDE"))
+        allowWide = atoi(e) != 0;
     double total = 0;
     int nl = 0;
     ngsf_ckt_t *d = nullptr;
     ck(cudaMalloc(&d, std::max<size_t>(1, cs.size()) * sizeof(ngsf_ckt_t)), "cudaMalloc(descs)");
+    int *d_order = nullptr, *d_queue = nullptr;
+    ck(cudaMalloc(&d_order, std::max<size_t>(1, cs.size()) * sizeof(int)), "cudaMalloc(order)");
+    ck(cudaMalloc(&d_queue, sizeof(int)), "cudaMalloc(queue)");
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
     try {
         while (!pending.empty()) {
-            if (nl > 64 + 8 * (int)cs.size())
+            if (nl > 256 + 8 * (int)cs.size())
                 throw std::runtime_error("too many re-pivot rounds");
             std::vector<ngsf_ckt_t> descs;
             std::vector<Prepared *> wide;
+            int maxn = 0, learned = 0;
             for (auto *c : pending) {
-                if (c->wide)
+                if (c->wide && allowWide) {
                     wide.push_back(c);
-                else
+                } else {
                     descs.push_back(c->dev->desc());
+                    maxn = std::max(maxn, c->img.n);
+                    learned |= c->dev->desc().pred.kind == 2;
+                }
             }
             if (!descs.empty()) {
                 ck(cudaMemcpy(d, descs.data(), descs.size() * sizeof(ngsf_ckt_t),
                               cudaMemcpyHostToDevice), "cudaMemcpy(descs)");
+                /* largest circuits first: the persistent blocks then finish
+                 * close together (longest-processing-time order) */
+                std::vector<int> order(descs.size());
+                for (size_t i = 0; i < order.size(); i++)
+                    order[i] = (int)i;
+                std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+                    const ngsf_ckt_t &x = descs[a], &y = descs[b];
+                    return (long long)x.nnz + 30LL * x.bsim4.n + 8LL * x.mos1.n >
+                           (long long)y.nnz + 30LL * y.bsim4.n + 8LL * y.mos1.n;
+                });
+                ck(cudaMemcpy(d_order, order.data(), order.size() * sizeof(int),
+                              cudaMemcpyHostToDevice), "cudaMemcpy(order)");
+                const int solveCap = ngsf_solve_smem_bytes(maxn);
+                const int gnnBytes = ngsf_pred_smem_bytes(learned);
+                int nblocks = ngsf_batch_blocks(solveCap + gnnBytes);
+                if (const char *e = getenv("NGSF_BATCH_BLOCKS"))
+                    nblocks = atoi(e);
+                if (nblocks <= 0)
+                    nblocks = (int)descs.size();
                 cudaEventRecord(e0, 0);
-                ck(ngsf_launch_tran(d, (int)descs.size(), mode, maxSteps, 0), "launch(tran)");
+                ck(ngsf_launch_tran(d, d_order, (int)descs.size(), d_queue, nblocks, mode,
+                                   maxSteps, solveCap, gnnBytes, 0), "launch(tran)");
                 cudaEventRecord(e1, 0);
                 ck(cudaEventSynchronize(e1), "tran");
                 float ms = 0;
@@ -488,7 +739,9 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
                 ck(cudaMemset(c->dev->desc().wide, 0, sizeof(ngsf_wide_t)), "cudaMemset(wide)");
                 int nb = c->wide_blocks;
                 cudaEventRecord(e0, 0);
-                ck(ngsf_launch_tran_wide(c->dev->device_desc(), nb, mode, maxSteps, 0),
+                ck(ngsf_launch_tran_wide(c->dev->device_desc(), nb, mode, maxSteps,
+                                        ngsf_solve_smem_bytes(c->img.n),
+                                        ngsf_pred_smem_bytes(c->dev->desc().pred.kind == 2), 0),
                    "launch(tran wide)");
                 cudaEventRecord(e1, 0);
                 ck(cudaEventSynchronize(e1), "tran wide");
@@ -532,11 +785,15 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
         cudaFree(d);
+        cudaFree(d_order);
+        cudaFree(d_queue);
         throw;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     cudaFree(d);
+    cudaFree(d_order);
+    cudaFree(d_queue);
     if (seconds)
         *seconds = total;
     if (launches)

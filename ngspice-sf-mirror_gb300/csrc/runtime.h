@@ -25,6 +25,7 @@ public:
     void read_points(int npoints, std::vector<double> &out);
     void read_capture(int ncap, std::vector<double> &ax, std::vector<double> &rhs,
                       std::vector<double> &meta);
+    void set_pred(const Image &img, int kind, const float *params);
     const ngsf_ckt_t &desc() const;
     ngsf_ckt_t *device_desc() const;
     size_t bytes() const;
@@ -35,6 +36,16 @@ private:
     std::vector<int> probes_;
     int n_ = 0, nnz_ = 0, outcap_ = 0, capmax_ = 0;
 };
+
+/* The Newton predictor's view of a circuit: its voltage unknowns (equation
+ * indices 1..n), their neighbour lists from the matrix pattern (symmetric,
+ * sorted), 1/degree, and per node log(1 + count) of the incident MOSFET
+ * gate, drain/source, bulk, capacitor, resistor and source terminals. */
+struct PredGraph {
+    std::vector<int> vnode, gptr, gidx;
+    std::vector<float> dinv, stat;
+};
+PredGraph pred_graph(const Image &img);
 
 /* A circuit compiled, pivoted and resident on the device. */
 struct Prepared {

@@ -16,6 +16,7 @@
  */
 #include <algorithm>
 #include <cmath>
+#include <array>
 #include <map>
 #include <set>
 #include <unordered_map>
@@ -377,8 +378,9 @@ bool plan_lu(int n, const std::vector<int> &cp, const std::vector<int> &ri,
         img.ud_cptr.assign(1, 0);
         img.ud_l.clear();
         img.ud_u.clear();
+        img.ud_p.clear();
         for (int l = 0; l < nl; l++) {
-            std::map<int, std::vector<std::pair<int, int>>> dst;
+            std::map<int, std::vector<std::array<int, 3>>> dst;
             for (int k : piv[l]) {
                 img.rl_col.push_back(k);
                 for (size_t s2 = 0; s2 < lcol[k].size(); s2++) {
@@ -395,15 +397,16 @@ bool plan_lu(int n, const std::vector<int> &cp, const std::vector<int> &ri,
                             err = "internal: fill closure violated (right-looking)";
                             return false;
                         }
-                        dst[d].push_back({lpos, upos});
+                        dst[d].push_back({lpos, upos, img.cdiag[k]});
                     }
                 }
             }
             for (auto &de : dst) {
                 img.ud_dst.push_back(de.first);
                 for (auto &c : de.second) {
-                    img.ud_l.push_back(c.first);
-                    img.ud_u.push_back(c.second);
+                    img.ud_l.push_back(c[0]);
+                    img.ud_u.push_back(c[1]);
+                    img.ud_p.push_back(c[2]);
                 }
                 img.ud_cptr.push_back((int)img.ud_l.size());
             }

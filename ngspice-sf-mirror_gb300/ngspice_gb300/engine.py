@@ -17,8 +17,8 @@ LIB_PATH = os.path.join(PKG, "lib", "libngspice_gb300.so")
 
 # integer result slots (ngsf_types.h NGSF_R_*)
 R_STATUS, R_NPOINTS, R_ACCEPTED, R_REJECTED, R_NUMITER, R_TRANITER, R_TIMEPTS, \
-    R_NCAP, R_OPITER, R_BADPIVOT, R_REORDERS = range(11)
-R_COUNT = 11
+    R_NCAP, R_OPITER, R_BADPIVOT, R_REORDERS, R_GUESSES, R_GUESS1, R_FALLBACKS = range(14)
+R_COUNT = 14
 F_COUNT = 3
 
 # C-ABI symbols declared in include/*.h
@@ -27,6 +27,9 @@ EXPORTS = [
     "ngsf_eq_name", "ngsf_pattern", "ngsf_probes", "ngsf_run", "ngsf_results",
     "ngsf_points", "ngsf_capture", "ngsf_lu_flops", "ngsf_device_bytes",
     "ngsf_last_launches", "ngsf_workload", "ngsf_stamp_initial_static",
+    "ngsf_gnn_param_count", "ngsf_gnn_create", "ngsf_gnn_destroy", "ngsf_gnn_set_params",
+    "ngsf_gnn_get_params", "ngsf_gnn_forward", "ngsf_gnn_train_step", "ngsf_gnn_gemm_test",
+    "ngsf_node_graph", "ngsf_set_predictor",
     "ngSpice_Init", "ngSpice_Init_Sync", "ngSpice_Command", "ngGet_Vec_Info",
     "ngSpice_Circ", "ngSpice_CurPlot", "ngSpice_AllPlots", "ngSpice_AllVecs",
     "ngSpice_running", "ngSpice_SetBkpt", "ngSpice_nospinit", "ngSpice_nospiceinit",
@@ -70,6 +73,10 @@ def lib(path: str | None = None) -> C.CDLL:
     L.ngsf_device_bytes.argtypes = [vp]
     L.ngsf_last_launches.restype = C.c_int
     L.ngsf_workload.argtypes = [vp, C.POINTER(C.c_longlong)]
+    fp = C.POINTER(C.c_float)
+    if hasattr(L, "ngsf_node_graph"):
+        L.ngsf_node_graph.argtypes = [vp, ip, ip, ip, ip, ip, fp]
+        L.ngsf_set_predictor.argtypes = [vp, C.c_int, fp]
     _lib = L
     return L
 
@@ -167,6 +174,32 @@ class Circuit:
 
     def device_bytes(self) -> int:
         return int(lib().ngsf_device_bytes(self._h))
+
+    def node_graph(self) -> dict:
+        """The predictor's view: voltage unknowns (0-based equation index),
+        neighbour CSR and log(1 + terminal counts)."""
+        L = lib()
+        nv, ne = C.c_int(), C.c_int()
+        L.ngsf_node_graph(self._h, C.byref(nv), C.byref(ne), None, None, None, None)
+        vnode = np.zeros(nv.value, np.int32)
+        gptr = np.zeros(nv.value + 1, np.int32)
+        gidx = np.zeros(max(ne.value, 1), np.int32)
+        stat = np.zeros((nv.value, 6), np.float32)
+        if L.ngsf_node_graph(self._h, None, None, _ptr(vnode, C.c_int), _ptr(gptr, C.c_int),
+                             _ptr(gidx, C.c_int), stat.ctypes.data_as(C.POINTER(C.c_float))):
+            raise EngineError(last_error())
+        return {"vnode": vnode - 1, "gptr": gptr, "gidx": gidx[:ne.value], "stat": stat}
+
+    def set_predictor(self, kind: int, params: np.ndarray | None = None):
+        """0: off (the reference's Newton start), 1: linear extrapolation,
+        2: with the trained network (flat parameters)."""
+        p = None
+        if params is not None:
+            params = np.ascontiguousarray(params, np.float32)
+            self._pred_params = params
+            p = params.ctypes.data_as(C.POINTER(C.c_float))
+        if lib().ngsf_set_predictor(self._h, int(kind), p):
+            raise EngineError(last_error())
 
     def workload(self) -> dict:
         a = (C.c_longlong * 10)()

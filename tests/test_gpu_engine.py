@@ -164,6 +164,26 @@ def test_wide_launch_equals_single_block(E, monkeypatch):
     np.testing.assert_array_equal(out["0"][1][1], out["1"][1][1])
 
 
+def test_wide_right_looking_equals_single_block(E, monkeypatch):
+    """The right-looking refactorization spread over the cooperative grid
+    (grid barriers, small phases in block 0) and the grid-wide gather give
+    bit-identical points to the same schedule in one block."""
+    monkeypatch.setenv("NGSF_LU", "rl")
+    g = golden("bsim4_logic_s3")
+    text = str(g["netlist"])
+    out = {}
+    for wide in ("0", "1"):
+        monkeypatch.setenv("NGSF_WIDE", wide)
+        c = run_one(E, text)
+        r = c.results()
+        assert r[E.R_STATUS] == 0
+        out[wide] = (list(r[[E.R_ACCEPTED, E.R_REJECTED, E.R_NUMITER, E.R_TRANITER]]),
+                     c.points())
+    assert out["0"][0] == out["1"][0]
+    np.testing.assert_array_equal(out["0"][1][0], out["1"][1][0])
+    np.testing.assert_array_equal(out["0"][1][1], out["1"][1][1])
+
+
 def test_right_looking_lu_matches_reference(E, monkeypatch):
     """The right-looking level-scheduled refactorization (the large-matrix
     path) forced on the BSIM4 logic deck: same Newton and step counts as the
@@ -202,6 +222,28 @@ def test_batch_equals_single_runs(E):
     batch = [E.Circuit(t) for t in texts]
     E.run(batch, max_steps=1_000_000)
     for a, b in zip(alone, batch):
+        ta, va = a.points()
+        tb, vb = b.points()
+        np.testing.assert_array_equal(ta, tb)
+        np.testing.assert_array_equal(va, vb)
+
+
+def test_persistent_batch_retires_and_refills(E, monkeypatch):
+    """Monte Carlo instances of uneven size (device mismatch) on a grid of
+    two persistent blocks: each block takes the next circuit from the queue
+    when it finishes one; every circuit's result is bit-identical to its
+    run alone."""
+    from ngspice_gb300 import netlists
+    texts = [netlists.random_logic(n_transistors=n, seed=40 + i, tstop="30p", mismatch=True)
+             for i, n in enumerate((60, 220, 40, 150, 90))]
+    alone = [run_one(E, t) for t in texts]
+    monkeypatch.setenv("NGSF_BATCH_BLOCKS", "2")
+    batch = [E.Circuit(t) for t in texts]
+    E.run(batch, max_steps=1_000_000)
+    for a, b in zip(alone, batch):
+        ra, rb = a.results(), b.results()
+        assert rb[E.R_STATUS] == 0
+        assert list(ra[:7]) == list(rb[:7])
         ta, va = a.points()
         tb, vb = b.points()
         np.testing.assert_array_equal(ta, tb)
