@@ -168,7 +168,10 @@ NGSF_API int ngsf_node_graph(const ngsf_handle *h, int *nv, int *nedges, int *vn
  * retried from the plain start.  Features per node at step n: v_n,
  * (v_n - v_{n-1})/0.05, (v_{n-1} - v_{n-2})/0.05, r1 = h_{n+1}/h_n and
  * r2 = h_n/h_{n-1} (each at most 4), r1 (v_n - v_{n-1})/0.05, stat[6], 1,
- * 0, 0, 0; the guess is v_n + r1 (v_n - v_{n-1}) + 0.05 pred. */
+ * r1 (r1+1) r2 (d1 - r2 d2) / ((r2+1) 0.05) with d1 = v_n - v_{n-1},
+ * d2 = v_{n-1} - v_{n-2}, 0, 0; the guess is v_n + r1 d1 + 0.05 g pred
+ * with g = a / (a + 1e-4 V), a = |d1| + |d2| (quiet nodes keep the
+ * linear extrapolation). */
 NGSF_API int ngsf_set_predictor(ngsf_handle *h, int kind, const float *params);
 
 #ifdef __cplusplus

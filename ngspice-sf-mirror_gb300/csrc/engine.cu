@@ -1106,6 +1106,35 @@ __device__ int rl_phase(const ngsf_ckt_t &C, int p, int t, int T)
     return bad;
 }
 
+/* One block: per level, the L entries of its pivots are divided first
+ * (one division per entry), then the updates use the stored quotients;
+ * the same quotients and products as rl_phase, two barriers per level. */
+__device__ int rl_level_block(const ngsf_ckt_t &C, int l)
+{
+    int bad = 0;
+    for (int c = C.rl_ptr[l] + threadIdx.x; c < C.rl_ptr[l + 1]; c += blockDim.x) {
+        double piv = C.lux[C.cdiag[C.rl_col[c]]];
+        if (!(fabs(piv) > 0.0) || !isfinite(piv))
+            bad = 1;
+    }
+    for (int e = C.sc_ptr[l] + threadIdx.x; e < C.sc_ptr[l + 1]; e += blockDim.x) {
+        double l_ik = C.lux[C.sc_pos[e]] / C.lux[C.sc_piv[e]];
+        C.lux[C.sc_pos[e]] = l_ik;
+        if (!(fabs(l_ik) <= NGSF_GROWTH))
+            bad = 1;
+    }
+    __syncthreads();
+    for (int d = C.ud_ptr[l] + threadIdx.x; d < C.ud_ptr[l + 1]; d += blockDim.x) {
+        const int dst = C.ud_dst[d];
+        double acc = C.lux[dst];
+        for (int c = C.ud_cptr[d]; c < C.ud_cptr[d + 1]; c++)
+            acc -= C.lux[C.ud_l[c]] * C.lux[C.ud_u[c]];
+        C.lux[dst] = acc;
+    }
+    __syncthreads();
+    return bad;
+}
+
 __device__ int lu_factor_rl(const ngsf_ckt_t &C, Ctl &s, int b, int nb)
 {
     const int t = b * blockDim.x + threadIdx.x, T = nb * blockDim.x;
@@ -1124,9 +1153,14 @@ __device__ int lu_factor_rl(const ngsf_ckt_t &C, Ctl &s, int b, int nb)
     }
     int bad = 0;
     const int L = C.rl_levels;
-    bool small = nb > 1 && rl_phase_work(C, 0) <= NGSF_RL_SMALL;
+    if (nb <= 1) {
+        for (int l = 0; l < L; l++)
+            bad |= rl_level_block(C, l);
+        return block_or(s, bad);
+    }
+    bool small = rl_phase_work(C, 0) <= NGSF_RL_SMALL;
     for (int p = 0; p <= L; p++) {
-        const bool nextSmall = p < L && nb > 1 && rl_phase_work(C, p + 1) <= NGSF_RL_SMALL;
+        const bool nextSmall = p < L && rl_phase_work(C, p + 1) <= NGSF_RL_SMALL;
         if (small) {
             if (b == 0) {
                 bad |= rl_phase(C, p, threadIdx.x, blockDim.x);
@@ -2144,41 +2178,34 @@ __device__ int dc_tran(const ngsf_ckt_t &C, Ctl &s, long long maxSteps, bool res
 
 __device__ void run_circuit(const ngsf_ckt_t &C, Ctl &s, int runMode, long long maxSteps);
 
-/* Batched launch: a persistent grid (as many blocks as stay resident)
- * takes circuits from a queue, largest first (order[]), and runs each
- * circuit's transient in one block; a block that finishes a circuit takes
- * the next one, so uneven circuits keep every SM busy until the queue is
- * empty.  *queue starts at 0. */
+/* Batched launch: block b runs the transient of circuit order[b] (the
+ * host orders the circuits largest first).  The hardware block scheduler
+ * starts a waiting block on an SM as soon as a block there retires, so
+ * circuits of uneven size keep every SM busy and the largest ones start
+ * first (longest-processing-time order). */
 __global__ void __launch_bounds__(NGSF_THREADS)
-tran_kernel(const ngsf_ckt_t *ckts, const int *order, int nckt, int *queue, int runMode,
+tran_kernel(const ngsf_ckt_t *ckts, const int *order, int nckt, int runMode,
             long long maxSteps, int solveCap, int gnnBytes)
 {
     extern __shared__ __align__(16) unsigned char ngsf_dyn[];
     __shared__ Ctl s;
     __shared__ __align__(16) ngsf_ckt_t Cs;
-    __shared__ int next;
+    const int q = blockIdx.x;
+    if (q >= nckt)
+        return;
     pred_block_init(gnnBytes >= PRED_STAGE_BYTES ? ngsf_dyn + solveCap : nullptr);
-    for (;;) {
-        if (threadIdx.x == 0)
-            next = atomicAdd(queue, 1);
-        __syncthreads();
-        const int q = next;
-        if (q >= nckt)
-            break;
-        {
-            const unsigned long long *src = (const unsigned long long *)(ckts + order[q]);
-            unsigned long long *dst = (unsigned long long *)&Cs;
-            for (int w = threadIdx.x; w < (int)(sizeof(ngsf_ckt_t) / 8); w += blockDim.x)
-                dst[w] = src[w];
-        }
-        __syncthreads();
-        if (threadIdx.x == 0)
-            Cs.wide = nullptr;
-        __syncthreads();
-        solve_buffers_init(Cs, ngsf_dyn, solveCap);
-        run_circuit(Cs, s, runMode, maxSteps);
-        __syncthreads();
+    {
+        const unsigned long long *src = (const unsigned long long *)(ckts + order[q]);
+        unsigned long long *dst = (unsigned long long *)&Cs;
+        for (int w = threadIdx.x; w < (int)(sizeof(ngsf_ckt_t) / 8); w += blockDim.x)
+            dst[w] = src[w];
     }
+    __syncthreads();
+    if (threadIdx.x == 0)
+        Cs.wide = nullptr;
+    __syncthreads();
+    solve_buffers_init(Cs, ngsf_dyn, solveCap);
+    run_circuit(Cs, s, runMode, maxSteps);
     pred_block_fini();
 }
 
@@ -2341,6 +2368,10 @@ static_assert(sizeof(Ctl) <= NGSF_WIDE_CTL_BYTES, "control block does not fit th
 
 extern "C" int ngsf_ctl_bytes(void) { return (int)sizeof(Ctl); }
 
+namespace {
+cudaError_t allow_dyn_smem(const void *fn);
+}
+
 /* Blocks a cooperative wide launch can keep resident on this device. */
 extern "C" int ngsf_wide_blocks(void)
 {
@@ -2348,6 +2379,9 @@ extern "C" int ngsf_wide_blocks(void)
     if (cudaGetDevice(&dev) != cudaSuccess)
         return 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return 0;
+    /* the launch may ask for the largest dynamic allocation: allow it first */
+    if (allow_dyn_smem((const void *)tran_wide_kernel) != cudaSuccess)
         return 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, tran_wide_kernel, NGSF_THREADS,
                                                       NGSF_SOLVE_SMEM_MAX + PRED_STAGE_BYTES) !=
@@ -2515,36 +2549,16 @@ extern "C" cudaError_t ngsf_launch_tran_wide(const ngsf_ckt_t *d_ckt, int nblock
                                        (size_t)solveCap + (size_t)gnnBytes, stream);
 }
 
-/* Resident blocks of the batched kernel for a dynamic shared allocation. */
-extern "C" int ngsf_batch_blocks(int dynBytes)
-{
-    int dev = 0, sms = 0, per = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess ||
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-        return 0;
-    if (allow_dyn_smem((const void *)tran_kernel) != cudaSuccess)
-        return 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, tran_kernel, NGSF_THREADS,
-                                                      (size_t)dynBytes) != cudaSuccess)
-        return 0;
-    return sms * per;
-}
-
 extern "C" cudaError_t ngsf_launch_tran(const ngsf_ckt_t *d_ckts, const int *d_order, int nckt,
-                                        int *d_queue, int nblocks, int runMode,
-                                        long long maxSteps, int solveCap, int gnnBytes,
-                                        cudaStream_t stream)
+                                        int runMode, long long maxSteps, int solveCap,
+                                        int gnnBytes, cudaStream_t stream)
 {
     if (nckt <= 0)
         return cudaSuccess;
     cudaError_t e = allow_dyn_smem((const void *)tran_kernel);
     if (e != cudaSuccess)
         return e;
-    e = cudaMemsetAsync(d_queue, 0, sizeof(int), stream);
-    if (e != cudaSuccess)
-        return e;
-    tran_kernel<<<std::max(1, std::min(nblocks, nckt)), NGSF_THREADS,
-                  (size_t)solveCap + (size_t)gnnBytes, stream>>>(
-        d_ckts, d_order, nckt, d_queue, runMode, maxSteps, solveCap, gnnBytes);
+    tran_kernel<<<nckt, NGSF_THREADS, (size_t)solveCap + (size_t)gnnBytes, stream>>>(
+        d_ckts, d_order, nckt, runMode, maxSteps, solveCap, gnnBytes);
     return cudaGetLastError();
 }

@@ -178,6 +178,7 @@ typedef struct {
  * 2: linear extrapolation plus the network's correction. */
 #define NGSF_PRED_VSCALE 0.05
 #define NGSF_PRED_RATIO_MAX 4.0
+#define NGSF_PRED_QUIET 1e-4     /* V: activity at which the correction is halved */
 typedef struct {
     int kind;
     int nv;                       /* voltage unknowns */

@@ -157,6 +157,9 @@ __device__ bool pred_network(const ngsf_ckt_t &C, const Iter &it, double r1, dou
                     f[2] = P.stat[(size_t)v * 6 + 4];
                     f[3] = P.stat[(size_t)v * 6 + 5];
                     f[4] = 1.0f;
+                    /* quadratic-extrapolation increment through the last
+                     * three points, beyond the linear one */
+                    f[5] = (float)(r1 * (r1 + 1.0) * r2 * (d1 - r2 * (v2 - v1)) / ((r2 + 1.0) * VS));
                 }
             }
             put8(sA, r, g * 8, 16, f);
@@ -248,8 +251,12 @@ __device__ bool pred_network(const ngsf_ckt_t &C, const Iter &it, double r1, dou
             float a[16];
             tc05_ld16(g_tmem + ((uint32_t)(warp * 32) << 16), a);
             if (v < nv) {
+                /* the correction fades out on quiet nodes, where the
+                 * linear extrapolation is already exact */
                 const int k = P.vnode[v];
-                it.rhsOld[k] += VS * (double)(a[0] + P.bout[0]);
+                const double act = fabs(P.cur[k] - P.h0[k]) + fabs(P.h0[k] - P.h1[k]);
+                const double gate = act / (act + NGSF_PRED_QUIET);
+                it.rhsOld[k] += VS * gate * (double)(a[0] + P.bout[0]);
             }
         }
         tc05_fence_before();

@@ -37,11 +37,9 @@ extern "C" int ngsf_pred_smem_bytes(int any);
 extern "C" cudaError_t ngsf_launch_tran_wide(const ngsf_ckt_t *d_ckt, int nblocks, int runMode,
                                              long long maxSteps, int solveCap, int gnnBytes,
                                              cudaStream_t stream);
-extern "C" int ngsf_batch_blocks(int dynBytes);
 extern "C" cudaError_t ngsf_launch_tran(const ngsf_ckt_t *d_ckts, const int *d_order, int nckt,
-                                        int *d_queue, int nblocks, int runMode,
-                                        long long maxSteps, int solveCap, int gnnBytes,
-                                        cudaStream_t stream);
+                                        int runMode, long long maxSteps, int solveCap,
+                                        int gnnBytes, cudaStream_t stream);
 extern "C" int ngsf_ctl_bytes(void);
 
 namespace ngsf {
@@ -680,9 +678,8 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
     int nl = 0;
     ngsf_ckt_t *d = nullptr;
     ck(cudaMalloc(&d, std::max<size_t>(1, cs.size()) * sizeof(ngsf_ckt_t)), "cudaMalloc(descs)");
-    int *d_order = nullptr, *d_queue = nullptr;
+    int *d_order = nullptr;
     ck(cudaMalloc(&d_order, std::max<size_t>(1, cs.size()) * sizeof(int)), "cudaMalloc(order)");
-    ck(cudaMalloc(&d_queue, sizeof(int)), "cudaMalloc(queue)");
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
@@ -705,8 +702,8 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
             if (!descs.empty()) {
                 ck(cudaMemcpy(d, descs.data(), descs.size() * sizeof(ngsf_ckt_t),
                               cudaMemcpyHostToDevice), "cudaMemcpy(descs)");
-                /* largest circuits first: the persistent blocks then finish
-                 * close together (longest-processing-time order) */
+                /* largest circuits first: the block scheduler then starts
+                 * them first (longest-processing-time order) */
                 std::vector<int> order(descs.size());
                 for (size_t i = 0; i < order.size(); i++)
                     order[i] = (int)i;
@@ -719,14 +716,9 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
                               cudaMemcpyHostToDevice), "cudaMemcpy(order)");
                 const int solveCap = ngsf_solve_smem_bytes(maxn);
                 const int gnnBytes = ngsf_pred_smem_bytes(learned);
-                int nblocks = ngsf_batch_blocks(solveCap + gnnBytes);
-                if (const char *e = getenv("NGSF_BATCH_BLOCKS"))
-                    nblocks = atoi(e);
-                if (nblocks <= 0)
-                    nblocks = (int)descs.size();
                 cudaEventRecord(e0, 0);
-                ck(ngsf_launch_tran(d, d_order, (int)descs.size(), d_queue, nblocks, mode,
-                                   maxSteps, solveCap, gnnBytes, 0), "launch(tran)");
+                ck(ngsf_launch_tran(d, d_order, (int)descs.size(), mode, maxSteps, solveCap,
+                                   gnnBytes, 0), "launch(tran)");
                 cudaEventRecord(e1, 0);
                 ck(cudaEventSynchronize(e1), "tran");
                 float ms = 0;
@@ -786,14 +778,12 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
         cudaEventDestroy(e1);
         cudaFree(d);
         cudaFree(d_order);
-        cudaFree(d_queue);
         throw;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     cudaFree(d);
     cudaFree(d_order);
-    cudaFree(d_queue);
     if (seconds)
         *seconds = total;
     if (launches)

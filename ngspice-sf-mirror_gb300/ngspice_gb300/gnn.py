@@ -5,12 +5,16 @@ The network predicts, per circuit node, a correction to the linear
 extrapolation of the node voltage to the next accepted timepoint:
 
     v_lin  = v_n + r1 (v_n - v_{n-1}),      r1 = h_{n+1} / h_n
-    v_next ~ v_lin + VSCALE * pred
+    v_next ~ v_lin + VSCALE * g * pred,     g = a / (a + QUIET),
+    a = |v_n - v_{n-1}| + |v_{n-1} - v_{n-2}|
 
 Node features (16): v_n, (v_n - v_{n-1}) / VSCALE, (v_{n-1} - v_{n-2}) /
 VSCALE, r1, r2 = h_n / h_{n-1}, r1 (v_n - v_{n-1}) / VSCALE, log(1 + count)
 of the incident MOSFET gate, drain/source, bulk, capacitor, resistor and
-source terminals (Circuit.node_graph), a constant 1, zeros.
+source terminals (Circuit.node_graph), a constant 1, the quadratic-
+extrapolation increment through the last three points r1 (r1 + 1) r2 (d1 -
+r2 d2) / ((r2 + 1) VSCALE) with d1 = v_n - v_{n-1}, d2 = v_{n-1} - v_{n-2},
+zeros.
 """
 from __future__ import annotations
 
@@ -24,6 +28,7 @@ from . import engine as E
 F_IN = 16
 VSCALE = 0.05
 RATIO_MAX = 4.0
+QUIET = 1e-4        # V: node activity at which the correction is halved
 
 
 def lib():
@@ -168,18 +173,27 @@ def features(v3: np.ndarray, v2: np.ndarray, v1: np.ndarray, h_next: float, h_n:
     X[:, 5] = r1 * d1 / VSCALE
     X[:, 6:12] = stat
     X[:, 12] = 1.0
+    X[:, 13] = r1 * (r1 + 1.0) * r2 * (d1 - r2 * (v2 - v1)) / ((r2 + 1.0) * VSCALE)
     vlin = v3 + r1 * d1
     return X, vlin.astype(np.float64)
 
 
+def gate(v3: np.ndarray, v2: np.ndarray, v1: np.ndarray) -> np.ndarray:
+    """Weight of the network's correction at each node: a / (a + QUIET)
+    with a = |v_n - v_{n-1}| + |v_{n-1} - v_{n-2}| (the transient kernel
+    applies the same, predict.cuh)."""
+    a = np.abs(v3 - v2) + np.abs(v2 - v1)
+    return a / (a + QUIET)
+
+
 def trajectory_samples(t: np.ndarray, V: np.ndarray, stat: np.ndarray,
-                       stride: int = 1) -> list[tuple[np.ndarray, np.ndarray]]:
-    """(X, y) training pairs from accepted points t[k], V[k, node]:
-    y = (v_{n+1} - v_lin) / VSCALE."""
+                       stride: int = 1) -> list[tuple[np.ndarray, np.ndarray, np.ndarray]]:
+    """(X, y, g) training triples from accepted points t[k], V[k, node]:
+    y = (v_{n+1} - v_lin) / VSCALE, g the correction's gate."""
     out = []
     for n in range(3, len(t) - 1, stride):
         h_next, h_n, h_prev = t[n + 1] - t[n], t[n] - t[n - 1], t[n - 1] - t[n - 2]
         X, vlin = features(V[n], V[n - 1], V[n - 2], h_next, h_n, h_prev, stat)
         y = ((V[n + 1] - vlin) / VSCALE).astype(np.float32)
-        out.append((X, y))
+        out.append((X, y, gate(V[n], V[n - 1], V[n - 2]).astype(np.float32)))
     return out

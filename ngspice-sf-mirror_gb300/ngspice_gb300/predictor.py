@@ -79,15 +79,21 @@ def train(data: list[dict], steps: int = 400, lr: float = 2e-3, seed: int = 0,
     net = gnn.Net(ptr, idx)
     net.set_params(params if params is not None else init_params(seed))
     n = len(ptr) - 1
-    w = np.ones(n, np.float32)
     losses = []
     for it in range(steps):
+        # the correction is applied as g * pred: minimise sum (g p - y)^2 =
+        # sum g^2 (p - y / g)^2, i.e. weights g^2 and targets y / g
         X = np.zeros((n, gnn.F_IN), np.float32)
         y = np.zeros(n, np.float32)
+        w = np.zeros(n, np.float32)
         for d, o in zip(data, offs):
-            Xs, ys = d["samples"][rng.integers(len(d["samples"]))]
+            Xs, ys, gs = d["samples"][rng.integers(len(d["samples"]))]
             X[o:o + len(ys)] = Xs
-            y[o:o + len(ys)] = ys
+            safe = np.maximum(gs, 1e-6)
+            y[o:o + len(ys)] = np.where(gs > 1e-6, ys / safe, 0.0)
+            w[o:o + len(ys)] = gs * gs
+        if not w.sum() > 0:
+            continue
         cur_lr = lr * (0.1 ** (it / max(steps, 1)))
         loss, _ = net.train_step(X, y, w, cur_lr)
         losses.append(loss)

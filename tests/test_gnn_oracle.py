@@ -78,8 +78,9 @@ def test_features_and_targets():
     stat = np.ones((3, 6), np.float32)
     samples = gnn.trajectory_samples(t, V, stat)
     assert len(samples) == 2
-    X, y = samples[0]
+    X, y, g = samples[0]
     assert X.shape == (3, gnn.F_IN)
+    assert np.all(g > 0.99)                  # 0.1 V steps: fully active
     assert np.allclose(X[:, 3], 1.5)         # r1 = 1.5p / 1p
     # v_lin = v3 + 1.5 * 0.1 = 0.45; v_next = 0.4 -> y = -0.05 / VSCALE
     assert np.allclose(y, (0.4 - 0.45) / gnn.VSCALE, atol=1e-6)

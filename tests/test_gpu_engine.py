@@ -228,16 +228,14 @@ def test_batch_equals_single_runs(E):
         np.testing.assert_array_equal(va, vb)
 
 
-def test_persistent_batch_retires_and_refills(E, monkeypatch):
-    """Monte Carlo instances of uneven size (device mismatch) on a grid of
-    two persistent blocks: each block takes the next circuit from the queue
-    when it finishes one; every circuit's result is bit-identical to its
-    run alone."""
+def test_uneven_monte_carlo_batch_equals_single_runs(E):
+    """Monte Carlo instances of uneven size (device mismatch) in one launch,
+    largest first: every circuit's result is bit-identical to its run
+    alone."""
     from ngspice_gb300 import netlists
     texts = [netlists.random_logic(n_transistors=n, seed=40 + i, tstop="30p", mismatch=True)
              for i, n in enumerate((60, 220, 40, 150, 90))]
     alone = [run_one(E, t) for t in texts]
-    monkeypatch.setenv("NGSF_BATCH_BLOCKS", "2")
     batch = [E.Circuit(t) for t in texts]
     E.run(batch, max_steps=1_000_000)
     for a, b in zip(alone, batch):
