@@ -3,7 +3,7 @@
 Workloads: c1 (default) one 10,000-transistor BSIM4 random-logic netlist,
 the plain drop-in at scale, over the first 500 ps of its transient; c2
 1024 Monte Carlo instances of uneven size (100-3000 transistors, device
-mismatch) in one launch, first 200 ps; c0 the 32-stage MOS1 inverter chain,
+mismatch) in one launch, first 100 ps; c0 the 32-stage MOS1 inverter chain,
 1216 instances, full 20 ns.
 
 Engine arm (default): the GPU transient engine runs `.tran` on the step's
@@ -53,7 +53,7 @@ BYTES_BSIM4 = 2296
 BYTES_DIO = 748
 
 DEFAULT_INSTANCES = {"c0": 1216, "c1": 1, "c2": 1024}
-DEFAULT_WINDOW = {"c0": "20n", "c1": "500p", "c2": "200p"}
+DEFAULT_WINDOW = {"c0": "20n", "c1": "500p", "c2": "100p"}
 
 
 def c2_sizes(instances: int) -> list[int]:

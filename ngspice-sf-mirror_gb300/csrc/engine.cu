@@ -839,26 +839,26 @@ __device__ int bsim4_load_one(const ngsf_ckt_t &C, const Ctl &s, const Iter &it,
 /* ---------------------------------------------------------------- */
 #define NGSF_WIDE_SPIN_LIMIT (1LL << 26)   /* polls: a few seconds */
 
-/* grid barriers this block has passed in the current launch */
-__shared__ unsigned long long g_barGen;
+/* grid (and refactor-group) barriers this block has passed in the launch */
+__shared__ unsigned long long g_barGen, g_fbarGen;
 
-/* Barrier over the nb blocks of a wide launch (every block calls the same
- * sequence of barriers); with nb == 1 a block barrier.  Arrivals count up
- * in one 64-bit word; the block that completes generation g publishes g in
- * a second word, which the others poll (so the polls do not contend with
- * the arrivals).  The wait is bounded and gives up at once after any
- * block's wait ran out (err). */
-__device__ void grid_sync(const ngsf_ckt_t &C, int nb)
+/* Barrier over nb blocks of a wide launch (every member calls the same
+ * sequence of barriers on the same words); with nb == 1 a block barrier.
+ * Arrivals count up in one 64-bit word; the block that completes
+ * generation g publishes g in a second word, which the others poll (so the
+ * polls do not contend with the arrivals).  The wait is bounded and gives
+ * up at once after any block's wait ran out (err). */
+__device__ void bar_sync(const ngsf_ckt_t &C, int nb, unsigned long long *arrive,
+                         unsigned long long *done, unsigned long long &passed)
 {
     __syncthreads();
     if (nb <= 1)
         return;
     if (threadIdx.x == 0) {
-        ngsf_wide_t *w = C.wide;
-        const unsigned long long g = g_barGen + 1;
-        cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> bar(w->bar);
-        cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> gen(w->gen);
-        cuda::atomic_ref<int, cuda::thread_scope_device> err(w->err);
+        const unsigned long long g = passed + 1;
+        cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> bar(*arrive);
+        cuda::atomic_ref<unsigned long long, cuda::thread_scope_device> gen(*done);
+        cuda::atomic_ref<int, cuda::thread_scope_device> err(C.wide->err);
         __threadfence();
         const unsigned long long old = bar.fetch_add(1ull, cuda::memory_order_acq_rel);
         if (old + 1 == g * (unsigned long long)nb) {
@@ -873,9 +873,18 @@ __device__ void grid_sync(const ngsf_ckt_t &C, int nb)
             }
         }
         __threadfence();
-        g_barGen = g;
+        passed = g;
     }
     __syncthreads();
+}
+
+__device__ void grid_sync(const ngsf_ckt_t &C, int nb)
+{
+    if (nb <= 1) {
+        __syncthreads();
+        return;
+    }
+    bar_sync(C, nb, &C.wide->bar, &C.wide->gen, g_barGen);
 }
 
 /* block 0: publish the control words and a command (thread 0 only) */
@@ -1135,57 +1144,86 @@ __device__ int rl_level_block(const ngsf_ckt_t &C, int l)
     return bad;
 }
 
-__device__ int lu_factor_rl(const ngsf_ckt_t &C, Ctl &s, int b, int nb)
+/* The solve's copy of the factor values in term order (threads t of T). */
+__device__ void solve_pack(const ngsf_ckt_t &C, int t, int T)
 {
-    const int t = b * blockDim.x + threadIdx.x, T = nb * blockDim.x;
-    for (int q = t; q < C.nlu; q += T)
-        C.lux[q] = 0.0;
-    grid_sync(C, nb);
-    for (int p = t; p < C.nnz; p += T)
-        C.lux[C.a_lupos[p]] = C.ax[p];
-    grid_sync(C, nb);
-    if (s.diagGmin != 0.0) {
-        /* LoadGmin: gmin on every structural diagonal (klusmp.c:587-589) */
-        for (int j = t; j < C.n; j += T)
-            if (C.a_diag[j] >= 0)
-                C.lux[C.a_lupos[C.a_diag[j]]] += s.diagGmin;
-        grid_sync(C, nb);
-    }
+    for (int q = t; q < C.nlterm; q += T)
+        C.lval[q] = C.lux[C.lr_pos[q]];
+    for (int q = t; q < C.nuterm; q += T)
+        C.uval[q] = C.lux[C.ur_pos[q]];
+}
+
+/* blocks of a wide launch that take part in the refactorization: enough
+ * threads for the widest levels, few enough for a cheap barrier */
+#define NGSF_RL_BLOCKS 48
+
+__device__ int lu_factor_rl(const ngsf_ckt_t &C, Ctl &s, int b, int nbAll)
+{
     int bad = 0;
-    const int L = C.rl_levels;
-    if (nb <= 1) {
-        for (int l = 0; l < L; l++)
+    if (nbAll <= 1) {
+        for (int q = threadIdx.x; q < C.nlu; q += blockDim.x)
+            C.lux[q] = 0.0;
+        __syncthreads();
+        for (int p = threadIdx.x; p < C.nnz; p += blockDim.x)
+            C.lux[C.a_lupos[p]] = C.ax[p];
+        __syncthreads();
+        if (s.diagGmin != 0.0) {
+            /* LoadGmin: gmin on every structural diagonal (klusmp.c:587-589) */
+            for (int j = threadIdx.x; j < C.n; j += blockDim.x)
+                if (C.a_diag[j] >= 0)
+                    C.lux[C.a_lupos[C.a_diag[j]]] += s.diagGmin;
+            __syncthreads();
+        }
+        for (int l = 0; l < C.rl_levels; l++)
             bad |= rl_level_block(C, l);
+        solve_pack(C, threadIdx.x, blockDim.x);
         return block_or(s, bad);
     }
-    bool small = rl_phase_work(C, 0) <= NGSF_RL_SMALL;
-    for (int p = 0; p <= L; p++) {
-        const bool nextSmall = p < L && rl_phase_work(C, p + 1) <= NGSF_RL_SMALL;
-        if (small) {
-            if (b == 0) {
-                bad |= rl_phase(C, p, threadIdx.x, blockDim.x);
-                __syncthreads();
-            }
-            if (!nextSmall)
-                grid_sync(C, nb);
-        } else {
-            bad |= rl_phase(C, p, t, T);
-            grid_sync(C, nb);
+    const int nb = min(nbAll, NGSF_RL_BLOCKS);
+    if (b < nb) {
+        ngsf_wide_t *w = C.wide;
+        auto gsync = [&]() { bar_sync(C, nb, &w->fbar, &w->fgen, g_fbarGen); };
+        const int t = b * blockDim.x + threadIdx.x, T = nb * blockDim.x;
+        for (int q = t; q < C.nlu; q += T)
+            C.lux[q] = 0.0;
+        gsync();
+        for (int p = t; p < C.nnz; p += T)
+            C.lux[C.a_lupos[p]] = C.ax[p];
+        gsync();
+        if (s.diagGmin != 0.0) {
+            for (int j = t; j < C.n; j += T)
+                if (C.a_diag[j] >= 0)
+                    C.lux[C.a_lupos[C.a_diag[j]]] += s.diagGmin;
+            gsync();
         }
-        small = nextSmall;
+        const int L = C.rl_levels;
+        bool small = rl_phase_work(C, 0) <= NGSF_RL_SMALL;
+        for (int p = 0; p <= L; p++) {
+            const bool nextSmall = p < L && rl_phase_work(C, p + 1) <= NGSF_RL_SMALL;
+            if (small) {
+                if (b == 0) {
+                    bad |= rl_phase(C, p, threadIdx.x, blockDim.x);
+                    __syncthreads();
+                }
+                if (!nextSmall)
+                    gsync();
+            } else {
+                bad |= rl_phase(C, p, t, T);
+                gsync();
+            }
+            small = nextSmall;
+        }
+        solve_pack(C, t, T);
     }
     bad = block_or(s, bad);
-    if (nb > 1) {
-        if (threadIdx.x == 0 && bad)
-            atomicOr(&C.wide->bad, 1);
-        grid_sync(C, nb);
-        __shared__ int allbad;
-        if (threadIdx.x == 0)
-            allbad = *(volatile int *)&C.wide->bad;
-        __syncthreads();
-        bad = allbad;
-    }
-    return bad;
+    if (threadIdx.x == 0 && bad)
+        atomicOr(&C.wide->bad, 1);
+    grid_sync(C, nbAll);
+    __shared__ int allbad;
+    if (threadIdx.x == 0)
+        allbad = *(volatile int *)&C.wide->bad;
+    __syncthreads();
+    return allbad;
 }
 
 __device__ int lu_factor(const ngsf_ckt_t &C, Ctl &s)
@@ -1233,6 +1271,7 @@ __device__ int lu_factor(const ngsf_ckt_t &C, Ctl &s)
         }
         __syncthreads();
     }
+    solve_pack(C, threadIdx.x, blockDim.x);
     return block_or(s, bad);
 }
 
@@ -1257,23 +1296,25 @@ __device__ void lu_solve(const ngsf_ckt_t &C, Ctl &s, double *rhs)
     __syncthreads();
     /* rows of up to 32 terms: one thread, terms in order; longer rows
      * (listed per level in fh/bh): a warp, lane-strided partial sums and a
-     * fixed butterfly */
+     * fixed butterfly.  Row descriptors and values in term order keep the
+     * chain of dependent loads per row short. */
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int4 *fd = (const int4 *)C.fdesc, *bd = (const int4 *)C.bdesc;
     for (int l = 0; l < C.nflevels; l++) {
         for (int r = C.fl_ptr[l] + threadIdx.x; r < C.fl_ptr[l + 1]; r += blockDim.x) {
-            int k = C.fl_row[r];
-            if (C.lr_ptr[k + 1] - C.lr_ptr[k] > 32)
+            const int4 d = fd[r];
+            if (d.z - d.y > 32)
                 continue;
-            double acc = w[k];
-            for (int q = C.lr_ptr[k]; q < C.lr_ptr[k + 1]; q++)
-                acc -= C.lux[C.lr_pos[q]] * w[C.lr_col[q]];
-            w[k] = acc;
+            double acc = w[d.x];
+            for (int q = d.y; q < d.z; q++)
+                acc -= C.lval[q] * w[C.lr_col[q]];
+            w[d.x] = acc;
         }
         for (int h = C.fh_ptr[l] + warp; h < C.fh_ptr[l + 1]; h += NGSF_WARPS) {
             int k = C.fh_row[h];
             double acc = 0.0;
             for (int q = C.lr_ptr[k] + lane; q < C.lr_ptr[k + 1]; q += 32)
-                acc += C.lux[C.lr_pos[q]] * w[C.lr_col[q]];
+                acc += C.lval[q] * w[C.lr_col[q]];
             for (int o = 16; o > 0; o >>= 1)
                 acc += __shfl_xor_sync(0xffffffffu, acc, o);
             if (lane == 0)
@@ -1283,19 +1324,20 @@ __device__ void lu_solve(const ngsf_ckt_t &C, Ctl &s, double *rhs)
     }
     for (int l = 0; l < C.nblevels; l++) {
         for (int r = C.bl_ptr[l] + threadIdx.x; r < C.bl_ptr[l + 1]; r += blockDim.x) {
-            int k = C.bl_row[r];
-            if (C.ur_ptr[k + 1] - C.ur_ptr[k] > 32)
+            const int4 d = bd[r];
+            if (d.z - d.y > 32)
                 continue;
-            double acc = w[k];
-            for (int q = C.ur_ptr[k]; q < C.ur_ptr[k + 1]; q++)
-                acc -= C.lux[C.ur_pos[q]] * w[C.ur_col[q]];
-            w[k] = acc / C.lux[C.cdiag[k]];
+            const double piv = C.lux[C.cdiag[d.x]];
+            double acc = w[d.x];
+            for (int q = d.y; q < d.z; q++)
+                acc -= C.uval[q] * w[C.ur_col[q]];
+            w[d.x] = acc / piv;
         }
         for (int h = C.bh_ptr[l] + warp; h < C.bh_ptr[l + 1]; h += NGSF_WARPS) {
             int k = C.bh_row[h];
             double acc = 0.0;
             for (int q = C.ur_ptr[k] + lane; q < C.ur_ptr[k + 1]; q += 32)
-                acc += C.lux[C.ur_pos[q]] * w[C.ur_col[q]];
+                acc += C.uval[q] * w[C.ur_col[q]];
             for (int o = 16; o > 0; o >>= 1)
                 acc += __shfl_xor_sync(0xffffffffu, acc, o);
             if (lane == 0)
@@ -2219,7 +2261,7 @@ tran_wide_kernel(const ngsf_ckt_t *ckt, int runMode, long long maxSteps, int sol
     __shared__ Ctl s;
     __shared__ __align__(16) ngsf_ckt_t Cs;
     if (threadIdx.x == 0)
-        g_barGen = 0;
+        g_barGen = g_fbarGen = 0;
     {
         const unsigned long long *src = (const unsigned long long *)ckt;
         unsigned long long *dst = (unsigned long long *)&Cs;

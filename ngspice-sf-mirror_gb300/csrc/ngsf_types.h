@@ -168,6 +168,7 @@ typedef struct {
     int bad;              /* OR of the blocks' pivot checks (factor command) */
     unsigned long long bar;  /* grid barrier: arrivals since the launch */
     unsigned long long gen;  /* grid barrier: generations completed (last arriver) */
+    unsigned long long fbar, fgen;  /* the same for the refactorization's block group */
     unsigned long long ctl[NGSF_WIDE_CTL_BYTES / 8];  /* block 0's control words */
 } ngsf_wide_t;
 
@@ -250,6 +251,12 @@ typedef struct {
     const int *bl_ptr, *bl_row;   /* backward levels */
     int nflevels, nblevels;
     const int *lr_ptr, *lr_col, *lr_pos;  /* L rows: (k, lux pos) for m<k */
+    /* the solve's view, refreshed after each refactorization: per row in
+     * level order {row, first term, end, 0} (fdesc forward, bdesc backward)
+     * and the L/U values in term order (lval[q] = lux[lr_pos[q]]) */
+    const int *fdesc, *bdesc;
+    double *lval, *uval;
+    int nlterm, nuterm;
     const int *ur_ptr, *ur_col, *ur_pos;  /* U rows: (m, lux pos) for m>k */
     const int *fh_ptr, *fh_row;   /* per forward level: rows reduced by a warp */
     const int *bh_ptr, *bh_row;   /* per backward level: rows reduced by a warp */

@@ -18,6 +18,8 @@
 #include <cuda_runtime.h>
 
 #include <chrono>
+#include <thread>
+#include <atomic>
 #include <cstdlib>
 #include <algorithm>
 #include <cmath>
@@ -501,6 +503,19 @@ void DeviceCircuit::upload_lu(const Image &img)
            o_lr_pos = puti(img.lr_pos), o_ur_ptr = puti(img.ur_ptr), o_ur_col = puti(img.ur_col),
            o_ur_pos = puti(img.ur_pos), o_fh_ptr = puti(img.fh_ptr),
            o_fh_row = puti(img.fh_row), o_bh_ptr = puti(img.bh_ptr), o_bh_row = puti(img.bh_row);
+    auto descs = [&](const std::vector<int> &rows, const std::vector<int> &ptr) {
+        std::vector<int> d(rows.size() * 4, 0);
+        for (size_t r = 0; r < rows.size(); r++) {
+            d[4 * r] = rows[r];
+            d[4 * r + 1] = ptr[rows[r]];
+            d[4 * r + 2] = ptr[rows[r] + 1];
+        }
+        return d;
+    };
+    const std::vector<int> fdesc = descs(img.fl_row, img.lr_ptr), bdesc = descs(img.bl_row, img.ur_ptr);
+    size_t o_fdesc = puti(fdesc), o_bdesc = puti(bdesc);
+    size_t o_lval = put(nullptr, std::max<size_t>(1, img.lr_col.size()) * sizeof(double));
+    size_t o_uval = put(nullptr, std::max<size_t>(1, img.ur_col.size()) * sizeof(double));
     /* the right-looking schedule is used for large matrices (its two
      * barriers per level beat a column's dependency chain); small ones keep
      * the left-looking order.  NGSF_LU=rl / ll overrides. */
@@ -554,6 +569,12 @@ void DeviceCircuit::upload_lu(const Image &img)
     h.ur_ptr = I(o_ur_ptr);
     h.ur_col = I(o_ur_col);
     h.ur_pos = I(o_ur_pos);
+    h.fdesc = I(o_fdesc);
+    h.bdesc = I(o_bdesc);
+    h.lval = (double *)(b + o_lval);
+    h.uval = (double *)(b + o_uval);
+    h.nlterm = (int)img.lr_col.size();
+    h.nuterm = (int)img.ur_col.size();
     h.fh_ptr = I(o_fh_ptr);
     h.fh_row = I(o_fh_row);
     h.bh_ptr = I(o_bh_ptr);
@@ -747,7 +768,8 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
                 if (err)
                     throw std::runtime_error("wide launch: a block hand-over wait ran out");
             }
-            std::vector<Prepared *> next;
+            std::vector<Prepared *> next, replan;
+            std::vector<std::vector<double>> axs;
             for (auto *c : pending) {
                 c->dev->read_results(c->ires, c->fres);
                 if (c->ires[NGSF_R_STATUS] == NGSF_NEED_REORDER) {
@@ -758,17 +780,42 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
                         for (int j = 0; j < c->img.n; j++)
                             if (c->img.a_diag[j] >= 0)
                                 ax[c->img.a_diag[j]] += dg;
-                    std::string err;
-                    if (!plan_lu(c->img.n, c->img.a_cp, c->img.a_ri, ax, c->img.opt.pivrel,
-                                 c->img.opt.pivtol, c->img, err)) {
-                        c->ires[NGSF_R_STATUS] = NGSF_E_SINGULAR;
-                        continue;
-                    }
-                    c->dev->upload_lu(c->img);
-                    next.push_back(c);
+                    replan.push_back(c);
+                    axs.push_back(std::move(ax));
                 } else {
                     c->dev->read_points(c->ires[NGSF_R_NPOINTS], c->points);
                 }
+            }
+            /* new pivots for every paused circuit, on all host cores (each
+             * plan only reads its own matrix and writes its own image) */
+            std::vector<char> ok(replan.size(), 0);
+            {
+                std::atomic<size_t> cursor{0};
+                auto work = [&]() {
+                    for (size_t i; (i = cursor.fetch_add(1)) < replan.size();) {
+                        Prepared *c = replan[i];
+                        std::string err;
+                        ok[i] = plan_lu(c->img.n, c->img.a_cp, c->img.a_ri, axs[i],
+                                        c->img.opt.pivrel, c->img.opt.pivtol, c->img, err);
+                    }
+                };
+                unsigned nt = std::min<unsigned>(std::max(1u, std::thread::hardware_concurrency()),
+                                                 (unsigned)std::max<size_t>(1, replan.size()));
+                std::vector<std::thread> pool;
+                for (unsigned k = 1; k < nt; k++)
+                    pool.emplace_back(work);
+                work();
+                for (auto &th : pool)
+                    th.join();
+            }
+            for (size_t i = 0; i < replan.size(); i++) {
+                Prepared *c = replan[i];
+                if (!ok[i]) {
+                    c->ires[NGSF_R_STATUS] = NGSF_E_SINGULAR;
+                    continue;
+                }
+                c->dev->upload_lu(c->img);
+                next.push_back(c);
             }
             pending.swap(next);
             mode = 1;   /* RUN_RESUME */
