@@ -90,6 +90,11 @@ def workload_texts(name: str, tstop: str | None, instances: int) -> tuple[list[s
     raise SystemExit(f"unknown workload {name}")
 
 
+def progress(msg: str) -> None:
+    """One progress line on stderr (the JSON result line alone goes to stdout)."""
+    print(f"[bench {time.strftime('%H:%M:%S')}] {msg}", file=sys.stderr, flush=True)
+
+
 def bytes_per_iteration(w: dict) -> int:
     n, nnz, nlu = w["n"], w["nnz"], w["nlu"]
     return (BYTES_BSIM4 * w["bsim4"] + BYTES_MOS1 * w["mos1"] + BYTES_DIO * w["dio"]
@@ -248,10 +253,20 @@ def engine_arm(args, texts, wdesc, rank, world) -> dict | None:
     # output, c2: the first gate output); every unknown for the single c1
     probes = {"c0": ["n32"], "c1": None, "c2": ["y0"]}[args.workload]
     outcap = 8192 if args.workload == "c1" else 1024
+    if args.workload == "c2":
+        # Monte Carlo batch: instances stop after their first accepted step
+        # until no instance still pauses for new pivots (operating point,
+        # MODEINITTRAN), then run their time loops in one launch
+        os.environ.setdefault("NGSF_HOLD", "1")
+    tb = time.perf_counter()
     circuits = [E.Circuit(t, probes=probes, outcap=outcap) for t in texts]
     wls = [c.workload() for c in circuits]
-    for _ in range(args.warmup):
-        E.run(circuits)
+    progress(f"compiled and uploaded {len(circuits)} circuits in {time.perf_counter() - tb:.1f} s")
+    for k in range(args.warmup):
+        tw = time.perf_counter()
+        sec = E.run(circuits)
+        progress(f"warm-up {k}: {sec:.3f} s device, {time.perf_counter() - tw:.1f} s wall,"
+                 f" {E.last_launches()} launches")
     clocks = Clocks()
     dev_times, accepted, launches, moved = [], 0, 0, 0
     iters_of = [0] * len(circuits)
@@ -260,6 +275,7 @@ def engine_arm(args, texts, wdesc, rank, world) -> dict | None:
         sec = E.run(circuits)
         dev_times.append(sec)
         launches += E.last_launches()
+        progress(f"step {len(dev_times) - 1}: {sec:.3f} s device, {E.last_launches()} launches")
         for i, c in enumerate(circuits):
             r = c.results()
             if r[E.R_STATUS] != 0:
@@ -297,6 +313,7 @@ def engine_arm(args, texts, wdesc, rank, world) -> dict | None:
             h2d += c.device_bytes()
         del cs
     e2e_time = time.perf_counter() - t0
+    progress(f"end-to-end pass: {e2e_time:.1f} s wall")
     e2e = {"value": world * e2e_acc / e2e_time, "unit": UNIT,
            "h2d_bytes_per_step": h2d // e2e_steps, "d2h_bytes_per_step": d2h // e2e_steps,
            "includes": "netlist compile, symbolic analysis, upload, run, read-back"}

@@ -1553,7 +1553,7 @@ __device__ int src_accept(const ngsf_ckt_t &C, Ctl &s, const ngsf_src_t &K)
 /* ---------------------------------------------------------------- */
 /* NIiter                                                            */
 /* ---------------------------------------------------------------- */
-enum { PH_OP = 1, PH_NEXTTIME = 2, PH_STEP = 3, PH_STEP_NIITER = 4 };
+enum { PH_OP = 1, PH_NEXTTIME = 2, PH_STEP = 3, PH_STEP_NIITER = 4, PH_HELD = 5 };
 
 __device__ void capture(const ngsf_ckt_t &C, Ctl &s, const Iter &it)
 {
@@ -1612,6 +1612,7 @@ __device__ int ni_iter(const ngsf_ckt_t &C, Ctl &s, int maxIter, bool resume)
             bool want = (s.mode & NGSF_MODEINITJCT) ||
                         ((s.mode & NGSF_MODEINITTRAN) && iterno == 1) || s.shouldReorder;
             if (want) {
+                __syncthreads();   /* every warp has read shouldReorder */
                 if (threadIdx.x == 0) {
                     s.savedIter = iterno;
                     s.savedNoncon = noncon;
@@ -1824,6 +1825,7 @@ __device__ int op_run(const ngsf_ckt_t &C, Ctl &s, bool resume)
                 op_save(C, s);
             if (action == 2)
                 op_restore(C, s);
+            __syncthreads();   /* every warp has read gmin, factor, itersBefore */
             if (threadIdx.x == 0) {
                 if (r == 0)
                     s.mode = contmode;
@@ -1963,6 +1965,7 @@ __device__ int op_run(const ngsf_ckt_t &C, Ctl &s, bool resume)
                     op_restore(C, s);
                 }
             }
+            __syncthreads();   /* every warp has read srcFact and convFact */
             if (threadIdx.x == 0) {
                 s.mode = contmode;
                 if (r == 0) {
@@ -2002,7 +2005,13 @@ __device__ int op_run(const ngsf_ckt_t &C, Ctl &s, bool resume)
 /* ---------------------------------------------------------------- */
 /* DCtran, as a resumable state machine                              */
 /* ---------------------------------------------------------------- */
-__device__ int dc_tran(const ngsf_ckt_t &C, Ctl &s, long long maxSteps, bool resume)
+/* With hold set, a circuit stops (NGSF_HELD) once its first transient step
+ * is accepted -- after the operating point and the re-pivots that the
+ * reference asks for at MODEINITJCT, MODEINITFIX and MODEINITTRAN -- and a
+ * held circuit stays held; the host releases the batch once no circuit
+ * still waits for new pivots, so those early pauses cost short launches
+ * instead of one long launch each. */
+__device__ int dc_tran(const ngsf_ckt_t &C, Ctl &s, long long maxSteps, bool resume, bool hold)
 {
     const ngsf_opts_t &o = C.opt;
     const int maxOrder = o.maxord;
@@ -2048,7 +2057,11 @@ __device__ int dc_tran(const ngsf_ckt_t &C, Ctl &s, long long maxSteps, bool res
     }
 
     for (;;) {
-        if (s.phase == PH_NEXTTIME) {
+        if (s.phase == PH_HELD) {
+            if (hold)
+                return NGSF_HELD;
+            resume = false;
+        } else if (s.phase == PH_NEXTTIME) {
             /* nextTime: CKTaccept, clear passed breakpoint, dump, finish test */
             if (threadIdx.x == 0) {
                 int e = src_accept(C, s, C.vsrc);
@@ -2069,7 +2082,17 @@ __device__ int dc_tran(const ngsf_ckt_t &C, Ctl &s, long long maxSteps, bool res
                 return NGSF_OK;
             if (s.steps + 1 > maxSteps)
                 return NGSF_E_WATCHDOG;
+            if (hold && s.accepted == 2) {
+                __syncthreads();   /* every warp has read accepted */
+                if (threadIdx.x == 0)
+                    s.phase = PH_HELD;
+                __syncthreads();
+                return NGSF_HELD;
+            }
+        }
+        if (s.phase == PH_NEXTTIME || s.phase == PH_HELD) {
             /* resume: */
+            __syncthreads();   /* every warp has read time, steps and the phase */
             if (threadIdx.x == 0) {
                 s.steps++;
                 double *b = C.breaks;
@@ -2102,6 +2125,7 @@ __device__ int dc_tran(const ngsf_ckt_t &C, Ctl &s, long long maxSteps, bool res
             __syncthreads();
         }
         if (s.phase == PH_STEP) {
+            __syncthreads();   /* every warp has read the phase */
             if (threadIdx.x == 0) {
                 s.olddelta = s.delta;
                 s.time += s.delta;
@@ -2124,6 +2148,7 @@ __device__ int dc_tran(const ngsf_ckt_t &C, Ctl &s, long long maxSteps, bool res
             converged != NGSF_E_WATCHDOG) {
             /* Newton from the predictor's guess missed itl4: the same step
              * again from the plain start (INITPRED) */
+            __syncthreads();   /* every warp has read guessUsed */
             if (threadIdx.x == 0) {
                 s.tranIter += s.numIter - s.iters0;
                 s.time -= s.delta;
@@ -2171,6 +2196,7 @@ __device__ int dc_tran(const ngsf_ckt_t &C, Ctl &s, long long maxSteps, bool res
             double newdelta = ckt_trunc(C, s, s.delta);
             if (newdelta > .9 * s.delta) {
                 if (s.order == 1 && maxOrder > 1) {
+                    __syncthreads();   /* every warp has read the order */
                     if (threadIdx.x == 0)
                         s.order = 2;
                     __syncthreads();
@@ -2186,6 +2212,7 @@ __device__ int dc_tran(const ngsf_ckt_t &C, Ctl &s, long long maxSteps, bool res
                 __syncthreads();
                 continue;
             } else {
+                __syncthreads();   /* every warp has compared against delta */
                 if (threadIdx.x == 0) {
                     s.time = s.time - s.delta;
                     s.rejected++;
@@ -2217,6 +2244,7 @@ __device__ int dc_tran(const ngsf_ckt_t &C, Ctl &s, long long maxSteps, bool res
 #define RUN_FRESH 0
 #define RUN_RESUME 1
 #define RUN_PROBE 2
+#define RUN_HOLD 4     /* or-ed into RUN_FRESH / RUN_RESUME: stop after the first step */
 
 __device__ void run_circuit(const ngsf_ckt_t &C, Ctl &s, int runMode, long long maxSteps);
 
@@ -2283,6 +2311,8 @@ tran_wide_kernel(const ngsf_ckt_t *ckt, int runMode, long long maxSteps, int sol
 
 __device__ void run_circuit(const ngsf_ckt_t &C, Ctl &s, int runMode, long long maxSteps)
 {
+    const bool hold = (runMode & RUN_HOLD) != 0;
+    runMode &= ~RUN_HOLD;
     if (runMode == RUN_RESUME) {
         const int *src = (const int *)C.ctlsave;
         int *dst = (int *)&s;
@@ -2344,11 +2374,11 @@ __device__ void run_circuit(const ngsf_ckt_t &C, Ctl &s, int runMode, long long 
         ckt_load(C, s, it);
         status = NGSF_OK;
     } else {
-        status = dc_tran(C, s, maxSteps, runMode == RUN_RESUME);
+        status = dc_tran(C, s, maxSteps, runMode == RUN_RESUME, hold);
     }
     __syncthreads();
-    if (status == NGSF_NEED_REORDER) {
-        if (threadIdx.x == 0)
+    if (status == NGSF_NEED_REORDER || status == NGSF_HELD) {
+        if (threadIdx.x == 0 && status == NGSF_NEED_REORDER)
             s.reorders++;
         __syncthreads();
         int *dst = (int *)C.ctlsave;

@@ -50,6 +50,8 @@ extern "C" {
 #define NGSF_E_BREAKS   120   /* breakpoint table overflow */
 #define NGSF_E_WATCHDOG 121   /* step budget exhausted */
 #define NGSF_NEED_REORDER (-2) /* paused: host must choose new pivots */
+#define NGSF_HELD (-3)        /* paused after the first transient step while
+                                 other circuits of the batch re-pivot */
 
 /* -------- MOS1 (level 1) --------------------------------------------- */
 enum {

@@ -23,6 +23,7 @@
 #include <cstdlib>
 #include <algorithm>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <string>
 #include <vector>
@@ -704,6 +705,15 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
+    /* NGSF_TRACE=1: one line per launch and per re-plan round on stderr */
+    const bool trace = getenv("NGSF_TRACE") && atoi(getenv("NGSF_TRACE")) != 0;
+    /* NGSF_HOLD=1: batched circuits stop after their first accepted
+     * transient step while any circuit of the batch still pauses for new
+     * pivots, so the early re-pivots (operating point, MODEINITTRAN) of
+     * the whole batch cost short launches; the batch then runs its time
+     * loops together.  Off by default. */
+    const bool holdPolicy = getenv("NGSF_HOLD") && atoi(getenv("NGSF_HOLD")) != 0;
+    bool holdNow = holdPolicy;
     try {
         while (!pending.empty()) {
             if (nl > 256 + 8 * (int)cs.size())
@@ -738,14 +748,17 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
                 const int solveCap = ngsf_solve_smem_bytes(maxn);
                 const int gnnBytes = ngsf_pred_smem_bytes(learned);
                 cudaEventRecord(e0, 0);
-                ck(ngsf_launch_tran(d, d_order, (int)descs.size(), mode, maxSteps, solveCap,
-                                   gnnBytes, 0), "launch(tran)");
+                ck(ngsf_launch_tran(d, d_order, (int)descs.size(), mode | (holdNow ? 4 : 0),
+                                   maxSteps, solveCap, gnnBytes, 0), "launch(tran)");
                 cudaEventRecord(e1, 0);
                 ck(cudaEventSynchronize(e1), "tran");
                 float ms = 0;
                 cudaEventElapsedTime(&ms, e0, e1);
                 total += ms * 1e-3;
                 nl++;
+                if (trace)
+                    fprintf(stderr, "ngsf: launch %d: %zu circuits, largest n %d,%s %.3f ms\n",
+                            nl, descs.size(), maxn, holdNow ? " hold," : "", ms);
             }
             for (auto *c : wide) {
                 /* a fresh hand-over block per launch: command numbers start at 0 */
@@ -762,6 +775,9 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
                 cudaEventElapsedTime(&ms, e0, e1);
                 total += ms * 1e-3;
                 nl++;
+                if (trace)
+                    fprintf(stderr, "ngsf: launch %d: wide, n %d, %d blocks, %.3f ms\n", nl,
+                            c->img.n, nb, ms);
                 int err = 0;
                 ck(cudaMemcpy(&err, &c->dev->desc().wide->err, sizeof(int),
                               cudaMemcpyDeviceToHost), "cudaMemcpy(wide err)");
@@ -782,6 +798,8 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
                                 ax[c->img.a_diag[j]] += dg;
                     replan.push_back(c);
                     axs.push_back(std::move(ax));
+                } else if (c->ires[NGSF_R_STATUS] == NGSF_HELD) {
+                    next.push_back(c);
                 } else {
                     c->dev->read_points(c->ires[NGSF_R_NPOINTS], c->points);
                 }
@@ -789,6 +807,7 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
             /* new pivots for every paused circuit, on all host cores (each
              * plan only reads its own matrix and writes its own image) */
             std::vector<char> ok(replan.size(), 0);
+            const auto tp = std::chrono::steady_clock::now();
             {
                 std::atomic<size_t> cursor{0};
                 auto work = [&]() {
@@ -808,6 +827,9 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
                 for (auto &th : pool)
                     th.join();
             }
+            if (trace && !replan.empty())
+                fprintf(stderr, "ngsf: re-plan of %zu circuits: %.3f s host\n", replan.size(),
+                        std::chrono::duration<double>(std::chrono::steady_clock::now() - tp).count());
             for (size_t i = 0; i < replan.size(); i++) {
                 Prepared *c = replan[i];
                 if (!ok[i]) {
@@ -819,6 +841,7 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
             }
             pending.swap(next);
             mode = 1;   /* RUN_RESUME */
+            holdNow = holdPolicy && !replan.empty();
         }
     } catch (...) {
         cudaEventDestroy(e0);
