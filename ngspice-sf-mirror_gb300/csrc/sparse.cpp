@@ -229,7 +229,14 @@ bool plan_lu(int n, const std::vector<int> &cp, const std::vector<int> &ri,
     img.upd_src.clear();
     img.kseg.push_back(0);
     double flops = 0;
+    /* where[row]: LU position of (row, k) in the current column k, or -1 */
+    std::vector<int> where(n, -1);
     for (int k = 0; k < n; k++) {
+        for (size_t t = 0; t < ucol[k].size(); t++)
+            where[ucol[k][t]] = img.cbeg[k] + (int)t;
+        where[k] = img.cdiag[k];
+        for (size_t t = 0; t < lcol[k].size(); t++)
+            where[lcol[k][t]] = img.cdiag[k] + 1 + (int)t;
         int lv = 0;
         for (size_t t = 0; t < ucol[k].size(); t++) {
             int m = ucol[k][t];
@@ -238,7 +245,7 @@ bool plan_lu(int n, const std::vector<int> &cp, const std::vector<int> &ri,
             img.kpos.push_back(img.cbeg[k] + (int)t);
             for (size_t s = 0; s < lcol[m].size(); s++) {
                 int i = lcol[m][s];
-                int dst = posIn(k, i);
+                int dst = where[i];
                 if (dst < 0) {
                     err = "internal: fill closure violated";
                     return false;
@@ -249,6 +256,11 @@ bool plan_lu(int n, const std::vector<int> &cp, const std::vector<int> &ri,
             flops += (double)lcol[m].size();
             img.kseg.push_back((int)img.upd_dst.size());
         }
+        for (int r : ucol[k])
+            where[r] = -1;
+        where[k] = -1;
+        for (int r : lcol[k])
+            where[r] = -1;
         flops += (double)lcol[k].size();
         level[k] = lv;
         img.kptr[k + 1] = (int)img.kdep.size();
@@ -379,36 +391,82 @@ bool plan_lu(int n, const std::vector<int> &cp, const std::vector<int> &ri,
         img.ud_l.clear();
         img.ud_u.clear();
         img.ud_p.clear();
+        /* the products are those of the left-looking lists, regrouped */
+        img.ud_l.reserve(img.upd_dst.size());
+        img.ud_u.reserve(img.upd_dst.size());
+        img.ud_p.reserve(img.upd_dst.size());
+        /* products of one level grouped by destination in ascending
+         * position, each group in generation order (a stable counting
+         * sort; cnt and start are indexed by LU position) */
+        std::vector<int> cnt(img.nlu, 0), start(img.nlu, 0), touched;
+        std::vector<int> colrow(img.nlu);   /* row of each LU position */
+        for (int j = 0; j < n; j++) {
+            for (size_t t = 0; t < ucol[j].size(); t++)
+                colrow[img.cbeg[j] + t] = ucol[j][t];
+            colrow[img.cdiag[j]] = j;
+            for (size_t t = 0; t < lcol[j].size(); t++)
+                colrow[img.cdiag[j] + 1 + t] = lcol[j][t];
+        }
+        std::vector<std::array<int, 4>> prod;   /* dst, lpos, upos, pivot */
         for (int l = 0; l < nl; l++) {
-            std::map<int, std::vector<std::array<int, 3>>> dst;
+            prod.clear();
+            touched.clear();
             for (int k : piv[l]) {
                 img.rl_col.push_back(k);
                 for (size_t s2 = 0; s2 < lcol[k].size(); s2++) {
                     img.sc_pos.push_back(img.cdiag[k] + 1 + (int)s2);
                     img.sc_piv.push_back(img.cdiag[k]);
                 }
-                for (size_t s2 = 0; s2 < lcol[k].size(); s2++) {
-                    int i = lcol[k][s2];
-                    int lpos = img.cdiag[k] + 1 + (int)s2;
-                    for (auto &e : urow[k]) {
-                        int j = e.first, upos = e.second;
-                        int d = posIn(j, i);
-                        if (d < 0) {
+                /* per U entry (k, j): the rows of L column k located in
+                 * column j by one merge walk (column j's rows are sorted
+                 * by position); within a destination the products keep
+                 * the pivot order, whatever the walk order */
+                const std::vector<int> &lk = lcol[k];
+                for (auto &e : urow[k]) {
+                    const int j = e.first, upos = e.second;
+                    int q = img.cbeg[j];
+                    const int qe = img.cend[j];
+                    for (size_t s2 = 0; s2 < lk.size(); s2++) {
+                        const int i = lk[s2];
+                        while (q < qe && colrow[q] < i)
+                            q++;
+                        if (q == qe || colrow[q] != i) {
                             err = "internal: fill closure violated (right-looking)";
                             return false;
                         }
-                        dst[d].push_back({lpos, upos, img.cdiag[k]});
+                        const int d = q;
+                        if (cnt[d]++ == 0)
+                            touched.push_back(d);
+                        prod.push_back({d, img.cdiag[k] + 1 + (int)s2, upos, img.cdiag[k]});
                     }
                 }
             }
-            for (auto &de : dst) {
-                img.ud_dst.push_back(de.first);
-                for (auto &c : de.second) {
-                    img.ud_l.push_back(c[0]);
-                    img.ud_u.push_back(c[1]);
-                    img.ud_p.push_back(c[2]);
-                }
-                img.ud_cptr.push_back((int)img.ud_l.size());
+            if (touched.size() * 16 > (size_t)img.nlu) {
+                /* a dense level: scanning the counts is cheaper than a sort */
+                touched.clear();
+                for (int d = 0; d < img.nlu; d++)
+                    if (cnt[d])
+                        touched.push_back(d);
+            } else {
+                std::sort(touched.begin(), touched.end());
+            }
+            const int base = (int)img.ud_l.size();
+            int off = base;
+            for (int d : touched) {
+                start[d] = off;
+                off += cnt[d];
+                img.ud_dst.push_back(d);
+                img.ud_cptr.push_back(off);
+                cnt[d] = 0;
+            }
+            img.ud_l.resize(off);
+            img.ud_u.resize(off);
+            img.ud_p.resize(off);
+            for (auto &c : prod) {
+                const int at = start[c[0]]++;
+                img.ud_l[at] = c[1];
+                img.ud_u[at] = c[2];
+                img.ud_p[at] = c[3];
             }
             img.rl_ptr[l + 1] = (int)img.rl_col.size();
             img.sc_ptr[l + 1] = (int)img.sc_pos.size();
