@@ -258,8 +258,14 @@ def engine_arm(args, texts, wdesc, rank, world) -> dict | None:
         # until no instance still pauses for new pivots (operating point,
         # MODEINITTRAN), then run their time loops in one launch
         os.environ.setdefault("NGSF_HOLD", "1")
+    def open_all():
+        # a batch opens through ngsf_open_many (parsing on all host cores)
+        if len(texts) > 1:
+            return E.open_many(texts, probes=probes, outcap=outcap)
+        return [E.Circuit(texts[0], probes=probes, outcap=outcap)]
+
     tb = time.perf_counter()
-    circuits = [E.Circuit(t, probes=probes, outcap=outcap) for t in texts]
+    circuits = open_all()
     wls = [c.workload() for c in circuits]
     progress(f"compiled and uploaded {len(circuits)} circuits in {time.perf_counter() - tb:.1f} s")
     for k in range(args.warmup):
@@ -304,7 +310,7 @@ def engine_arm(args, texts, wdesc, rank, world) -> dict | None:
     h2d = d2h = 0
     e2e_acc = 0
     for _ in range(e2e_steps):
-        cs = [E.Circuit(t, probes=probes, outcap=outcap) for t in texts]
+        cs = open_all()
         E.run(cs)
         for c in cs:
             tt, vv = c.points()

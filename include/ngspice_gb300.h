@@ -9,6 +9,8 @@
  *                 cktsetup.c:34), CKTtemp, SMPpreOrder + SMPreorder
  *                 (src/maths/KLU/klusmp.c:1256, :753) on the first stamped
  *                 matrix
+ *   ngsf_open_many  ngsf_open for a batch (Monte Carlo instances, corners):
+ *                 the parse/setup half on all host cores
  *   ngsf_run      CKTdoJob -> DCtran (src/spicelib/analysis/dctran.c:67) with
  *                 CKTload/DEVload, SMPluFac, SMPsolve, NIconvTest, CKTtrunc on
  *                 the GPU; many circuits in one launch
@@ -37,6 +39,13 @@ typedef struct ngsf_handle ngsf_handle;
  * stamped system is captured (0 = none).  Returns NULL on error. */
 NGSF_API ngsf_handle *ngsf_open(const char *netlist, const char *probes, int outcap,
                                 int capmax);
+/* ngsf_open for count netlists with the same probes, outcap and capmax:
+ * parsing and setup run on all host cores, allocation and upload on the
+ * calling thread's device.  On success out[0..count-1] receive the handles
+ * and 0 is returned; on any failure nothing is returned in out, -1 is
+ * returned and ngsf_last_error() names the failing netlist. */
+NGSF_API int ngsf_open_many(const char *const *netlists, int count, const char *probes,
+                            int outcap, int capmax, ngsf_handle **out);
 /* Host-only compile (parse, setup, temperature; no device, no pivoting):
  * ngsf_info / ngsf_eq_name / ngsf_pattern work on the result, ngsf_run
  * refuses it.  Replaces the reference's INPpas1/INPpas2 + CKTsetup +

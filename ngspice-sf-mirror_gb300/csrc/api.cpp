@@ -9,6 +9,8 @@
  * SendInitData has described the vectors, output vectors are looked up by
  * name with ngGet_Vec_Info, errors return 1.
  */
+#include <algorithm>
+#include <atomic>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -51,6 +53,22 @@ int fail(const std::string &msg, int code = -1)
     g_err = msg;
     return code;
 }
+
+/* probe names: whitespace separated, matched in lower case */
+std::vector<std::string> probe_names(const char *probes)
+{
+    std::vector<std::string> pr;
+    if (probes) {
+        std::istringstream is(probes);
+        std::string t;
+        while (is >> t) {
+            for (auto &ch : t)
+                ch = (char)tolower((unsigned char)ch);
+            pr.push_back(t);
+        }
+    }
+    return pr;
+}
 }  // namespace
 
 extern "C" {
@@ -61,21 +79,56 @@ NGSF_API ngsf_handle *ngsf_open(const char *netlist, const char *probes, int out
 {
     try {
         auto h = std::make_unique<ngsf_handle>();
-        std::vector<std::string> pr;
-        if (probes) {
-            std::istringstream is(probes);
-            std::string t;
-            while (is >> t) {
-                for (auto &ch : t)
-                    ch = (char)tolower((unsigned char)ch);
-                pr.push_back(t);
-            }
-        }
-        prepare(h->p, netlist ? netlist : "", pr, outcap > 0 ? outcap : 1, capmax > 0 ? capmax : 0);
+        prepare(h->p, netlist ? netlist : "", probe_names(probes), outcap > 0 ? outcap : 1,
+                capmax > 0 ? capmax : 0);
         return h.release();
     } catch (const std::exception &e) {
         g_err = e.what();
         return nullptr;
+    }
+}
+
+NGSF_API int ngsf_open_many(const char *const *netlists, int count, const char *probes,
+                            int outcap, int capmax, ngsf_handle **out)
+{
+    if (count < 0 || (count > 0 && (!netlists || !out)))
+        return fail("ngsf_open_many: bad arguments");
+    try {
+        const std::vector<std::string> pr = probe_names(probes);
+        std::vector<std::unique_ptr<ngsf_handle>> hs(count);
+        std::vector<std::string> errs(count);
+        /* parse and compile on all host cores; each netlist only touches
+         * its own circuit */
+        std::atomic<int> cursor{0};
+        auto work = [&]() {
+            for (int i; (i = cursor.fetch_add(1)) < count;) {
+                try {
+                    hs[i] = std::make_unique<ngsf_handle>();
+                    prepare_host(hs[i]->p, netlists[i] ? netlists[i] : "", pr);
+                } catch (const std::exception &e) {
+                    errs[i] = e.what();
+                }
+            }
+        };
+        unsigned nt = std::min<unsigned>(std::max(1u, std::thread::hardware_concurrency()),
+                                         (unsigned)std::max(1, count));
+        std::vector<std::thread> pool;
+        for (unsigned k = 1; k < nt; k++)
+            pool.emplace_back(work);
+        work();
+        for (auto &th : pool)
+            th.join();
+        for (int i = 0; i < count; i++)
+            if (!errs[i].empty())
+                return fail("netlist " + std::to_string(i) + ": " + errs[i]);
+        /* device allocation and upload on the calling thread (its device) */
+        for (int i = 0; i < count; i++)
+            prepare_device(hs[i]->p, outcap > 0 ? outcap : 1, capmax > 0 ? capmax : 0);
+        for (int i = 0; i < count; i++)
+            out[i] = hs[i].release();
+        return 0;
+    } catch (const std::exception &e) {
+        return fail(e.what());
     }
 }
 

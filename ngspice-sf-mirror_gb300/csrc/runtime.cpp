@@ -645,6 +645,12 @@ void DeviceCircuit::read_capture(int ncap, std::vector<double> &ax, std::vector<
 void prepare(Prepared &p, const std::string &netlist, const std::vector<std::string> &probeNames,
              int outcap, int capmax)
 {
+    prepare_host(p, netlist, probeNames);
+    prepare_device(p, outcap, capmax);
+}
+
+void prepare_host(Prepared &p, const std::string &netlist, const std::vector<std::string> &probeNames)
+{
     p.ckt = parse_netlist(netlist);
     compile(*p.ckt, p.img);
     std::vector<int> probes;
@@ -663,8 +669,12 @@ void prepare(Prepared &p, const std::string &netlist, const std::vector<std::str
         }
     }
     p.probes = probes;
+}
+
+void prepare_device(Prepared &p, int outcap, int capmax)
+{
     p.dev = std::make_unique<DeviceCircuit>();
-    p.dev->upload(p.img, probes, outcap, capmax);
+    p.dev->upload(p.img, p.probes, outcap, capmax);
     /* large circuits may take the whole device (a wide launch) when they
      * run in a small batch; NGSF_WIDE=0/1 overrides the size rule */
     int transistors = p.img.nb4 + p.img.nmos1;

@@ -62,6 +62,11 @@ struct Prepared {
 
 void prepare(Prepared &p, const std::string &netlist, const std::vector<std::string> &probes,
              int outcap, int capmax);
+/* the two halves of prepare(): parse, compile and resolve the probes (host
+ * only, safe to run for different circuits on different threads), then
+ * allocate and upload on the calling thread's device */
+void prepare_host(Prepared &p, const std::string &netlist, const std::vector<std::string> &probes);
+void prepare_device(Prepared &p, int outcap, int capmax);
 int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *seconds,
               int *launches = nullptr);
 

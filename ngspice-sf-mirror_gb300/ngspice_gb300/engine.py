@@ -23,7 +23,7 @@ F_COUNT = 3
 
 # C-ABI symbols declared in include/*.h
 EXPORTS = [
-    "ngsf_open", "ngsf_compile", "ngsf_close", "ngsf_last_error", "ngsf_info",
+    "ngsf_open", "ngsf_open_many", "ngsf_compile", "ngsf_close", "ngsf_last_error", "ngsf_info",
     "ngsf_eq_name", "ngsf_pattern", "ngsf_probes", "ngsf_run", "ngsf_results",
     "ngsf_points", "ngsf_capture", "ngsf_lu_flops", "ngsf_device_bytes",
     "ngsf_last_launches", "ngsf_workload", "ngsf_stamp_initial_static",
@@ -55,6 +55,7 @@ def lib(path: str | None = None) -> C.CDLL:
     vp, ip, dp, cp = C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_double), C.c_char_p
     L.ngsf_open.restype = vp
     L.ngsf_open.argtypes = [cp, cp, C.c_int, C.c_int]
+    L.ngsf_open_many.argtypes = [C.POINTER(cp), C.c_int, cp, C.c_int, C.c_int, C.POINTER(vp)]
     L.ngsf_compile.restype = vp
     L.ngsf_compile.argtypes = [cp]
     L.ngsf_close.argtypes = [vp]
@@ -102,6 +103,16 @@ class Circuit:
             h = L.ngsf_open(netlist.encode(), pr, int(outcap), int(capmax))
         if not h:
             raise EngineError(last_error())
+        self._adopt(h, host_only)
+
+    @classmethod
+    def _from_handle(cls, h) -> "Circuit":
+        c = cls.__new__(cls)
+        c._adopt(h, False)
+        return c
+
+    def _adopt(self, h, host_only: bool):
+        L = lib()
         self._h = C.c_void_p(h)
         n, nnz, ns, nlu = C.c_int(), C.c_int(), C.c_int(), C.c_int()
         L.ngsf_info(self._h, C.byref(n), C.byref(nnz), C.byref(ns), C.byref(nlu))
@@ -210,6 +221,21 @@ class Circuit:
 
 def last_launches() -> int:
     return int(lib().ngsf_last_launches())
+
+
+def open_many(netlists: list[str], probes: list[str] | None = None, outcap: int = 200000,
+              capmax: int = 0) -> list[Circuit]:
+    """Circuit(...) for a batch of netlists with the same probes (ngsf_open_many:
+    parsing and setup on all host cores)."""
+    n = len(netlists)
+    if n == 0:
+        return []
+    texts = (C.c_char_p * n)(*[t.encode() for t in netlists])
+    out = (C.c_void_p * n)()
+    pr = " ".join(probes).encode() if probes else None
+    if lib().ngsf_open_many(texts, n, pr, int(outcap), int(capmax), out):
+        raise EngineError(last_error())
+    return [Circuit._from_handle(out[i]) for i in range(n)]
 
 
 def run(circuits: list[Circuit], max_steps: int = 0) -> float:

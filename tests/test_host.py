@@ -55,3 +55,16 @@ def test_run_refuses_host_only_circuit(built_lib):
     c = E.Circuit(str(g["netlist"]), host_only=True)
     with pytest.raises(E.EngineError, match="without a device"):
         E.run([c])
+
+
+def test_open_many_reports_the_failing_netlist(built_lib):
+    """ngsf_open_many parses every netlist on the host cores before any
+    device work, so a bad netlist fails the whole batch on the CPU, naming
+    its index; an empty batch is empty."""
+    from ngspice_gb300 import engine as E, netlists
+    good = netlists.random_logic(n_transistors=40, seed=3, tstop="5p")
+    with pytest.raises(E.EngineError, match="netlist 1: short card"):
+        E.open_many([good, "* broken\nR1 a\n.tran 1p 2p\n.end\n", good])
+    with pytest.raises(E.EngineError, match="netlist 0: unsupported element"):
+        E.open_many(["t\nq1 c b e qmod\n.tran 1n 10n\n.end\n"])
+    assert E.open_many([]) == []
