@@ -19,7 +19,6 @@
 #include <array>
 #include <map>
 #include <set>
-#include <unordered_map>
 
 #include "circuit.h"
 #include "sparse.h"
@@ -31,13 +30,29 @@ bool plan_lu(int n, const std::vector<int> &cp, const std::vector<int> &ri,
              Image &img, std::string &err)
 {
     /* ---------------- numeric Markowitz elimination ------------------ */
-    std::vector<std::unordered_map<int, double>> rows(n);
+    /* active rows: (column, value) in no particular order; active columns:
+     * row sets in ascending order (the candidate search visits rows in
+     * that order) */
+    std::vector<std::vector<std::pair<int, double>>> rows(n);
     std::vector<std::set<int>> cols(n);
     for (int j = 0; j < n; j++)
         for (int p = cp[j]; p < cp[j + 1]; p++) {
-            rows[ri[p]][j] += ax[p];
+            /* columns arrive in ascending order: a repeated (row, column)
+             * can only be the row's last entry */
+            auto &r = rows[ri[p]];
+            if (!r.empty() && r.back().first == j)
+                r.back().second += ax[p];
+            else
+                r.push_back({j, 0.0 + ax[p]});
             cols[j].insert(ri[p]);
         }
+    auto val = [&](int i, int j) -> double {
+        for (auto &e : rows[i])
+            if (e.first == j)
+                return e.second;
+        return 0.0;
+    };
+    std::vector<int> colpos(n, -1);   /* scatter of one row: column -> index */
     std::set<std::pair<int, int>> colq;  /* (count, col) */
     for (int j = 0; j < n; j++)
         colq.insert({(int)cols[j].size(), j});
@@ -64,11 +79,11 @@ bool plan_lu(int n, const std::vector<int> &cp, const std::vector<int> &ri,
             singles.erase(singles.begin());
             if (rowDone[i] || rows[i].size() != 1)
                 continue;
-            int q = rows[i].begin()->first;
-            double a = std::fabs(rows[i].begin()->second);
+            int q = rows[i][0].first;
+            double a = std::fabs(rows[i][0].second);
             double cmax = 0;
             for (int r : cols[q])
-                cmax = std::max(cmax, std::fabs(rows[r][q]));
+                cmax = std::max(cmax, std::fabs(val(r, q)));
             if (cmax > 0 && a >= pivrel * cmax && a > pivtol) {
                 bestCost = 0;
                 bp = i;
@@ -86,12 +101,12 @@ bool plan_lu(int n, const std::vector<int> &cp, const std::vector<int> &ri,
                 continue;
             double cmax = 0;
             for (int i : cols[q])
-                cmax = std::max(cmax, std::fabs(rows[i][q]));
+                cmax = std::max(cmax, std::fabs(val(i, q)));
             if (!(cmax > 0))
                 continue;
             bool found = false;
             for (int i : cols[q]) {
-                double a = std::fabs(rows[i][q]);
+                double a = std::fabs(val(i, q));
                 if (a < pivrel * cmax || a <= pivtol)
                     continue;
                 long cost = (long)((int)rows[i].size() - 1) * (long)(cc - 1);
@@ -115,7 +130,7 @@ bool plan_lu(int n, const std::vector<int> &cp, const std::vector<int> &ri,
         int p = bp, q = bq;
         prow[k] = p;
         pcol[k] = q;
-        double d = rows[p][q];
+        double d = val(p, q);
         /* U row k: columns of row p except q */
         for (auto &e : rows[p])
             if (e.first != q)
@@ -125,23 +140,29 @@ bool plan_lu(int n, const std::vector<int> &cp, const std::vector<int> &ri,
         for (int i : cols[q])
             if (i != p)
                 Lrows[k].push_back(i);
-        /* Schur update */
+        /* Schur update: row i's entries scattered by column, so each
+         * entry of the pivot row finds its partner in one lookup */
         for (int i : Lrows[k]) {
-            double l = rows[i][q] / d;
+            auto &r = rows[i];
+            const size_t len0 = r.size();
+            for (size_t t = 0; t < len0; t++)
+                colpos[r[t].first] = (int)t;
+            double l = r[colpos[q]].second / d;
             for (auto &e : rows[p]) {
                 int j = e.first;
                 if (j == q)
                     continue;
-                auto f = rows[i].find(j);
-                if (f == rows[i].end()) {
-                    rows[i][j] = -l * e.second;
+                if (colpos[j] < 0) {
+                    r.push_back({j, -l * e.second});
                     colq.erase({(int)cols[j].size(), j});
                     cols[j].insert(i);
                     colq.insert({(int)cols[j].size(), j});
                 } else {
-                    f->second -= l * e.second;
+                    r[colpos[j]].second -= l * e.second;
                 }
             }
+            for (size_t t = 0; t < len0; t++)
+                colpos[r[t].first] = -1;
         }
         /* remove pivot row and column from the active matrix */
         for (auto &e : rows[p]) {
@@ -152,8 +173,14 @@ bool plan_lu(int n, const std::vector<int> &cp, const std::vector<int> &ri,
                 colq.insert({(int)cols[j].size(), j});
         }
         for (int i : Lrows[k]) {
-            rows[i].erase(q);
-            if (rows[i].size() == 1)
+            auto &r = rows[i];
+            for (size_t t = 0; t < r.size(); t++)
+                if (r[t].first == q) {
+                    r[t] = r.back();
+                    r.pop_back();
+                    break;
+                }
+            if (r.size() == 1)
                 singles.insert(i);
         }
         colq.erase({(int)cols[q].size(), q});
