@@ -96,8 +96,9 @@ __device__ bool pred_mma(int n, int kt)
                           tc05_smem_desc(sb + q * 256, 128, sbo), idesc, q ? 1u : 0u);
         tc05_commit(bar);
     }
-    const bool ok = tc05_mbar_wait(bar, g_pphase);
-    __syncthreads();
+    /* every thread waits on its own count: the block agrees on the
+     * outcome, so all threads leave the product loops together */
+    const bool ok = __syncthreads_and(tc05_mbar_wait(bar, g_pphase) ? 1 : 0) != 0;
     if (threadIdx.x == 0)
         g_pphase ^= 1u;
     tc05_fence_after();
