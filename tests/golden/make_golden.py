@@ -45,6 +45,9 @@ CASES = {
     "bsim4_logic_s3": (netlists.random_logic(n_transistors=120, seed=3, n_inputs=6,
                                              tstop="1n"), 200),
     "bsim4_chain8": (None, 200),
+    # one Monte Carlo instance: per-device mismatch model cards
+    "bsim4_mc_s5": (netlists.random_logic(n_transistors=120, seed=5, n_inputs=6,
+                                          tstop="600p", mismatch=True), 150),
 }
 
 

@@ -5,9 +5,15 @@
   circuit resumes exactly where it stopped, so every result is
   bit-identical to the run without holding.
 * ngsf_open_many (parsing and setup on all host cores): the same circuits,
-  and the same results, as one ngsf_open per netlist."""
+  and the same results, as one ngsf_open per netlist.
+* One Monte Carlo instance (per-device mismatch model cards) against the
+  reference: the same counts, time points to rounding, waveforms within
+  tolerance."""
 import numpy as np
 import pytest
+
+from conftest import golden
+from tolerances import waveform_violation
 
 pytestmark = pytest.mark.gpu
 
@@ -60,3 +66,17 @@ def test_open_many_equals_single_opens(E):
         np.testing.assert_array_equal(ta, tb)
         np.testing.assert_array_equal(va, vb)
 
+
+
+def test_monte_carlo_instance_matches_reference(E):
+    g = golden("bsim4_mc_s5")
+    c = E.Circuit(str(g["netlist"]))
+    E.run([c], max_steps=1_000_000)
+    r = c.results()
+    ref = g["stats"]
+    assert r[E.R_STATUS] == 0
+    assert (r[E.R_ACCEPTED], r[E.R_REJECTED], r[E.R_TRANITER]) == (ref[3], ref[4], ref[1])
+    t, v = c.points()
+    assert len(t) == len(g["times"])
+    assert np.max(np.abs(t - g["times"])) <= 1e-9 * g["times"][-1]
+    assert waveform_violation(c.names(), g["times"], g["values"], t, v) < 1.0

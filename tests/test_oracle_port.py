@@ -68,6 +68,24 @@ def test_port_bsim4_logic_matches_reference():
                               r["values"][:, idx]) < 0.01
 
 
+def test_port_bsim4_monte_carlo_instance_matches_reference():
+    """One Monte Carlo instance (seed 5, ~120 transistors, per-device
+    mismatch of vth0, toxe and W through one model card per device):
+    identical Newton and step counts, time points equal to rounding,
+    waveforms within 1% of the tolerance."""
+    g = golden("bsim4_mc_s5")
+    r = port.simulate(str(g["netlist"]))
+    st, ref = r["stats"], g["stats"]
+    assert st["status"] == 0
+    assert (st["numIter"], st["tranIter"], st["accepted"], st["rejected"]) == \
+        (ref[0], ref[1], ref[3], ref[4])
+    assert np.max(np.abs(r["times"] - g["times"])) <= 1e-9 * g["times"][-1]
+    names = list(g["names"])
+    idx = [r["names"].index(x) for x in names]
+    assert waveform_violation(names, g["times"], g["values"], r["times"],
+                              r["values"][:, idx]) < 0.01
+
+
 def test_port_bsim4_newton_stamps_match_reference():
     """Per-iteration stamped Jacobian and right-hand side of the first
     200 Newton iterations of the BSIM4 inverter chain (operating point and
