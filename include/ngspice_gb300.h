@@ -183,6 +183,17 @@ NGSF_API int ngsf_node_graph(const ngsf_handle *h, int *nv, int *nedges, int *vn
  * linear extrapolation). */
 NGSF_API int ngsf_set_predictor(ngsf_handle *h, int kind, const float *params);
 
+/* Whether the circuit runs over the whole grid when it is alone or in a
+ * batch of at most four (wide), and with how many blocks. */
+NGSF_API int ngsf_wide_info(const ngsf_handle *h, int *wide, int *blocks);
+/* Shape of the refactorization in a wide launch: the number of blocks that
+ * take part (0 = 48) and the work (updates + divisions) at or below which a
+ * level runs in one block without a grid barrier (0 = 1024).  Every shape
+ * gives the same result; the autotuner (engine.tune_factor_shape) picks
+ * the fastest by timing short runs.  No reference counterpart: it is the
+ * tuning knob of the GPU refactorization that replaces SMPluFac. */
+NGSF_API int ngsf_set_factor_shape(ngsf_handle *h, int blocks, int small_work);
+
 #ifdef __cplusplus
 }
 #endif

@@ -310,6 +310,31 @@ NGSF_API int ngsf_node_graph(const ngsf_handle *h, int *nv, int *nedges, int *vn
     return 0;
 }
 
+NGSF_API int ngsf_wide_info(const ngsf_handle *h, int *wide, int *blocks)
+{
+    if (!h || !h->p.dev)
+        return fail("ngsf_wide_info: null or host-only handle");
+    if (wide)
+        *wide = h->p.wide ? 1 : 0;
+    if (blocks)
+        *blocks = h->p.wide_blocks;
+    return 0;
+}
+
+NGSF_API int ngsf_set_factor_shape(ngsf_handle *h, int blocks, int small_work)
+{
+    if (!h || !h->p.dev)
+        return fail("ngsf_set_factor_shape: null or host-only handle");
+    if (blocks < 0 || small_work < 0)
+        return fail("ngsf_set_factor_shape: negative shape");
+    try {
+        h->p.dev->set_factor_shape(blocks, small_work);
+        return 0;
+    } catch (const std::exception &e) {
+        return fail(e.what());
+    }
+}
+
 NGSF_API int ngsf_set_predictor(ngsf_handle *h, int kind, const float *params)
 {
     if (!h || !h->p.dev)

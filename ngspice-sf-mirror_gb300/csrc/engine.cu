@@ -1179,7 +1179,8 @@ __device__ int lu_factor_rl(const ngsf_ckt_t &C, Ctl &s, int b, int nbAll)
         solve_pack(C, threadIdx.x, blockDim.x);
         return block_or(s, bad);
     }
-    const int nb = min(nbAll, NGSF_RL_BLOCKS);
+    const int nb = min(nbAll, C.rl_blocks > 0 ? C.rl_blocks : NGSF_RL_BLOCKS);
+    const int smallWork = C.rl_small > 0 ? C.rl_small : NGSF_RL_SMALL;
     if (b < nb) {
         ngsf_wide_t *w = C.wide;
         auto gsync = [&]() { bar_sync(C, nb, &w->fbar, &w->fgen, g_fbarGen); };
@@ -1197,9 +1198,9 @@ __device__ int lu_factor_rl(const ngsf_ckt_t &C, Ctl &s, int b, int nbAll)
             gsync();
         }
         const int L = C.rl_levels;
-        bool small = rl_phase_work(C, 0) <= NGSF_RL_SMALL;
+        bool small = rl_phase_work(C, 0) <= smallWork;
         for (int p = 0; p <= L; p++) {
-            const bool nextSmall = p < L && rl_phase_work(C, p + 1) <= NGSF_RL_SMALL;
+            const bool nextSmall = p < L && rl_phase_work(C, p + 1) <= smallWork;
             if (small) {
                 if (b == 0) {
                     bad |= rl_phase(C, p, threadIdx.x, blockDim.x);

@@ -266,6 +266,10 @@ typedef struct {
      * pivot columns, the L entries to divide by their pivot, and the
      * destinations with their lists of (L pos, U pos) products */
     int rl_levels;
+    /* refactorization shape in a wide launch, 0 = built-in default:
+     * blocks that take part, and the phase work at or below which a phase
+     * runs in block 0 alone (the result is the same for every shape) */
+    int rl_blocks, rl_small;
     const int *rl_ptr, *rl_col, *sc_ptr, *sc_pos, *sc_piv;
     const int *ud_ptr, *ud_dst, *ud_cptr, *ud_l, *ud_u, *ud_p;  /* ud_p: pivot pos */
     double *work;         /* [n] solve workspace */

@@ -285,6 +285,15 @@ void DeviceCircuit::upload(const Image &img, const std::vector<int> &probes, int
     capmax_ = capmax;
 }
 
+void DeviceCircuit::set_factor_shape(int blocks, int small)
+{
+    impl->h.rl_blocks = blocks > 0 ? blocks : 0;
+    impl->h.rl_small = small > 0 ? small : 0;
+    if (impl->d_desc)
+        ck(cudaMemcpy(impl->d_desc, &impl->h, sizeof(impl->h), cudaMemcpyHostToDevice),
+           "cudaMemcpy(desc)");
+}
+
 const ngsf_ckt_t &DeviceCircuit::desc() const { return impl->h; }
 ngsf_ckt_t *DeviceCircuit::device_desc() const { return impl->d_desc; }
 size_t DeviceCircuit::bytes() const

@@ -26,6 +26,8 @@ public:
     void read_capture(int ncap, std::vector<double> &ax, std::vector<double> &rhs,
                       std::vector<double> &meta);
     void set_pred(const Image &img, int kind, const float *params);
+    /* refactorization shape of a wide launch (0 = default) */
+    void set_factor_shape(int blocks, int small);
     const ngsf_ckt_t &desc() const;
     ngsf_ckt_t *device_desc() const;
     size_t bytes() const;

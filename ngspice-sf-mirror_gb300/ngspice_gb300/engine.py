@@ -29,7 +29,7 @@ EXPORTS = [
     "ngsf_last_launches", "ngsf_workload", "ngsf_stamp_initial_static",
     "ngsf_gnn_param_count", "ngsf_gnn_create", "ngsf_gnn_destroy", "ngsf_gnn_set_params",
     "ngsf_gnn_get_params", "ngsf_gnn_forward", "ngsf_gnn_train_step", "ngsf_gnn_gemm_test",
-    "ngsf_node_graph", "ngsf_set_predictor",
+    "ngsf_node_graph", "ngsf_set_predictor", "ngsf_wide_info", "ngsf_set_factor_shape",
     "ngSpice_Init", "ngSpice_Init_Sync", "ngSpice_Command", "ngGet_Vec_Info",
     "ngSpice_Circ", "ngSpice_CurPlot", "ngSpice_AllPlots", "ngSpice_AllVecs",
     "ngSpice_running", "ngSpice_SetBkpt", "ngSpice_nospinit", "ngSpice_nospiceinit",
@@ -57,6 +57,8 @@ def lib(path: str | None = None) -> C.CDLL:
     L.ngsf_open.argtypes = [cp, cp, C.c_int, C.c_int]
     L.ngsf_open_many.argtypes = [C.POINTER(cp), C.c_int, cp, C.c_int, C.c_int, C.POINTER(vp)]
     L.ngsf_compile.restype = vp
+    L.ngsf_wide_info.argtypes = [vp, ip, ip]
+    L.ngsf_set_factor_shape.argtypes = [vp, C.c_int, C.c_int]
     L.ngsf_compile.argtypes = [cp]
     L.ngsf_close.argtypes = [vp]
     L.ngsf_last_error.restype = cp
@@ -118,6 +120,19 @@ class Circuit:
         L.ngsf_info(self._h, C.byref(n), C.byref(nnz), C.byref(ns), C.byref(nlu))
         self.n, self.nnz, self.nstates, self.nlu = n.value, nnz.value, ns.value, nlu.value
         self.host_only = host_only
+
+    def wide_info(self) -> tuple[bool, int]:
+        """(runs over the whole grid when alone, blocks of that launch)"""
+        w, b = C.c_int(), C.c_int()
+        if lib().ngsf_wide_info(self._h, C.byref(w), C.byref(b)):
+            raise EngineError(last_error())
+        return bool(w.value), b.value
+
+    def set_factor_shape(self, blocks: int = 0, small_work: int = 0):
+        """Refactorization shape of the wide launch (0 = default); every
+        shape gives the same result."""
+        if lib().ngsf_set_factor_shape(self._h, int(blocks), int(small_work)):
+            raise EngineError(last_error())
 
     def close(self):
         if self._h:
@@ -236,6 +251,36 @@ def open_many(netlists: list[str], probes: list[str] | None = None, outcap: int 
     if lib().ngsf_open_many(texts, n, pr, int(outcap), int(capmax), out):
         raise EngineError(last_error())
     return [Circuit._from_handle(out[i]) for i in range(n)]
+
+
+def tune_factor_shape(circuit: Circuit, blocks=(16, 24, 32, 48, 64, 96, 152),
+                      small_works=(256, 1024, 4096, 16384), max_steps: int = 40,
+                      repeats: int = 2) -> dict:
+    """Autotuner of the wide refactorization over the circuit's level
+    schedule: times short runs (the operating point and max_steps
+    timesteps, device time, best of `repeats`) for each group size at the
+    default small-level threshold, then each threshold at the best group
+    size, and leaves the fastest shape set on the circuit.  Every shape
+    computes the same result, so tuning changes no waveform.  A circuit
+    that does not run wide keeps the default.  Returns the choice and the
+    timings."""
+    wide, nb = circuit.wide_info()
+    if not wide:
+        return {"blocks": 0, "small_work": 0, "timings": {}}
+
+    def time_shape(b: int, sw: int) -> float:
+        circuit.set_factor_shape(b, sw)
+        return min(run([circuit], max_steps=max_steps) for _ in range(repeats))
+
+    timings = {}
+    for b in [b for b in blocks if b <= nb] or [nb]:
+        timings[(b, 0)] = time_shape(b, 0)
+    best_b = min(timings, key=timings.get)[0]
+    for sw in small_works:
+        timings[(best_b, sw)] = time_shape(best_b, sw)
+    best = min(timings, key=timings.get)
+    circuit.set_factor_shape(*best)
+    return {"blocks": best[0], "small_work": best[1], "timings": timings}
 
 
 def run(circuits: list[Circuit], max_steps: int = 0) -> float:

@@ -68,3 +68,12 @@ def test_open_many_reports_the_failing_netlist(built_lib):
     with pytest.raises(E.EngineError, match="netlist 0: unsupported element"):
         E.open_many(["t\nq1 c b e qmod\n.tran 1n 10n\n.end\n"])
     assert E.open_many([]) == []
+
+
+def test_factor_shape_needs_a_device_circuit(built_lib):
+    from ngspice_gb300 import engine as E
+    c = E.Circuit(str(golden("rc_ladder")["netlist"]), host_only=True)
+    with pytest.raises(E.EngineError, match="host-only"):
+        c.set_factor_shape(32, 1024)
+    with pytest.raises(E.EngineError, match="host-only"):
+        c.wide_info()
