@@ -19,6 +19,7 @@
 #include <mutex>
 #include <sstream>
 #include <string>
+#include <system_error>
 #include <thread>
 #include <vector>
 
@@ -113,8 +114,12 @@ NGSF_API int ngsf_open_many(const char *const *netlists, int count, const char *
         unsigned nt = std::min<unsigned>(std::max(1u, std::thread::hardware_concurrency()),
                                          (unsigned)std::max(1, count));
         std::vector<std::thread> pool;
-        for (unsigned k = 1; k < nt; k++)
-            pool.emplace_back(work);
+        try {
+            for (unsigned k = 1; k < nt; k++)
+                pool.emplace_back(work);
+        } catch (const std::system_error &) {
+            /* fewer threads: the calling thread takes the rest */
+        }
         work();
         for (auto &th : pool)
             th.join();

@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include <chrono>
+#include <system_error>
 #include <thread>
 #include <atomic>
 #include <cstdlib>
@@ -840,8 +841,12 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
                 unsigned nt = std::min<unsigned>(std::max(1u, std::thread::hardware_concurrency()),
                                                  (unsigned)std::max<size_t>(1, replan.size()));
                 std::vector<std::thread> pool;
-                for (unsigned k = 1; k < nt; k++)
-                    pool.emplace_back(work);
+                try {
+                    for (unsigned k = 1; k < nt; k++)
+                        pool.emplace_back(work);
+                } catch (const std::system_error &) {
+                    /* fewer threads: the calling thread takes the rest */
+                }
                 work();
                 for (auto &th : pool)
                     th.join();
