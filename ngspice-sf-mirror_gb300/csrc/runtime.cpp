@@ -826,16 +826,21 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
             }
             /* new pivots for every paused circuit, on all host cores (each
              * plan only reads its own matrix and writes its own image) */
-            std::vector<char> ok(replan.size(), 0);
+            std::vector<int> ok(replan.size(), 0);
             const auto tp = std::chrono::steady_clock::now();
             {
                 std::atomic<size_t> cursor{0};
+                /* 1 planned, 0 singular, -1 the planner itself failed */
                 auto work = [&]() {
                     for (size_t i; (i = cursor.fetch_add(1)) < replan.size();) {
                         Prepared *c = replan[i];
                         std::string err;
-                        ok[i] = plan_lu(c->img.n, c->img.a_cp, c->img.a_ri, axs[i],
-                                        c->img.opt.pivrel, c->img.opt.pivtol, c->img, err);
+                        try {
+                            ok[i] = plan_lu(c->img.n, c->img.a_cp, c->img.a_ri, axs[i],
+                                            c->img.opt.pivrel, c->img.opt.pivtol, c->img, err);
+                        } catch (const std::exception &) {
+                            ok[i] = -1;
+                        }
                     }
                 };
                 unsigned nt = std::min<unsigned>(std::max(1u, std::thread::hardware_concurrency()),
@@ -854,6 +859,9 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
             if (trace && !replan.empty())
                 fprintf(stderr, "ngsf: re-plan of %zu circuits: %.3f s host\n", replan.size(),
                         std::chrono::duration<double>(std::chrono::steady_clock::now() - tp).count());
+            for (size_t i = 0; i < replan.size(); i++)
+                if (ok[i] < 0)
+                    throw std::runtime_error("pivot planning failed (out of host memory?)");
             for (size_t i = 0; i < replan.size(); i++) {
                 Prepared *c = replan[i];
                 if (!ok[i]) {
