@@ -125,3 +125,21 @@ def test_number_evaluation_matches_reference_rules():
     assert ev("3mil") == 3 * 25.4 * 10.0 ** -6
     assert ev("-1.5e-3k") == -15 * 10.0 ** (-1 - 3 + 3)
     assert ev("abc") is None
+
+
+def test_port_sparse_planner_is_deterministic_and_pinned():
+    """A 600-transistor Monte Carlo instance (612 unknowns) takes the
+    port's sparse path, i.e. the same host pivot planner the engine uses
+    at every re-pivot.  Two runs are bit-identical, and the Newton, step
+    and re-pivot counts stay pinned: a planner change that alters a pivot
+    choice shows up here."""
+    from ngspice_gb300 import netlists
+    text = netlists.random_logic(n_transistors=600, seed=7, tstop="15p", mismatch=True)
+    a = port.simulate(text)
+    b = port.simulate(text)
+    st = a["stats"]
+    assert len(a["names"]) > 400
+    assert (st["status"], st["numIter"], st["tranIter"], st["accepted"], st["rejected"],
+            st["reorders"]) == (0, 160, 116, 59, 0, 6)
+    np.testing.assert_array_equal(a["times"], b["times"])
+    np.testing.assert_array_equal(a["values"], b["values"])
