@@ -52,15 +52,23 @@ BYTES_SRC = 120
 BYTES_BSIM4 = 2296
 BYTES_DIO = 748
 
-DEFAULT_INSTANCES = {"c0": 1216, "c1": 1, "c2": 1024}
-DEFAULT_WINDOW = {"c0": "20n", "c1": "500p", "c2": "100p"}
+DEFAULT_INSTANCES = {"c0": 1216, "c1": 1, "c2": 1024, "c4": 4096}
+DEFAULT_WINDOW = {"c0": "20n", "c1": "500p", "c2": "2n", "c4": "2n"}
+# transistor-count range of the Monte Carlo instances
+MC_RANGE = {"c2": (100, 3000), "c4": (100, 5000)}
+
+
+def mc_sizes(workload: str, instances: int) -> list[int]:
+    """Transistor counts of the Monte Carlo instances: uniform over the
+    workload's range, seeded."""
+    import random
+    lo, hi = MC_RANGE[workload]
+    rng = random.Random(20240 if workload == "c2" else 40960)
+    return [rng.randint(lo, hi) for _ in range(instances)]
 
 
 def c2_sizes(instances: int) -> list[int]:
-    """Transistor counts of the Monte Carlo instances: U[100, 3000], seeded."""
-    import random
-    rng = random.Random(20240)
-    return [rng.randint(100, 3000) for _ in range(instances)]
+    return mc_sizes("c2", instances)
 
 
 def workload_texts(name: str, tstop: str | None, instances: int) -> tuple[list[str], dict]:
@@ -78,15 +86,18 @@ def workload_texts(name: str, tstop: str | None, instances: int) -> tuple[list[s
             "circuit": "seeded random CMOS logic, 10,000 BSIM4 (level 54) transistors, gate mix"
                        " INV/NAND2/NOR2 40/35/25 %, RC pi nets, 64 PULSE inputs, VDD 1.0 V",
             "tran": f".tran 1p {tstop} (the first {tstop} of the 5n transient)"}
-    if name == "c2":
-        sizes = c2_sizes(instances)
-        texts = [netlists.random_logic(n_transistors=n, seed=i, tstop=tstop, mismatch=True)
+    if name in ("c2", "c4"):
+        sizes = mc_sizes(name, instances)
+        base = 0 if name == "c2" else 100000
+        texts = [netlists.random_logic(n_transistors=n, seed=base + i, tstop=tstop, mismatch=True)
                  for i, n in enumerate(sizes)]
+        full = tstop in ("2n", "2000p")
         return texts, {
             "circuit": f"{instances} Monte Carlo instances of seeded random BSIM4 logic,"
                        f" {min(sizes)}-{max(sizes)} transistors ({sum(sizes)} total), per-device"
                        " mismatch vth0 N(nom, 15 mV), toxe N(nom, 2 %), W N(nom, 3 %)",
-            "tran": f".tran 1p {tstop} (the first {tstop} of the 2n transient)"}
+            "tran": f".tran 1p {tstop}" + ("" if full else f" (the first {tstop} of the 2n transient)"),
+            "sizes": sizes}
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -210,18 +221,26 @@ def cpu_measure(args) -> dict:
                 "sample": f"C1 netlist on 1 core (single-threaded port): accepted steps between the"
                           f" 20p and 50p windows ({a2 - a1} steps in {t2 - t1:.1f} s; operating"
                           f" point excluded)"}
-    texts, _ = workload_texts(args.workload, args.tstop, args.instances)
     if args.workload == "c0":
+        texts, _ = workload_texts(args.workload, args.tstop, args.instances)
         sample = args.cpu_sample or 4 * procs
         batch = [texts[0]] * sample
-    else:
-        sample = args.cpu_sample or 2 * procs
-        step = max(1, len(texts) // sample)
-        batch = texts[::step][:sample]
+        a, dt = cpu_pool(batch, procs)
+        return {"value": a / dt, "cores": procs, "seconds": dt,
+                "sample": f"{len(batch)} of the step's instances across {procs} processes"
+                          f" ({a} accepted steps in {dt:.1f} s)"}
+    # Monte Carlo: instances spread over the sorted sizes, each over the
+    # first cpu_window of its transient (operating point included), one
+    # process per core; throughput = accepted steps / makespan
+    win = args.cpu_window
+    texts, tdesc = workload_texts(args.workload, win, args.instances)
+    sample = args.cpu_sample or 2 * procs
+    batch = [texts[i] for i in plain_sample(texts, tdesc.get("sizes"), sample)]
     a, dt = cpu_pool(batch, procs)
     return {"value": a / dt, "cores": procs, "seconds": dt,
-            "sample": f"{len(batch)} of the step's instances across {procs} processes"
-                      f" ({a} accepted steps in {dt:.1f} s)"}
+            "sample": f"{len(batch)} of the step's instances (spread over the sorted sizes),"
+                      f" each over .tran 1p {win} (operating point included), across {procs}"
+                      f" processes ({a} accepted steps in {dt:.1f} s)"}
 
 
 def cpu_arm(args, wdesc) -> dict:
@@ -237,7 +256,7 @@ def cpu_arm(args, wdesc) -> dict:
             "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": 1e3 * statistics.mean(times), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": wdesc,
+            "config": {k: v for k, v in wdesc.items() if not k.startswith("_")},
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": desc + " (oracle restatement, oracle/port)"},
             "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
@@ -247,25 +266,36 @@ def cpu_arm(args, wdesc) -> dict:
 # ---------------------------------------------------------------------------
 # engine arm
 # ---------------------------------------------------------------------------
+def plain_sample(texts: list[str], sizes: list[int] | None, k: int) -> list[int]:
+    """Indices of k instances spread evenly over the sorted sizes (the
+    plain drop-in is timed on them, one circuit per call)."""
+    n = len(texts)
+    k = max(1, min(k, n))
+    order = sorted(range(n), key=lambda i: (sizes[i] if sizes else 0, i))
+    return [order[(2 * j + 1) * n // (2 * k)] for j in range(k)]
+
+
 def engine_arm(args, texts, wdesc, rank, world) -> dict | None:
     from ngspice_gb300 import engine as E
+    mc = args.workload in ("c2", "c4")
     # one observed node per instance for the batches (c0: the chain's
-    # output, c2: the first gate output); every unknown for the single c1
-    probes = {"c0": ["n32"], "c1": None, "c2": ["y0"]}[args.workload]
-    outcap = 8192 if args.workload == "c1" else 1024
-    if args.workload == "c2":
+    # output, c2/c4: the first gate output); every unknown for the single c1
+    probes = {"c0": ["n32"], "c1": None, "c2": ["y0"], "c4": ["y0"]}[args.workload]
+    outcap = 8192 if args.workload == "c1" else (4096 if mc else 1024)
+    if mc:
         # Monte Carlo batch: instances stop after their first accepted step
         # until no instance still pauses for new pivots (operating point,
         # MODEINITTRAN), then run their time loops in one launch
         os.environ.setdefault("NGSF_HOLD", "1")
-    def open_all():
+
+    def open_all(txts):
         # a batch opens through ngsf_open_many (parsing on all host cores)
-        if len(texts) > 1:
-            return E.open_many(texts, probes=probes, outcap=outcap)
-        return [E.Circuit(texts[0], probes=probes, outcap=outcap)]
+        if len(txts) > 1:
+            return E.open_many(txts, probes=probes, outcap=outcap)
+        return [E.Circuit(txts[0], probes=probes, outcap=outcap)]
 
     tb = time.perf_counter()
-    circuits = open_all()
+    circuits = open_all(texts)
     wls = [c.workload() for c in circuits]
     progress(f"compiled and uploaded {len(circuits)} circuits in {time.perf_counter() - tb:.1f} s")
     for k in range(args.warmup):
@@ -274,7 +304,7 @@ def engine_arm(args, texts, wdesc, rank, world) -> dict | None:
         progress(f"warm-up {k}: {sec:.3f} s device, {time.perf_counter() - tw:.1f} s wall,"
                  f" {E.last_launches()} launches")
     clocks = Clocks()
-    dev_times, accepted, launches, moved = [], 0, 0, 0
+    dev_times, accepted, launches, rejected = [], 0, 0, 0
     iters_of = [0] * len(circuits)
     for _ in range(args.steps):
         flush_l2()
@@ -287,6 +317,7 @@ def engine_arm(args, texts, wdesc, rank, world) -> dict | None:
             if r[E.R_STATUS] != 0:
                 raise SystemExit(f"engine status {r[E.R_STATUS]} on instance {i}")
             accepted += int(r[E.R_ACCEPTED])
+            rejected += int(r[E.R_REJECTED])
             iters_of[i] += int(r[E.R_NUMITER])
     clk = clocks.stop()
     iters = sum(iters_of)
@@ -303,26 +334,65 @@ def engine_arm(args, texts, wdesc, rank, world) -> dict | None:
     else:
         accepted_all = accepted
     value = accepted_all / total
+    del circuits
 
     # e2e: host netlist text -> compile/upload -> run -> accepted points on host
-    e2e_steps = 1
     t0 = time.perf_counter()
     h2d = d2h = 0
     e2e_acc = 0
-    for _ in range(e2e_steps):
-        cs = open_all()
-        E.run(cs)
-        for c in cs:
-            tt, vv = c.points()
-            d2h += tt.nbytes + vv.nbytes
-            e2e_acc += int(c.results()[E.R_ACCEPTED])
-            h2d += c.device_bytes()
-        del cs
+    cs = open_all(texts)
+    E.run(cs)
+    for c in cs:
+        tt, vv = c.points()
+        d2h += tt.nbytes + vv.nbytes
+        e2e_acc += int(c.results()[E.R_ACCEPTED])
+        h2d += c.device_bytes()
+    del cs
     e2e_time = time.perf_counter() - t0
     progress(f"end-to-end pass: {e2e_time:.1f} s wall")
     e2e = {"value": world * e2e_acc / e2e_time, "unit": UNIT,
-           "h2d_bytes_per_step": h2d // e2e_steps, "d2h_bytes_per_step": d2h // e2e_steps,
+           "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
            "includes": "netlist compile, symbolic analysis, upload, run, read-back"}
+
+    out_extra = {}
+    if mc and args.plain_sample > 0:
+        # the plain drop-in on a sample of the same instances: one circuit
+        # per call through the same C ABI (a circuit of >= 1024 transistors
+        # alone in a call runs over the whole grid), device time and wall
+        # time from netlist text
+        os.environ["NGSF_HOLD"] = "0"
+        idx = plain_sample(texts, wdesc.get("_sizes"), args.plain_sample)
+        p_acc = p_dev = p_wall = 0.0
+        p_iters = 0
+        for j, i in enumerate(idx):
+            tw = time.perf_counter()
+            c = open_all([texts[i]])[0]
+            sec = E.run([c])
+            c.points()
+            wall = time.perf_counter() - tw
+            r = c.results()
+            if r[E.R_STATUS] != 0:
+                raise SystemExit(f"engine status {r[E.R_STATUS]} on plain instance {i}")
+            if j == 0:
+                # first call pays module warm-up: run it again for the time
+                sec = E.run([c])
+            p_acc += int(r[E.R_ACCEPTED])
+            p_iters += int(r[E.R_NUMITER])
+            p_dev += sec
+            p_wall += wall
+            progress(f"plain instance {i} ({wdesc['_sizes'][i]} transistors): {sec:.3f} s device,"
+                     f" {wall:.1f} s wall, {int(r[E.R_ACCEPTED])} steps")
+            c.close()
+        plain = p_acc / p_dev
+        out_extra["forms"] = {
+            "batched": {"value": value, "e2e": e2e["value"], "instances": len(texts)},
+            "plain_gpu": {"value": plain, "e2e": p_acc / p_wall, "instances": len(idx),
+                          "newton_iterations_per_accepted_step": p_iters / max(p_acc, 1),
+                          "sample": f"{len(idx)} instances spread over the sorted sizes, each"
+                                    " alone in its own call (device time; e2e: wall time from"
+                                    " netlist text)"},
+            "batched_vs_plain": value / plain,
+            "batched_vs_plain_e2e": e2e["value"] / (p_acc / p_wall)}
 
     pk = peaks()
     achieved = moved / total / 1e9
@@ -338,19 +408,85 @@ def engine_arm(args, texts, wdesc, rank, world) -> dict | None:
             "traffic": traffic, "traffic_unit": "bytes per Newton iteration" if traffic else None,
             "peak_source": pk["src"], "kernel": kernel,
             "algorithmic_bytes_per_newton_iteration": moved // max(iters, 1)}
+    cfg = {k: v for k, v in wdesc.items() if not k.startswith("_")}
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": 1e3 * total / args.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-           "data": "synthetic", "config": wdesc, "clocks": clk, "e2e": e2e,
+           "data": "synthetic", "config": cfg, "clocks": clk, "e2e": e2e,
            "gpu_launches": launches, "roofline": roof,
            "newton_iterations_per_s": iters * world / total,
-           "newton_iterations_per_accepted_step": iters / max(accepted, 1)}
+           "newton_iterations_per_accepted_step": iters / max(accepted, 1),
+           "rejected_steps": rejected}
+    out.update(out_extra)
     if rank == 0 and not args.no_cpu_baseline:
         m = cpu_measure(args)
         out["cpu_baseline"] = {"value": m["value"], "unit": UNIT, "cores": m["cores"],
                                "kind": "port", "sample": m["sample"]}
     return out
+
+
+# FP64 operations of one BSIM4 evaluation (default selectors, transient
+# Newton iteration): counted once with ncu over the grid-wide evaluation
+# kernel (sm__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on, fma
+# counted as 2) on the 10,000-transistor netlist, divided by the
+# evaluations; None until measured.
+FLOPS_BSIM4 = None
+
+
+def device_eval(args) -> dict:
+    """Stand-alone timing of the BSIM4 device evaluation over the
+    10,000-transistor netlist's instances (the transient's device function,
+    one instance per grid thread), against the measured FP64 peak."""
+    from ngspice_gb300 import engine as E, netlists
+    text = netlists.random_logic(n_transistors=10000, seed=1, tstop="5p")
+    c = E.Circuit(text, outcap=16)
+    E.run([c])                      # a realistic linearisation point: 5 ps in
+    r = c.results()
+    pt = E.make_point(time=5e-12, delta=1e-13, deltaOld=(1e-13, 1e-13, 1e-13),
+                      ag=(2e13, -2e13), gmin=1e-12, mode=0x1 | 0x100, order=1)
+    reps = args.eval_reps
+    sec = c.eval_bench(pt, 1 << E.DEV_BSIM4, reps=reps)
+    nb4 = c.workload()["bsim4"]
+    evals = reps * nb4 / sec
+    peak = E.fp64_peak()
+    out = {"instances": nb4, "reps": reps, "seconds": sec, "evaluations_per_s": evals,
+           "fp64_peak_measured_flops": peak, "transient_steps_before": int(r[E.R_ACCEPTED])}
+    if FLOPS_BSIM4:
+        out["flops_per_evaluation"] = FLOPS_BSIM4
+        out["fp64_frac"] = evals * FLOPS_BSIM4 / peak
+    c.close()
+    return out
+
+
+def phase_split(args, texts) -> None:
+    """Per-phase clock split of one untimed run of the workload (circuits
+    opened with NGSF_PHASES=1, so the timed runs carry no clock reads)."""
+    from ngspice_gb300 import engine as E
+    os.environ["NGSF_PHASES"] = "1"
+    if args.workload in ("c2", "c4"):
+        os.environ.setdefault("NGSF_HOLD", "1")
+    try:
+        cs = E.open_many(texts, probes=None if args.workload == "c1" else ["vdd"], outcap=16) \
+            if len(texts) > 1 else [E.Circuit(texts[0], outcap=16)]
+        sec = E.run(cs)
+        tot = {}
+        for c in cs:
+            for k, v in c.phase_cycles().items():
+                tot[k] = tot.get(k, 0) + v
+        busy = sum(tot[k] for k in ("load", "gather", "factor", "solve", "conv", "trunc"))
+        split = {k: tot[k] / tot["total"] for k in ("load", "gather", "factor", "solve", "conv",
+                                                     "trunc")}
+        split["rest"] = 1.0 - busy / tot["total"]
+        per_it = {k: tot[k] / max(tot["iterations"], 1) for k in
+                  ("load", "gather", "factor", "solve", "conv")}
+        print(json.dumps({"phases": split, "cycles_per_newton_iteration": per_it,
+                          "block_cycles": tot["total"], "newton_iterations": tot["iterations"],
+                          "device_seconds": sec, "circuits": len(cs)}), file=sys.stderr,
+              flush=True)
+        del cs
+    finally:
+        os.environ.pop("NGSF_PHASES", None)
 
 
 def main():
@@ -359,11 +495,26 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--workload", default="c1", choices=["c0", "c1", "c2"])
+    ap.add_argument("--workload", default="c2", choices=["c0", "c1", "c2", "c4"])
+    ap.add_argument("--plain-sample", type=int, default=8,
+                    help="instances of a Monte Carlo workload timed through the plain drop-in")
     ap.add_argument("--instances", type=int, default=0,
                     help="instances per launch (default: 1216 for c0, 1 for c1, 1024 for c2)")
     ap.add_argument("--cpu-sample", type=int, default=0)
+    ap.add_argument("--cpu-window", default="100p",
+                    help="transient window of each Monte Carlo instance in the CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--phases", action="store_true",
+                    help="one extra untimed run with per-phase SM clock records: prints the"
+                         " split of each circuit block's time (loads, gather, refactor, solves,"
+                         " convergence, truncation error, the rest) as one JSON line on stderr")
+    ap.add_argument("--device-eval", action="store_true",
+                    help="also time the BSIM4 evaluation alone over the 10,000-transistor"
+                         " netlist and the FP64 peak (one JSON line on stderr, and a"
+                         " device_eval key in the result)")
+    ap.add_argument("--eval-reps", type=int, default=20)
+    ap.add_argument("--device-eval-only", action="store_true",
+                    help="print the device_eval JSON line and stop (profiling case)")
     ap.add_argument("--tstop", default=None,
                     help="shorter .tran stop time (small cases for profiling)")
     args = ap.parse_args()
@@ -374,7 +525,7 @@ def main():
     wdesc = {"workload": f"{args.workload.upper()}: {tdesc['circuit']}, {tdesc['tran']},"
                          f" {args.instances} independent instance(s) per launch",
              "instances_per_gpu": args.instances, "l2": "flushed between timed steps",
-             "parallelism": f"replicas x{world}"}
+             "parallelism": f"replicas x{world}", "_sizes": tdesc.get("sizes")}
     if args.impl == "reference":
         if rank != 0:
             return
@@ -386,7 +537,18 @@ def main():
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("nccl")
         dist.barrier()
+    if args.device_eval_only:
+        print(json.dumps({"device_eval": device_eval(args)}))
+        return
+    if args.phases:
+        phase_split(args, texts)
+    dev_eval = None
+    if args.device_eval:
+        dev_eval = device_eval(args)
+        print(json.dumps({"device_eval": dev_eval}), file=sys.stderr, flush=True)
     out = engine_arm(args, texts, wdesc, rank, world)
+    if dev_eval:
+        out["device_eval"] = dev_eval
     if world > 1:
         import torch.distributed as dist
         dist.barrier()

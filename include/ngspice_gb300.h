@@ -194,6 +194,124 @@ NGSF_API int ngsf_wide_info(const ngsf_handle *h, int *wide, int *blocks);
  * tuning knob of the GPU refactorization that replaces SMPluFac. */
 NGSF_API int ngsf_set_factor_shape(ngsf_handle *h, int blocks, int small_work);
 
+/* ---------------------------------------------------------------------- *
+ * Operator surface: the device-plugin and matrix calls of one Newton
+ * iteration, one at a time on an opened circuit's device arrays, outside
+ * ngsf_run.  They replace
+ *   CKTload / DEVload    src/spicelib/analysis/cktload.c:32-180 and the
+ *                        SPICEdev DEVload entries (src/include/ngspice/
+ *                        devdefs.h:50-129), device types in the table
+ *                        order of src/spicelib/devices/dev.c:142-200
+ *   CKTtrunc / DEVtrunc  src/spicelib/analysis/ckttrunc.c:20-57
+ *   NIconvTest           src/maths/ni/niconv.c:21-90
+ *   SMPreorder           src/maths/KLU/klusmp.c:753-806 (smpdefs.h:61-86)
+ *   SMPluFac             src/maths/KLU/klusmp.c:574-624
+ *   SMPsolve             src/maths/KLU/klusmp.c:951-1011
+ * Each call is synchronous (it returns after the device work and the
+ * copies) and leaves the circuit's arrays as the operation left them; a
+ * later ngsf_run starts its transient from scratch.  Matrices are in the
+ * CSC order of ngsf_pattern; right-hand sides and solutions are n+1
+ * doubles with entry 0 the ground.  Not for concurrent use on one circuit.
+ * ---------------------------------------------------------------------- */
+
+/* device types, in the reference's device-table order; bit k of a `types`
+ * mask selects type k */
+enum {
+    NGSF_DEV_BSIM4, NGSF_DEV_CAP, NGSF_DEV_DIO, NGSF_DEV_ISRC, NGSF_DEV_MOS1,
+    NGSF_DEV_RES, NGSF_DEV_VSRC, NGSF_DEV_TYPES
+};
+#define NGSF_DEV_ALL ((1 << NGSF_DEV_TYPES) - 1)
+
+/* One row of the device table: the SPICEdev entries each type has on the
+ * GPU (DEVload always; DEVtrunc for the charge-storing types; DEVaccept
+ * for the sources, whose breakpoints the transient kernel sets). */
+typedef struct {
+    const char *name;       /* DEVpublic.name of the reference */
+    int states;             /* state doubles per instance (DEVinfo numStates) */
+    int stamps;             /* stamp slots per instance */
+    int has_load, has_trunc, has_accept;
+} ngsf_devinfo;
+NGSF_API int ngsf_dev_table(int *count, const ngsf_devinfo **table);
+
+/* The control scalars of a CKTcircuit that a load, a truncation-error
+ * estimate or a factorization reads. */
+typedef struct {
+    double time;            /* CKTtime */
+    double delta;           /* CKTdelta */
+    double deltaOld[3];     /* CKTdeltaOld[0..2] */
+    double ag[2];           /* CKTag[0..1] (NIcomCof) */
+    double gmin;            /* CKTgmin (junction gmin of the devices) */
+    double srcFact;         /* CKTsrcFact (source stepping) */
+    double diagGmin;        /* CKTdiagGmin (added to the diagonal when factoring) */
+    int mode;               /* CKTmode bits */
+    int order;              /* CKTorder */
+} ngsf_point;
+
+/* CKTload at a linearisation point: the device loads of the types in
+ * `types` (NGSF_DEV_ALL: every device, the whole CKTload) evaluated at
+ * rhsOld[n+1] with CKTstates[0..nvec-1] = states[nvec][nstates] and, for
+ * BSIM4, the gate voltage of the last iteration's limiting (BSIM4von,
+ * von[BSIM4 instances in load order]).  Any of rhsOld, states, von may be
+ * NULL to keep the circuit's current values.  Writes the stamped matrix
+ * ax[nnz] and right-hand side rhs[n+1]; *noncon (may be NULL) receives
+ * the devices' non-convergence flag (CKTnoncon != 0).  The load updates
+ * the circuit's state vectors as the reference's does (read them back
+ * with ngsf_ckt_read_states). */
+NGSF_API int ngsf_ckt_load(ngsf_handle *h, const ngsf_point *pt, int types,
+                           const double *rhsOld, const double *states, int nvec,
+                           const double *von, double *ax, double *rhs, int *noncon);
+/* the circuit's state vectors CKTstates[0..nvec-1] -> states[nvec][nstates] */
+NGSF_API int ngsf_ckt_read_states(const ngsf_handle *h, double *states, int nvec);
+/* CKTtrunc: the next time step allowed by the local truncation error of
+ * every charge (capacitors, diodes, BSIM4 qb/qg/qd, MOS1 Meyer charges),
+ * min(2 * pt->delta, CKTterr over all charges), from CKTstates[0..nvec-1]
+ * (order + 2 vectors are read; pt->order 1 or 2, trapezoidal). */
+NGSF_API int ngsf_ckt_trunc(ngsf_handle *h, const ngsf_point *pt, const double *states,
+                            int nvec, double *timestep);
+/* NIconvTest of a new solution rhs against the previous one rhsOld
+ * (node voltages against vntol, branch currents against abstol, both
+ * plus reltol); *noncon = 1 when any unknown has not converged. */
+NGSF_API int ngsf_ni_convtest(ngsf_handle *h, const double *rhs, const double *rhsOld,
+                              int *noncon);
+/* The device matrix values (what the devices' stamp pointers write into
+ * KLU's Ax): set them, or read them back after a load. */
+NGSF_API int ngsf_smp_set_matrix(ngsf_handle *h, const double *ax);
+NGSF_API int ngsf_smp_get_matrix(const ngsf_handle *h, double *ax);
+/* SMPreorder: new pivots from the device matrix (threshold pivoting with
+ * pivrel and pivtol, diag_gmin added to every structural diagonal), then
+ * the device factorization on them.  Returns 0, NGSF_E_SINGULAR (102), or
+ * -1 on an error. */
+NGSF_API int ngsf_smp_reorder(ngsf_handle *h, double pivtol, double pivrel, double diag_gmin);
+/* SMPluFac: refactor the device matrix on the current pivots (diag_gmin
+ * added to the diagonal).  Like klu_refactor it fails only on a zero or
+ * non-finite pivot: NGSF_E_SINGULAR, after which ngsf_smp_reorder picks
+ * new pivots.  -1 when no pivots exist yet. */
+NGSF_API int ngsf_smp_lufac(ngsf_handle *h, double diag_gmin);
+/* SMPsolve: rhs[n+1] <- the solution of the factored system, in place. */
+NGSF_API int ngsf_smp_solve(ngsf_handle *h, double *rhs);
+
+/* Per-phase SM clock cycles of the circuit's last ngsf_run, as its
+ * (first) block saw them: cycles[8] = device loads, stamp gather, LU
+ * refactorization, triangular solves, convergence test, truncation-error
+ * estimate, the whole run, and the Newton iterations counted.  Recorded
+ * only for circuits opened while the environment variable NGSF_PHASES=1
+ * is set (a profiling aid, no reference counterpart: the reference keeps
+ * STATloadTime / STATdecompTime / STATsolveTime in its statistics,
+ * src/include/ngspice/optdefs.h:20-53). */
+NGSF_API int ngsf_phase_cycles(const ngsf_handle *h, long long *cycles);
+
+/* Measurement aids (no reference counterpart).  ngsf_eval_bench times the
+ * device evaluation half of CKTload on its own: every thread of a grid of
+ * `blocks` blocks (0 = one per SM) evaluates the circuit's devices of the
+ * types in `types` (BSIM4, MOS1, diode) one instance at a time, `reps`
+ * times, at the circuit's current linearisation point with the control
+ * scalars of pt; *seconds receives the device time (CUDA events).
+ * ngsf_fp64_peak measures the device's FP64 fused-multiply-add
+ * throughput (flop/s) with independent chains on every SM. */
+NGSF_API int ngsf_eval_bench(ngsf_handle *h, const ngsf_point *pt, int types, int reps,
+                             int blocks, double *seconds);
+NGSF_API int ngsf_fp64_peak(double *flops_per_second);
+
 #ifdef __cplusplus
 }
 #endif

@@ -23,10 +23,15 @@
 #include <thread>
 #include <vector>
 
+#include <cuda_runtime.h>
+
 #include "../../include/ngspice_gb300.h"
 #include "../../include/sharedspice.h"
+#include "bsim4.h"
 #include "circuit.h"
+#include "dio.h"
 #include "runtime.h"
+#include "sparse.h"
 
 using namespace ngsf;
 
@@ -46,6 +51,11 @@ extern "C" const ngsf_ckt_t *ngsf_internal_desc(const ngsf_handle *h)
     return (h && h->p.dev) ? &h->p.dev->desc() : nullptr;
 }
 extern "C" void ngsf_internal_set_error(const char *msg) { g_err = msg ? msg : ""; }
+extern "C" const ngsf_ckt_t *ngsf_internal_ddesc(const ngsf_handle *h)
+{
+    return (h && h->p.dev) ? h->p.dev->device_desc() : nullptr;
+}
+extern "C" int ngsf_internal_lufac(ngsf_handle *h, double diag_gmin);
 
 namespace {
 
@@ -794,3 +804,67 @@ IMPEXP int ngSpice_Reset(void)
 }
 
 }  // extern "C"
+
+/* ------------------------------------------------------------------ */
+/* Operator surface: SMPreorder and the device-type table              */
+/* ------------------------------------------------------------------ */
+extern "C" {
+
+NGSF_API int ngsf_smp_reorder(ngsf_handle *h, double pivtol, double pivrel, double diag_gmin)
+{
+    if (!h || !h->p.dev)
+        return fail("ngsf_smp_reorder: null or host-only handle");
+    try {
+        Prepared &p = h->p;
+        std::vector<double> ax = p.dev->read_ax();
+        /* the factorization sees gmin on every structural diagonal
+         * (LoadGmin, src/maths/KLU/klusmp.c:762-764) */
+        if (diag_gmin != 0.0)
+            for (int j = 0; j < p.img.n; j++)
+                if (p.img.a_diag[j] >= 0)
+                    ax[p.img.a_diag[j]] += diag_gmin;
+        if (!plan_lu(p.img.n, p.img.a_cp, p.img.a_ri, ax, pivrel, pivtol, p.img, g_err))
+            return NGSF_E_SINGULAR;
+        p.dev->upload_lu(p.img);
+    } catch (const std::exception &e) {
+        return fail(std::string("ngsf_smp_reorder: ") + e.what());
+    }
+    return ngsf_internal_lufac(h, diag_gmin);
+}
+
+NGSF_API int ngsf_phase_cycles(const ngsf_handle *h, long long *cycles)
+{
+    const ngsf_ckt_t *d = ngsf_internal_desc(h);
+    if (!d || !cycles)
+        return fail("ngsf_phase_cycles: null handle or buffer");
+    if (!d->prof)
+        return fail("ngsf_phase_cycles: the circuit was opened without NGSF_PHASES=1");
+    cudaError_t e = cudaMemcpy(cycles, d->prof, NGSF_P_COUNT * sizeof(long long),
+                               cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess)
+        return fail(std::string("ngsf_phase_cycles: ") + cudaGetErrorString(e));
+    return 0;
+}
+
+static const ngsf_devinfo g_devtable[NGSF_DEV_TYPES] = {
+    /* name, states/instance, stamp slots/instance, load, trunc, accept */
+    {"BSIM4", B4S_COUNT, B4_NSTAMP, 1, 1, 0},
+    {"Capacitor", 2, 6, 1, 1, 0},
+    {"Diode", DIS_COUNT, DIO_NSTAMP, 1, 1, 0},
+    {"Isource", 0, 2, 1, 0, 1},
+    {"Mos1", M1S_COUNT, M1_NSTAMP, 1, 1, 0},
+    {"Resistor", 0, 4, 1, 0, 0},
+    {"Vsource", 0, 5, 1, 0, 1},
+};
+
+NGSF_API int ngsf_dev_table(int *count, const ngsf_devinfo **table)
+{
+    if (count)
+        *count = NGSF_DEV_TYPES;
+    if (table)
+        *table = g_devtable;
+    return 0;
+}
+
+}  // extern "C"
+

@@ -27,7 +27,9 @@
 #include <cuda_bf16.h>
 #include <mutex>
 #include <string>
+#include <float.h>
 #include <math.h>
+#include <string.h>
 #include <stdint.h>
 
 #include "../../include/ngspice_gb300.h"
@@ -69,6 +71,18 @@ struct Ctl {
     int opPhase, gi, itersBefore;
     double gmin, diagGmin, srcFact, factor, oldGmin, gtarget, startgmin, convFact, raise;
 };
+
+/* Per-phase clock record (C.prof, optional): thread 0 of the circuit's
+ * block adds the SM clock cycles between two block-wide barriers. */
+__device__ __forceinline__ long long prof_t(const ngsf_ckt_t &C)
+{
+    return C.prof ? clock64() : 0;
+}
+__device__ __forceinline__ void prof_add(const ngsf_ckt_t &C, int k, long long t0)
+{
+    if (C.prof && threadIdx.x == 0)
+        C.prof[k] += clock64() - t0;
+}
 
 /* ---------------------------------------------------------------- */
 /* block reductions                                                  */
@@ -974,6 +988,7 @@ __device__ void gather_heavy_combine(const ngsf_ckt_t &C, const Iter &it)
 __device__ int load_phase(const ngsf_ckt_t &C, Ctl &s, const Iter &it, int b, int nb, bool master)
 {
     const int t = b * blockDim.x + threadIdx.x, T = nb * blockDim.x;
+    const long long t0 = master ? prof_t(C) : 0;
     int nc = 0;
     for (int i = t; i < C.bsim4.n; i += T)
         nc |= bsim4_load_one(C, s, it, i);
@@ -989,9 +1004,14 @@ __device__ int load_phase(const ngsf_ckt_t &C, Ctl &s, const Iter &it, int b, in
     if (nb > 1 && threadIdx.x == 0 && nc && !master)
         atomicOr(&C.wide->noncon, 1);
     grid_sync(C, nb);
+    if (master)
+        prof_add(C, NGSF_P_LOAD, t0);
+    const long long t1 = master ? prof_t(C) : 0;
     const int warp = threadIdx.x >> 5;
     gather(C, it, t, T, b * NGSF_WARPS + warp, nb * NGSF_WARPS);
     grid_sync(C, nb);
+    if (master)
+        prof_add(C, NGSF_P_GATHER, t1);
     return nc;
 }
 
@@ -1061,11 +1081,19 @@ __device__ int ckt_load(const ngsf_ckt_t &C, Ctl &s, const Iter &it)
 
 /* SMPluFac: left-looking refactorization on the fixed pivot sequence.
  * One warp per column; columns of one level are independent.
- * Returns 1 when a pivot is zero or not finite, or when the pivot has lost
- * so much ground to its column that |L(i,k)| > NGSF_GROWTH: the host then
- * chooses new pivots from this matrix (the reference re-factors with
- * pivoting when refactoring fails, src/maths/ni/niiter.c:161-195). */
+ * Returns 1 when a pivot is zero or not finite, or an L entry is not
+ * finite: the host then chooses new pivots from this matrix (the reference
+ * re-factors with pivoting when refactoring fails,
+ * src/maths/ni/niiter.c:161-195; klu_refactor fails on a zero pivot only,
+ * src/maths/KLU/klusmp.c:591-602).  In the operating point (gmin and
+ * source stepping move the matrix far from the one the pivots were chosen
+ * on) an L entry above NGSF_GROWTH also asks for new pivots; the transient
+ * refactors on its pivots like the reference. */
 #define NGSF_GROWTH 1e6
+__device__ __forceinline__ double growth_limit(const Ctl &s)
+{
+    return (s.mode & (NGSF_MODEDCOP | NGSF_MODETRANOP)) ? NGSF_GROWTH : DBL_MAX;
+}
 
 /* Right-looking refactorization on the fixed pivot sequence, level by
  * level of the column dependency graph (large matrices).  Phase p applies
@@ -1087,7 +1115,7 @@ __device__ __forceinline__ int rl_phase_work(const ngsf_ckt_t &C, int p)
     return w;
 }
 
-__device__ int rl_phase(const ngsf_ckt_t &C, int p, int t, int T)
+__device__ int rl_phase(const ngsf_ckt_t &C, int p, int t, int T, double growth)
 {
     int bad = 0;
     if (p < C.rl_levels) {
@@ -1108,7 +1136,7 @@ __device__ int rl_phase(const ngsf_ckt_t &C, int p, int t, int T)
         for (int e = C.sc_ptr[p - 1] + t; e < C.sc_ptr[p]; e += T) {
             double l_ik = C.lux[C.sc_pos[e]] / C.lux[C.sc_piv[e]];
             C.lux[C.sc_pos[e]] = l_ik;
-            if (!(fabs(l_ik) <= NGSF_GROWTH))
+            if (!(fabs(l_ik) <= growth))
                 bad = 1;
         }
     }
@@ -1118,7 +1146,7 @@ __device__ int rl_phase(const ngsf_ckt_t &C, int p, int t, int T)
 /* One block: per level, the L entries of its pivots are divided first
  * (one division per entry), then the updates use the stored quotients;
  * the same quotients and products as rl_phase, two barriers per level. */
-__device__ int rl_level_block(const ngsf_ckt_t &C, int l)
+__device__ int rl_level_block(const ngsf_ckt_t &C, int l, double growth)
 {
     int bad = 0;
     for (int c = C.rl_ptr[l] + threadIdx.x; c < C.rl_ptr[l + 1]; c += blockDim.x) {
@@ -1129,7 +1157,7 @@ __device__ int rl_level_block(const ngsf_ckt_t &C, int l)
     for (int e = C.sc_ptr[l] + threadIdx.x; e < C.sc_ptr[l + 1]; e += blockDim.x) {
         double l_ik = C.lux[C.sc_pos[e]] / C.lux[C.sc_piv[e]];
         C.lux[C.sc_pos[e]] = l_ik;
-        if (!(fabs(l_ik) <= NGSF_GROWTH))
+        if (!(fabs(l_ik) <= growth))
             bad = 1;
     }
     __syncthreads();
@@ -1174,8 +1202,9 @@ __device__ int lu_factor_rl(const ngsf_ckt_t &C, Ctl &s, int b, int nbAll)
                     C.lux[C.a_lupos[C.a_diag[j]]] += s.diagGmin;
             __syncthreads();
         }
+        const double growth = growth_limit(s);
         for (int l = 0; l < C.rl_levels; l++)
-            bad |= rl_level_block(C, l);
+            bad |= rl_level_block(C, l, growth);
         solve_pack(C, threadIdx.x, blockDim.x);
         return block_or(s, bad);
     }
@@ -1198,18 +1227,19 @@ __device__ int lu_factor_rl(const ngsf_ckt_t &C, Ctl &s, int b, int nbAll)
             gsync();
         }
         const int L = C.rl_levels;
+        const double growth = growth_limit(s);
         bool small = rl_phase_work(C, 0) <= smallWork;
         for (int p = 0; p <= L; p++) {
             const bool nextSmall = p < L && rl_phase_work(C, p + 1) <= smallWork;
             if (small) {
                 if (b == 0) {
-                    bad |= rl_phase(C, p, threadIdx.x, blockDim.x);
+                    bad |= rl_phase(C, p, threadIdx.x, blockDim.x, growth);
                     __syncthreads();
                 }
                 if (!nextSmall)
                     gsync();
             } else {
-                bad |= rl_phase(C, p, t, T);
+                bad |= rl_phase(C, p, t, T, growth);
                 gsync();
             }
             small = nextSmall;
@@ -1249,6 +1279,7 @@ __device__ int lu_factor(const ngsf_ckt_t &C, Ctl &s)
         __syncthreads();
     }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const double growth = growth_limit(s);
     int bad = 0;
     for (int l = 0; l < C.nlevels; l++) {
         for (int c = C.lvl_ptr[l] + warp; c < C.lvl_ptr[l + 1]; c += NGSF_WARPS) {
@@ -1265,7 +1296,7 @@ __device__ int lu_factor(const ngsf_ckt_t &C, Ctl &s)
             for (int q = C.cdiag[k] + 1 + lane; q < C.cend[k]; q += 32) {
                 double l_ik = C.lux[q] / piv;
                 C.lux[q] = l_ik;
-                if (!(fabs(l_ik) <= NGSF_GROWTH))
+                if (!(fabs(l_ik) <= growth))
                     bad = 1;
             }
             __syncwarp();
@@ -1623,7 +1654,9 @@ __device__ int ni_iter(const ngsf_ckt_t &C, Ctl &s, int maxIter, bool resume)
                 return NGSF_NEED_REORDER;
             }
         }
+        long long tp = prof_t(C);
         int bad = lu_factor(C, s);
+        prof_add(C, NGSF_P_FACTOR, tp);
         if (bad) {
             if (resume) {
                 /* fresh pivots from this very matrix still fail: singular */
@@ -1643,12 +1676,16 @@ __device__ int ni_iter(const ngsf_ckt_t &C, Ctl &s, int maxIter, bool resume)
             return NGSF_NEED_REORDER;
         }
         resume = false;
+        tp = prof_t(C);
         lu_solve(C, s, it.rhs);
         if (threadIdx.x == 0) {
             it.rhs[0] = 0;
             it.rhsOld[0] = 0;
         }
         __syncthreads();
+        prof_add(C, NGSF_P_SOLVE, tp);
+        if (C.prof && threadIdx.x == 0)
+            C.prof[NGSF_P_ITERS]++;
         if (iterno > maxIter) {
             if (threadIdx.x == 0)
                 s.numIter += iterno;
@@ -1659,10 +1696,12 @@ __device__ int ni_iter(const ngsf_ckt_t &C, Ctl &s, int maxIter, bool resume)
          * the first when it started from the predictor's guess (every
          * unknown against its guessed value, the same test) */
         const bool guess1 = (s.mode & NGSF_MODEGUESS) && iterno == 1;
+        tp = prof_t(C);
         if (noncon == 0 && (iterno != 1 || guess1))
             noncon = conv_test(C, s, it);
         else
             noncon = 1;
+        prof_add(C, NGSF_P_CONV, tp);
         int mode = s.mode & ~NGSF_MODEGUESS;
         int ret = -1, reorder = 0;
         if (mode & NGSF_MODEINITFLOAT) {
@@ -2194,7 +2233,9 @@ __device__ int dc_tran(const ngsf_ckt_t &C, Ctl &s, long long maxSteps, bool res
                 __syncthreads();
                 continue;
             }
+            const long long tt = prof_t(C);
             double newdelta = ckt_trunc(C, s, s.delta);
+            prof_add(C, NGSF_P_TRUNC, tt);
             if (newdelta > .9 * s.delta) {
                 if (s.order == 1 && maxOrder > 1) {
                     __syncthreads();   /* every warp has read the order */
@@ -2314,6 +2355,11 @@ __device__ void run_circuit(const ngsf_ckt_t &C, Ctl &s, int runMode, long long 
 {
     const bool hold = (runMode & RUN_HOLD) != 0;
     runMode &= ~RUN_HOLD;
+    if (C.prof && threadIdx.x == 0 && runMode == RUN_FRESH)
+        for (int k = 0; k < NGSF_P_COUNT; k++)
+            C.prof[k] = 0;
+    __syncthreads();
+    const long long tRun = prof_t(C);
     if (runMode == RUN_RESUME) {
         const int *src = (const int *)C.ctlsave;
         int *dst = (int *)&s;
@@ -2406,6 +2452,7 @@ __device__ void run_circuit(const ngsf_ckt_t &C, Ctl &s, int runMode, long long 
         C.fresult[NGSF_F_DELTA] = s.delta;
         C.fresult[NGSF_F_DIAGGMIN] = s.diagGmin;
     }
+    prof_add(C, NGSF_P_TOTAL, tRun);
 }
 
 }  // namespace
@@ -2435,6 +2482,200 @@ __global__ void __launch_bounds__(NGSF_THREADS) stamp_static_kernel(ngsf_ckt_t C
         g_psm = nullptr;
     }
     run_circuit(Cs, s, RUN_PROBE, 0);
+}
+
+/* ---------------------------------------------------------------- */
+/* Operator surface: one device operation on a circuit's arrays,      */
+/* outside the transient -- CKTload / DEVload of chosen device types, */
+/* SMPluFac, SMPsolve, NIconvTest, CKTtrunc -- on one block, with the */
+/* control scalars the caller gives (ngsf_ckt_load and friends)        */
+/* ---------------------------------------------------------------- */
+struct OpArgs {
+    int op, mode, order, types;
+    double time, delta, deltaOld[3], ag0, ag1, gmin, srcFact, diagGmin;
+};
+enum { OPK_LOAD = 1, OPK_LUFAC, OPK_SOLVE, OPK_CONV, OPK_TRUNC };
+
+/* first stamp slot of each device type in table order (bsim4, cap, dio,
+ * isrc, mos1, res, vsrc), then the slot count: the compiler lays the
+ * types' slot blocks out in this order */
+__device__ void type_slot_starts(const ngsf_ckt_t &C, int st[8])
+{
+    st[0] = C.bsim4.stamp0;
+    st[1] = C.cap.stamp0;
+    st[2] = C.dio.stamp0;
+    st[3] = C.isrc.stamp0;
+    st[4] = C.mos1.stamp0;
+    st[5] = C.res.stamp0;
+    st[6] = C.vsrc.stamp0;
+    st[7] = C.nstamp;
+}
+
+/* CKTload restricted to the device types in `types` (bit k = type k of
+ * the table order): the other types' stamp slots are cleared, so the
+ * gather sums exactly the selected DEVload contributions, in the
+ * reference's order.  All types: the whole CKTload. */
+__device__ int op_load(const ngsf_ckt_t &C, Ctl &s, const Iter &it, int types)
+{
+    const int t = threadIdx.x, T = blockDim.x;
+    int st[8];
+    type_slot_starts(C, st);
+    int nc = 0;
+    if (types & (1 << NGSF_DEV_BSIM4))
+        for (int i = t; i < C.bsim4.n; i += T)
+            nc |= bsim4_load_one(C, s, it, i);
+    if (types & (1 << NGSF_DEV_CAP))
+        cap_load(C, s, it, t, T);
+    if (types & (1 << NGSF_DEV_DIO))
+        for (int i = t; i < C.dio.n; i += T)
+            nc |= dio_load_one(C, s, it, i);
+    if (types & (1 << NGSF_DEV_MOS1))
+        for (int i = t; i < C.mos1.n; i += T)
+            nc |= mos1_load_one(C, s, it, i);
+    if (types & (1 << NGSF_DEV_RES))
+        res_load(C, t, T);
+    if (types & ((1 << NGSF_DEV_VSRC) | (1 << NGSF_DEV_ISRC)))
+        src_load(C, s);
+    __syncthreads();
+    for (int k = 0; k < NGSF_DEV_TYPES; k++)
+        if (!(types & (1 << k)))
+            for (int q = st[k] + t; q < st[k + 1]; q += T)
+                C.stampv[q] = 0.0;
+    nc = block_or(s, nc);   /* includes __syncthreads: stamps visible */
+    gather(C, it, t, T, t >> 5, NGSF_WARPS);
+    __syncthreads();
+    gather_heavy_combine(C, it);
+    __syncthreads();
+    return nc;
+}
+
+__global__ void __launch_bounds__(NGSF_THREADS)
+op_kernel(const ngsf_ckt_t *ckt, OpArgs a, int solveCap, int *iout, double *dout)
+{
+    extern __shared__ __align__(16) unsigned char ngsf_dyn[];
+    __shared__ Ctl s;
+    __shared__ __align__(16) ngsf_ckt_t Cs;
+    {
+        const unsigned long long *src = (const unsigned long long *)ckt;
+        unsigned long long *dst = (unsigned long long *)&Cs;
+        for (int w = threadIdx.x; w < (int)(sizeof(ngsf_ckt_t) / 8); w += blockDim.x)
+            dst[w] = src[w];
+        unsigned long long *z = (unsigned long long *)&s;
+        for (int w = threadIdx.x; w < (int)(sizeof(Ctl) / 8); w += blockDim.x)
+            z[w] = 0ull;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        Cs.wide = nullptr;
+        g_psm = nullptr;
+        s.time = a.time;
+        s.delta = a.delta;
+        for (int k = 0; k < 3; k++)
+            s.deltaOld[k] = a.deltaOld[k];
+        s.ag[0] = a.ag0;
+        s.ag[1] = a.ag1;
+        s.order = a.order;
+        s.mode = a.mode;
+        s.gmin = a.gmin;
+        s.srcFact = a.srcFact;
+        s.diagGmin = a.diagGmin;
+        for (int k = 0; k < 4; k++)
+            s.ring[k] = k;
+        s.rhsSel = 0;
+    }
+    __syncthreads();
+    solve_buffers_init(Cs, ngsf_dyn, solveCap);
+    Iter it = iter_ctx(Cs, s);
+    int r = 0;
+    double d = 0.0;
+    switch (a.op) {
+    case OPK_LOAD:
+        r = op_load(Cs, s, it, a.types);
+        break;
+    case OPK_LUFAC:
+        r = lu_factor(Cs, s);
+        break;
+    case OPK_SOLVE:
+        lu_solve(Cs, s, it.rhs);
+        break;
+    case OPK_CONV:
+        r = conv_test(Cs, s, it);
+        break;
+    case OPK_TRUNC:
+        d = ckt_trunc(Cs, s, a.delta);
+        break;
+    default:
+        r = -1;
+    }
+    if (threadIdx.x == 0) {
+        iout[0] = r;
+        dout[0] = d;
+    }
+}
+
+/* Stand-alone device evaluation over the whole grid: every thread of the
+ * grid evaluates the devices of the selected types one instance at a time
+ * (the same device functions the transient calls), `reps` times, with no
+ * gather.  It times the FP64-bound half of CKTload on its own. */
+__global__ void __launch_bounds__(NGSF_THREADS)
+eval_kernel(const ngsf_ckt_t *ckt, OpArgs a, int reps)
+{
+    __shared__ Ctl s;
+    __shared__ __align__(16) ngsf_ckt_t Cs;
+    {
+        const unsigned long long *src = (const unsigned long long *)ckt;
+        unsigned long long *dst = (unsigned long long *)&Cs;
+        for (int w = threadIdx.x; w < (int)(sizeof(ngsf_ckt_t) / 8); w += blockDim.x)
+            dst[w] = src[w];
+        unsigned long long *z = (unsigned long long *)&s;
+        for (int w = threadIdx.x; w < (int)(sizeof(Ctl) / 8); w += blockDim.x)
+            z[w] = 0ull;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        s.time = a.time;
+        s.delta = a.delta;
+        for (int k = 0; k < 3; k++)
+            s.deltaOld[k] = a.deltaOld[k];
+        s.ag[0] = a.ag0;
+        s.ag[1] = a.ag1;
+        s.order = a.order;
+        s.mode = a.mode;
+        s.gmin = a.gmin;
+        s.srcFact = a.srcFact;
+        for (int k = 0; k < 4; k++)
+            s.ring[k] = k;
+    }
+    __syncthreads();
+    const Iter it = iter_ctx(Cs, s);
+    const int t = blockIdx.x * blockDim.x + threadIdx.x, T = gridDim.x * blockDim.x;
+    for (int r = 0; r < reps; r++) {
+        if (a.types & (1 << NGSF_DEV_BSIM4))
+            for (int i = t; i < Cs.bsim4.n; i += T)
+                bsim4_load_one(Cs, s, it, i);
+        if (a.types & (1 << NGSF_DEV_MOS1))
+            for (int i = t; i < Cs.mos1.n; i += T)
+                mos1_load_one(Cs, s, it, i);
+        if (a.types & (1 << NGSF_DEV_DIO))
+            for (int i = t; i < Cs.dio.n; i += T)
+                dio_load_one(Cs, s, it, i);
+    }
+}
+
+/* FP64 throughput probe: independent fused multiply-add chains per
+ * thread (2 flops each), the result kept live through one store. */
+__global__ void fp64_peak_kernel(double *out, int iters)
+{
+    double a0 = threadIdx.x * 1e-9, a1 = a0 + 1e-10, a2 = a0 + 2e-10, a3 = a0 + 3e-10;
+    double a4 = a0 + 4e-10, a5 = a0 + 5e-10, a6 = a0 + 6e-10, a7 = a0 + 7e-10;
+    const double m = 0.999999999, c = 1e-12;
+    for (int i = 0; i < iters; i++) {
+        a0 = fma(a0, m, c); a1 = fma(a1, m, c); a2 = fma(a2, m, c); a3 = fma(a3, m, c);
+        a4 = fma(a4, m, c); a5 = fma(a5, m, c); a6 = fma(a6, m, c); a7 = fma(a7, m, c);
+    }
+    const double r = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+    if (r == 12345.678)
+        out[blockIdx.x] = r;
 }
 
 static_assert(sizeof(Ctl) <= NGSF_WIDE_CTL_BYTES, "control block does not fit the wide hand-over");
@@ -2555,6 +2796,7 @@ extern "C" NGSF_API int ngsf_stamp_initial_static(const ngsf_handle *h, double *
     c.capmax = 0;
     c.wide = nullptr;
     c.pred.kind = 0;
+    c.prof = nullptr;
     stamp_static_kernel<<<1, NGSF_THREADS>>>(c);
     e = cudaGetLastError();
     if (e == cudaSuccess && ax)
@@ -2635,3 +2877,345 @@ extern "C" cudaError_t ngsf_launch_tran(const ngsf_ckt_t *d_ckts, const int *d_o
         d_ckts, d_order, nckt, runMode, maxSteps, solveCap, gnnBytes);
     return cudaGetLastError();
 }
+
+/* ---------------------------------------------------------------- */
+/* Operator surface, host side (declared in ngspice_gb300.h)          */
+/* ---------------------------------------------------------------- */
+extern "C" const ngsf_ckt_t *ngsf_internal_ddesc(const ngsf_handle *h);
+
+namespace {
+
+OpArgs op_args(int op, const ngsf_point *pt, int types)
+{
+    OpArgs a{};
+    a.op = op;
+    a.types = types;
+    if (pt) {
+        a.mode = pt->mode;
+        a.order = pt->order;
+        a.time = pt->time;
+        a.delta = pt->delta;
+        for (int k = 0; k < 3; k++)
+            a.deltaOld[k] = pt->deltaOld[k];
+        a.ag0 = pt->ag[0];
+        a.ag1 = pt->ag[1];
+        a.gmin = pt->gmin;
+        a.srcFact = pt->srcFact;
+        a.diagGmin = pt->diagGmin;
+    }
+    return a;
+}
+
+/* one op_kernel launch on circuit h; *r / *dv receive its result words */
+int launch_op(const ngsf_handle *h, const OpArgs &a, int *r, double *dv, const char *who)
+{
+    const ngsf_ckt_t *hd = ngsf_internal_desc(h), *dd = ngsf_internal_ddesc(h);
+    if (!hd || !dd) {
+        ngsf_internal_set_error((std::string(who) + ": null or host-only handle").c_str());
+        return -1;
+    }
+    int *d_i = nullptr;
+    cudaError_t e = cudaMalloc(&d_i, 16);
+    if (e == cudaSuccess)
+        e = allow_dyn_smem((const void *)op_kernel);
+    const int solveCap = ngsf_solve_smem_bytes(hd->n);
+    if (e == cudaSuccess) {
+        op_kernel<<<1, NGSF_THREADS, (size_t)solveCap>>>(dd, a, solveCap, d_i,
+                                                          (double *)(d_i + 2));
+        e = cudaGetLastError();
+    }
+    int ri[4] = {0};
+    if (e == cudaSuccess)
+        e = cudaMemcpy(ri, d_i, 16, cudaMemcpyDeviceToHost);
+    if (d_i)
+        cudaFree(d_i);
+    if (e != cudaSuccess) {
+        ngsf_internal_set_error((std::string(who) + ": " + cudaGetErrorString(e)).c_str());
+        return -1;
+    }
+    if (r)
+        *r = ri[0];
+    if (dv)
+        memcpy(dv, ri + 2, sizeof(double));
+    return 0;
+}
+
+int put(void *dst, const void *src, size_t bytes, const char *who)
+{
+    if (!src || !bytes)
+        return 0;
+    cudaError_t e = cudaMemcpy(dst, src, bytes, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        ngsf_internal_set_error((std::string(who) + ": " + cudaGetErrorString(e)).c_str());
+        return -1;
+    }
+    return 0;
+}
+
+int get(void *dst, const void *src, size_t bytes, const char *who)
+{
+    if (!dst || !bytes)
+        return 0;
+    cudaError_t e = cudaMemcpy(dst, src, bytes, cudaMemcpyDeviceToHost);
+    if (e != cudaSuccess) {
+        ngsf_internal_set_error((std::string(who) + ": " + cudaGetErrorString(e)).c_str());
+        return -1;
+    }
+    return 0;
+}
+
+/* the linearisation point: rhsOld, CKTstates[0..nvec-1], BSIM4von */
+int put_point(const ngsf_ckt_t *d, const double *rhsOld, const double *states, int nvec,
+              const double *von, const char *who)
+{
+    if (nvec < 0 || nvec > 4) {
+        ngsf_internal_set_error((std::string(who) + ": nvec must be 0..4").c_str());
+        return -1;
+    }
+    const size_t n1 = (size_t)d->n + 1;
+    if (put(d->rhsOld, rhsOld, n1 * sizeof(double), who))
+        return -1;
+    if (states && put(d->states, states, (size_t)nvec * d->nstates * sizeof(double), who))
+        return -1;
+    if (von && d->bsim4.n > 0 &&
+        put(d->bsim4.h + (size_t)B4H_VON * d->bsim4.n, von, (size_t)d->bsim4.n * sizeof(double),
+            who))
+        return -1;
+    return 0;
+}
+
+}  // namespace
+
+extern "C" NGSF_API int ngsf_ckt_load(ngsf_handle *h, const ngsf_point *pt, int types,
+                                      const double *rhsOld, const double *states, int nvec,
+                                      const double *von, double *ax, double *rhs, int *noncon)
+{
+    const char *who = "ngsf_ckt_load";
+    const ngsf_ckt_t *d = ngsf_internal_desc(h);
+    if (!d || !pt) {
+        ngsf_internal_set_error("ngsf_ckt_load: null handle or point");
+        return -1;
+    }
+    const int starts[8] = {d->bsim4.stamp0, d->cap.stamp0, d->dio.stamp0, d->isrc.stamp0,
+                           d->mos1.stamp0,  d->res.stamp0, d->vsrc.stamp0, d->nstamp};
+    for (int k = 0; k < NGSF_DEV_TYPES; k++)
+        if (starts[k] > starts[k + 1]) {
+            ngsf_internal_set_error("ngsf_ckt_load: stamp slot blocks out of table order");
+            return -1;
+        }
+    if (put_point(d, rhsOld, states, nvec, von, who))
+        return -1;
+    int nc = 0;
+    if (launch_op(h, op_args(OPK_LOAD, pt, types & ((1 << NGSF_DEV_TYPES) - 1)), &nc, nullptr,
+                  who))
+        return -1;
+    if (get(ax, d->ax, (size_t)d->nnz * sizeof(double), who) ||
+        get(rhs, d->rhs, ((size_t)d->n + 1) * sizeof(double), who))
+        return -1;
+    if (noncon)
+        *noncon = nc;
+    return 0;
+}
+
+extern "C" NGSF_API int ngsf_ckt_read_states(const ngsf_handle *h, double *states, int nvec)
+{
+    const ngsf_ckt_t *d = ngsf_internal_desc(h);
+    if (!d || nvec < 0 || nvec > 4) {
+        ngsf_internal_set_error("ngsf_ckt_read_states: null handle or nvec outside 0..4");
+        return -1;
+    }
+    return get(states, d->states, (size_t)nvec * d->nstates * sizeof(double),
+               "ngsf_ckt_read_states");
+}
+
+extern "C" NGSF_API int ngsf_ckt_trunc(ngsf_handle *h, const ngsf_point *pt,
+                                       const double *states, int nvec, double *timestep)
+{
+    const char *who = "ngsf_ckt_trunc";
+    const ngsf_ckt_t *d = ngsf_internal_desc(h);
+    if (!d || !pt || pt->order < 1 || pt->order > 2) {
+        ngsf_internal_set_error("ngsf_ckt_trunc: null handle or point, or order outside 1..2");
+        return -1;
+    }
+    if (put_point(d, nullptr, states, nvec, nullptr, who))
+        return -1;
+    double t = 0;
+    if (launch_op(h, op_args(OPK_TRUNC, pt, 0), nullptr, &t, who))
+        return -1;
+    if (timestep)
+        *timestep = t;
+    return 0;
+}
+
+extern "C" NGSF_API int ngsf_ni_convtest(ngsf_handle *h, const double *rhs, const double *rhsOld,
+                                         int *noncon)
+{
+    const char *who = "ngsf_ni_convtest";
+    const ngsf_ckt_t *d = ngsf_internal_desc(h);
+    if (!d || !rhs || !rhsOld) {
+        ngsf_internal_set_error("ngsf_ni_convtest: null handle or vector");
+        return -1;
+    }
+    const size_t b = ((size_t)d->n + 1) * sizeof(double);
+    if (put(d->rhs, rhs, b, who) || put(d->rhsOld, rhsOld, b, who))
+        return -1;
+    int nc = 0;
+    if (launch_op(h, op_args(OPK_CONV, nullptr, 0), &nc, nullptr, who))
+        return -1;
+    if (noncon)
+        *noncon = nc;
+    return 0;
+}
+
+extern "C" NGSF_API int ngsf_smp_set_matrix(ngsf_handle *h, const double *ax)
+{
+    const ngsf_ckt_t *d = ngsf_internal_desc(h);
+    if (!d || !ax) {
+        ngsf_internal_set_error("ngsf_smp_set_matrix: null handle or values");
+        return -1;
+    }
+    return put(d->ax, ax, (size_t)d->nnz * sizeof(double), "ngsf_smp_set_matrix");
+}
+
+extern "C" NGSF_API int ngsf_smp_get_matrix(const ngsf_handle *h, double *ax)
+{
+    const ngsf_ckt_t *d = ngsf_internal_desc(h);
+    if (!d || !ax) {
+        ngsf_internal_set_error("ngsf_smp_get_matrix: null handle or buffer");
+        return -1;
+    }
+    return get(ax, d->ax, (size_t)d->nnz * sizeof(double), "ngsf_smp_get_matrix");
+}
+
+extern "C" NGSF_API int ngsf_smp_lufac(ngsf_handle *h, double diag_gmin)
+{
+    const ngsf_ckt_t *d = ngsf_internal_desc(h);
+    if (!d) {
+        ngsf_internal_set_error("ngsf_smp_lufac: null handle");
+        return -1;
+    }
+    if (d->nlu <= 0) {
+        ngsf_internal_set_error("ngsf_smp_lufac: no pivot sequence yet (call ngsf_smp_reorder)");
+        return -1;
+    }
+    ngsf_point pt{};
+    pt.diagGmin = diag_gmin;
+    int bad = 0;
+    if (launch_op(h, op_args(OPK_LUFAC, &pt, 0), &bad, nullptr, "ngsf_smp_lufac"))
+        return -1;
+    return bad ? NGSF_E_SINGULAR : 0;
+}
+
+extern "C" NGSF_API int ngsf_smp_solve(ngsf_handle *h, double *rhs)
+{
+    const char *who = "ngsf_smp_solve";
+    const ngsf_ckt_t *d = ngsf_internal_desc(h);
+    if (!d || !rhs || d->nlu <= 0) {
+        ngsf_internal_set_error("ngsf_smp_solve: null handle or vector, or no factor yet");
+        return -1;
+    }
+    const size_t b = ((size_t)d->n + 1) * sizeof(double);
+    if (put(d->rhs, rhs, b, who))
+        return -1;
+    if (launch_op(h, op_args(OPK_SOLVE, nullptr, 0), nullptr, nullptr, who))
+        return -1;
+    if (get(rhs, d->rhs, b, who))
+        return -1;
+    rhs[0] = 0.0;
+    return 0;
+}
+
+/* the engine side of ngsf_smp_reorder (api.cpp plans the pivots) */
+extern "C" int ngsf_internal_lufac(ngsf_handle *h, double diag_gmin)
+{
+    return ngsf_smp_lufac(h, diag_gmin);
+}
+
+extern "C" NGSF_API int ngsf_eval_bench(ngsf_handle *h, const ngsf_point *pt, int types,
+                                        int reps, int blocks, double *seconds)
+{
+    const char *who = "ngsf_eval_bench";
+    const ngsf_ckt_t *dd = ngsf_internal_ddesc(h);
+    if (!dd || !pt || reps < 1) {
+        ngsf_internal_set_error("ngsf_eval_bench: null handle or point, or reps < 1");
+        return -1;
+    }
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess)
+        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (blocks <= 0)
+        blocks = sms;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (e == cudaSuccess)
+        e = cudaEventCreate(&e0);
+    if (e == cudaSuccess)
+        e = cudaEventCreate(&e1);
+    OpArgs a = op_args(0, pt, types);
+    if (e == cudaSuccess) {
+        eval_kernel<<<blocks, NGSF_THREADS>>>(dd, a, 1);   /* warm-up */
+        cudaEventRecord(e0, 0);
+        eval_kernel<<<blocks, NGSF_THREADS>>>(dd, a, reps);
+        cudaEventRecord(e1, 0);
+        e = cudaEventSynchronize(e1);
+    }
+    if (e == cudaSuccess)
+        e = cudaGetLastError();
+    float ms = 0;
+    if (e == cudaSuccess)
+        e = cudaEventElapsedTime(&ms, e0, e1);
+    if (e0)
+        cudaEventDestroy(e0);
+    if (e1)
+        cudaEventDestroy(e1);
+    if (e != cudaSuccess) {
+        ngsf_internal_set_error((std::string(who) + ": " + cudaGetErrorString(e)).c_str());
+        return -1;
+    }
+    if (seconds)
+        *seconds = ms * 1e-3;
+    return 0;
+}
+
+extern "C" NGSF_API int ngsf_fp64_peak(double *flops_per_second)
+{
+    int dev = 0, sms = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess)
+        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    double *d = nullptr;
+    const int blocks = 8 * (sms > 0 ? sms : 1), threads = 256, iters = 1 << 14;
+    if (e == cudaSuccess)
+        e = cudaMalloc(&d, (size_t)blocks * sizeof(double));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (e == cudaSuccess)
+        e = cudaEventCreate(&e0);
+    if (e == cudaSuccess)
+        e = cudaEventCreate(&e1);
+    float best = 0;
+    for (int rep = 0; rep < 4 && e == cudaSuccess; rep++) {
+        cudaEventRecord(e0, 0);
+        fp64_peak_kernel<<<blocks, threads>>>(d, iters);
+        cudaEventRecord(e1, 0);
+        e = cudaEventSynchronize(e1);
+        float ms = 0;
+        if (e == cudaSuccess)
+            e = cudaEventElapsedTime(&ms, e0, e1);
+        if (e == cudaSuccess && rep > 0 && (best == 0 || ms < best))
+            best = ms;
+    }
+    if (e0)
+        cudaEventDestroy(e0);
+    if (e1)
+        cudaEventDestroy(e1);
+    if (d)
+        cudaFree(d);
+    if (e != cudaSuccess || best <= 0) {
+        ngsf_internal_set_error(e != cudaSuccess ? cudaGetErrorString(e) : "fp64 probe: no time");
+        return -1;
+    }
+    if (flops_per_second)
+        *flops_per_second = 2.0 * 8.0 * (double)iters * blocks * threads / (best * 1e-3);
+    return 0;
+}
+

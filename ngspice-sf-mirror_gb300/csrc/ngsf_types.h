@@ -310,7 +310,16 @@ typedef struct {
     double *fresult;      /* see NGSF_F_* */
     ngsf_wide_t *wide;    /* set only for a wide (cooperative) launch */
     ngsf_pred_t pred;     /* learned Newton predictor (kind 0: off) */
+    /* per-phase SM clock cycles of the circuit's block (NGSF_P_*), summed
+     * over a run; null = not recorded */
+    long long *prof;
 } ngsf_ckt_t;
+
+/* phases of the per-phase clock record */
+enum {
+    NGSF_P_LOAD, NGSF_P_GATHER, NGSF_P_FACTOR, NGSF_P_SOLVE, NGSF_P_CONV, NGSF_P_TRUNC,
+    NGSF_P_TOTAL, NGSF_P_ITERS, NGSF_P_COUNT
+};
 
 /* integer results */
 enum {

@@ -134,7 +134,7 @@ void DeviceCircuit::upload(const Image &img, const std::vector<int> &probes, int
             upd_src, prow, pcol, fl_ptr, fl_row, bl_ptr, bl_row, lr_ptr, lr_col, lr_pos,
             ur_ptr, ur_col, ur_pos, work;
         size_t states, rhs, rhsOld, breaks, out, probe, cap_ax, cap_rhs, cap_meta, result,
-            fresult, ctlsave, wide;
+            fresult, ctlsave, wide, prof;
     } o{};
     o.b4_node = puti(img.b4_node);
     o.b4_st = puti(img.b4_st);
@@ -212,6 +212,7 @@ void DeviceCircuit::upload(const Image &img, const std::vector<int> &probes, int
     o.result = zero(NGSF_R_COUNT * sizeof(int));
     o.fresult = zero(NGSF_F_COUNT * sizeof(double));
     o.wide = zero(sizeof(ngsf_wide_t));
+    o.prof = zero(NGSF_P_COUNT * sizeof(long long));
 
     if (impl->base)
         cudaFree(impl->base);
@@ -277,6 +278,9 @@ void DeviceCircuit::upload(const Image &img, const std::vector<int> &probes, int
     h.result = I(o.result);
     h.fresult = D(o.fresult);
     h.wide = (ngsf_wide_t *)(b + o.wide);
+    /* NGSF_PHASES=1: record per-phase clock cycles (ngsf_phase_cycles) */
+    const char *ph = getenv("NGSF_PHASES");
+    h.prof = (ph && atoi(ph) != 0) ? (long long *)(b + o.prof) : nullptr;
     if (!impl->d_desc)
         ck(cudaMalloc(&impl->d_desc, sizeof(ngsf_ckt_t)), "cudaMalloc(desc)");
     ck(cudaMemcpy(impl->d_desc, &h, sizeof(h), cudaMemcpyHostToDevice), "cudaMemcpy(desc)");

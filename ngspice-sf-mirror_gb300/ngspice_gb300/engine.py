@@ -30,6 +30,10 @@ EXPORTS = [
     "ngsf_gnn_param_count", "ngsf_gnn_create", "ngsf_gnn_destroy", "ngsf_gnn_set_params",
     "ngsf_gnn_get_params", "ngsf_gnn_forward", "ngsf_gnn_train_step", "ngsf_gnn_gemm_test",
     "ngsf_node_graph", "ngsf_set_predictor", "ngsf_wide_info", "ngsf_set_factor_shape",
+    "ngsf_dev_table", "ngsf_ckt_load", "ngsf_ckt_read_states", "ngsf_ckt_trunc",
+    "ngsf_ni_convtest", "ngsf_smp_set_matrix", "ngsf_smp_get_matrix", "ngsf_smp_reorder",
+    "ngsf_smp_lufac", "ngsf_smp_solve", "ngsf_phase_cycles", "ngsf_eval_bench",
+    "ngsf_fp64_peak",
     "ngSpice_Init", "ngSpice_Init_Sync", "ngSpice_Command", "ngGet_Vec_Info",
     "ngSpice_Circ", "ngSpice_CurPlot", "ngSpice_AllPlots", "ngSpice_AllVecs",
     "ngSpice_running", "ngSpice_SetBkpt", "ngSpice_nospinit", "ngSpice_nospiceinit",
@@ -38,9 +42,47 @@ EXPORTS = [
 
 _lib = None
 
+# device types in the reference's device-table order (NGSF_DEV_*)
+DEV_BSIM4, DEV_CAP, DEV_DIO, DEV_ISRC, DEV_MOS1, DEV_RES, DEV_VSRC = range(7)
+DEV_ALL = (1 << 7) - 1
+E_SINGULAR = 102
+
 
 class EngineError(RuntimeError):
     pass
+
+
+class Point(C.Structure):
+    """ngsf_point: the CKTcircuit control scalars of one operation."""
+    _fields_ = [("time", C.c_double), ("delta", C.c_double), ("deltaOld", C.c_double * 3),
+                ("ag", C.c_double * 2), ("gmin", C.c_double), ("srcFact", C.c_double),
+                ("diagGmin", C.c_double), ("mode", C.c_int), ("order", C.c_int)]
+
+
+class DevInfo(C.Structure):
+    _fields_ = [("name", C.c_char_p), ("states", C.c_int), ("stamps", C.c_int),
+                ("has_load", C.c_int), ("has_trunc", C.c_int), ("has_accept", C.c_int)]
+
+
+def make_point(time=0.0, delta=0.0, deltaOld=(0.0, 0.0, 0.0), ag=(0.0, 0.0), gmin=1e-12,
+               srcFact=1.0, diagGmin=0.0, mode=0, order=1) -> Point:
+    p = Point()
+    p.time, p.delta, p.gmin, p.srcFact, p.diagGmin = time, delta, gmin, srcFact, diagGmin
+    p.mode, p.order = int(mode), int(order)
+    for k in range(3):
+        p.deltaOld[k] = deltaOld[k] if k < len(deltaOld) else 0.0
+    p.ag[0], p.ag[1] = ag[0], ag[1]
+    return p
+
+
+def dev_table() -> list[dict]:
+    """The device table (ngsf_dev_table), one dict per device type."""
+    n = C.c_int()
+    t = C.POINTER(DevInfo)()
+    lib().ngsf_dev_table(C.byref(n), C.byref(t))
+    return [{"name": t[k].name.decode(), "states": t[k].states, "stamps": t[k].stamps,
+             "load": bool(t[k].has_load), "trunc": bool(t[k].has_trunc),
+             "accept": bool(t[k].has_accept)} for k in range(n.value)]
 
 
 def lib(path: str | None = None) -> C.CDLL:
@@ -76,6 +118,20 @@ def lib(path: str | None = None) -> C.CDLL:
     L.ngsf_device_bytes.argtypes = [vp]
     L.ngsf_last_launches.restype = C.c_int
     L.ngsf_workload.argtypes = [vp, C.POINTER(C.c_longlong)]
+    pp = C.POINTER(Point)
+    L.ngsf_dev_table.argtypes = [ip, C.POINTER(C.POINTER(DevInfo))]
+    L.ngsf_ckt_load.argtypes = [vp, pp, C.c_int, dp, dp, C.c_int, dp, dp, dp, ip]
+    L.ngsf_ckt_read_states.argtypes = [vp, dp, C.c_int]
+    L.ngsf_ckt_trunc.argtypes = [vp, pp, dp, C.c_int, dp]
+    L.ngsf_ni_convtest.argtypes = [vp, dp, dp, ip]
+    L.ngsf_smp_set_matrix.argtypes = [vp, dp]
+    L.ngsf_smp_get_matrix.argtypes = [vp, dp]
+    L.ngsf_smp_reorder.argtypes = [vp, C.c_double, C.c_double, C.c_double]
+    L.ngsf_smp_lufac.argtypes = [vp, C.c_double]
+    L.ngsf_smp_solve.argtypes = [vp, dp]
+    L.ngsf_phase_cycles.argtypes = [vp, C.POINTER(C.c_longlong)]
+    L.ngsf_eval_bench.argtypes = [vp, pp, C.c_int, C.c_int, C.c_int, dp]
+    L.ngsf_fp64_peak.argtypes = [dp]
     fp = C.POINTER(C.c_float)
     if hasattr(L, "ngsf_node_graph"):
         L.ngsf_node_graph.argtypes = [vp, ip, ip, ip, ip, ip, fp]
@@ -227,11 +283,109 @@ class Circuit:
         if lib().ngsf_set_predictor(self._h, int(kind), p):
             raise EngineError(last_error())
 
+    # ---- operator surface (CKTload / DEVload, CKTtrunc, NIconvTest, SMP*) ----
+    def ckt_load(self, point: Point, types: int = DEV_ALL, rhs_old=None, states=None,
+                 von=None) -> tuple[np.ndarray, np.ndarray, int]:
+        """(ax[nnz], rhs[n+1], noncon) of one CKTload at the given point."""
+        ax = np.zeros(self.nnz)
+        rhs = np.zeros(self.n + 1)
+        nc = C.c_int()
+        ro = None if rhs_old is None else np.ascontiguousarray(rhs_old, np.float64)
+        st = None if states is None else np.ascontiguousarray(states, np.float64)
+        vo = None if von is None else np.ascontiguousarray(von, np.float64)
+        nvec = 0 if st is None else st.shape[0]
+        if lib().ngsf_ckt_load(self._h, C.byref(point), int(types),
+                               None if ro is None else _ptr(ro, C.c_double),
+                               None if st is None else _ptr(st, C.c_double), nvec,
+                               None if vo is None else _ptr(vo, C.c_double),
+                               _ptr(ax, C.c_double), _ptr(rhs, C.c_double), C.byref(nc)):
+            raise EngineError(last_error())
+        return ax, rhs, nc.value
+
+    def read_states(self, nvec: int = 4) -> np.ndarray:
+        out = np.zeros((nvec, self.nstates))
+        if lib().ngsf_ckt_read_states(self._h, _ptr(out, C.c_double), nvec):
+            raise EngineError(last_error())
+        return out
+
+    def ckt_trunc(self, point: Point, states) -> float:
+        st = np.ascontiguousarray(states, np.float64)
+        t = C.c_double()
+        if lib().ngsf_ckt_trunc(self._h, C.byref(point), _ptr(st, C.c_double), st.shape[0],
+                                C.byref(t)):
+            raise EngineError(last_error())
+        return t.value
+
+    def ni_convtest(self, rhs, rhs_old) -> int:
+        a = np.ascontiguousarray(rhs, np.float64)
+        b = np.ascontiguousarray(rhs_old, np.float64)
+        nc = C.c_int()
+        if lib().ngsf_ni_convtest(self._h, _ptr(a, C.c_double), _ptr(b, C.c_double),
+                                  C.byref(nc)):
+            raise EngineError(last_error())
+        return nc.value
+
+    def smp_set_matrix(self, ax):
+        a = np.ascontiguousarray(ax, np.float64)
+        if lib().ngsf_smp_set_matrix(self._h, _ptr(a, C.c_double)):
+            raise EngineError(last_error())
+
+    def smp_get_matrix(self) -> np.ndarray:
+        a = np.zeros(self.nnz)
+        if lib().ngsf_smp_get_matrix(self._h, _ptr(a, C.c_double)):
+            raise EngineError(last_error())
+        return a
+
+    def smp_reorder(self, pivtol: float = 1e-13, pivrel: float = 1e-3,
+                    diag_gmin: float = 0.0) -> int:
+        """0, or E_SINGULAR; raises on an error."""
+        r = lib().ngsf_smp_reorder(self._h, pivtol, pivrel, diag_gmin)
+        if r not in (0, E_SINGULAR):
+            raise EngineError(last_error())
+        return r
+
+    def smp_lufac(self, diag_gmin: float = 0.0) -> int:
+        r = lib().ngsf_smp_lufac(self._h, diag_gmin)
+        if r not in (0, E_SINGULAR):
+            raise EngineError(last_error())
+        return r
+
+    def smp_solve(self, rhs) -> np.ndarray:
+        x = np.array(rhs, dtype=np.float64, copy=True)
+        if lib().ngsf_smp_solve(self._h, _ptr(x, C.c_double)):
+            raise EngineError(last_error())
+        return x
+
+    def phase_cycles(self) -> dict:
+        """SM clock cycles per phase of the last run (opened with NGSF_PHASES=1)."""
+        a = (C.c_longlong * 8)()
+        if lib().ngsf_phase_cycles(self._h, a):
+            raise EngineError(last_error())
+        keys = ["load", "gather", "factor", "solve", "conv", "trunc", "total", "iterations"]
+        return dict(zip(keys, [int(x) for x in a]))
+
+    def eval_bench(self, point: Point, types: int, reps: int = 10, blocks: int = 0) -> float:
+        """Device seconds of `reps` grid-wide evaluations of the selected
+        device types (ngsf_eval_bench)."""
+        sec = C.c_double()
+        if lib().ngsf_eval_bench(self._h, C.byref(point), int(types), int(reps), int(blocks),
+                                 C.byref(sec)):
+            raise EngineError(last_error())
+        return sec.value
+
     def workload(self) -> dict:
         a = (C.c_longlong * 10)()
         lib().ngsf_workload(self._h, a)
         keys = ["mos1", "res", "cap", "vsrc", "isrc", "nnz", "nlu", "n", "bsim4", "dio"]
         return dict(zip(keys, [int(x) for x in a]))
+
+
+def fp64_peak() -> float:
+    """Measured FP64 FMA throughput of the device, flop/s (ngsf_fp64_peak)."""
+    f = C.c_double()
+    if lib().ngsf_fp64_peak(C.byref(f)):
+        raise EngineError(last_error())
+    return f.value
 
 
 def last_launches() -> int:

@@ -33,6 +33,7 @@
  * Compile with floating-point contraction off (-ffp-contract=off) so that
  * x86-64 and Arm hosts evaluate every expression the same way.
  */
+#include <float.h>
 #include <math.h>
 #include <stdint.h>
 #include <stdlib.h>
@@ -1100,11 +1101,16 @@ static int ckt_load_devices(port_t *c)
 /* ------------------------------------------------------------------ */
 /* sparse refactorization on the planned pattern: left-looking, columns
  * in dependency-level order; fails (asking for new pivots) on a zero or
- * non-finite pivot or an L entry above 1e6 */
+ * non-finite pivot or a non-finite L entry, and in the operating point
+ * (MODEDCOP / MODETRANOP, where gmin and source stepping move the matrix
+ * far from the one the pivots were chosen on) also on an L entry above
+ * 1e6.  The transient refactors on its pivots like klu_refactor
+ * (src/maths/KLU/klusmp.c:591-602: only a zero pivot fails). */
 static int sp_factor(port_t *c)
 {
     port_plan_t *P = &c->plan;
     int n = c->n;
+    const double growth = (c->mode & (MODEDCOP | MODETRANOP)) ? 1e6 : DBL_MAX;
     double *lux = c->lux;
     memset(lux, 0, sizeof(double) * (size_t)P->nlu);
     for (int p = 0; p < c->nnz; p++)
@@ -1128,7 +1134,7 @@ static int sp_factor(port_t *c)
             for (int q2 = P->cdiag[k] + 1; q2 < P->cend[k]; q2++) {
                 double lik = lux[q2] / piv;
                 lux[q2] = lik;
-                if (!(fabs(lik) <= 1e6))
+                if (!(fabs(lik) <= growth))
                     return E_SINGULAR;
             }
         }

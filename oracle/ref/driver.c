@@ -2,6 +2,7 @@
  * Test infrastructure: batch driver for the reference ngspice transient path.
  *
  *   ngspice_ref NETLIST OUT.bin [--iters ITERS.bin] [--max-iters N]
+ *               [--states STATES.bin] [--states-every K]
  *
  * Reads a flat netlist (no .subckt, no .param, no braces), hands its cards
  * to the reference parser passes INPpas1/INPpas2/INPpas4/INPpas3 in the order
@@ -14,6 +15,17 @@
  * (captured just before the reference factors them, through the linker
  * wrappers __wrap_SMPluFac / __wrap_SMPreorder) are written to ITERS.bin,
  * up to N iterations (default 2000).
+ *
+ * With --states STATES.bin [--states-every K], every K-th captured
+ * iteration also records the linearisation point CKTload started from:
+ * CKTstates[0..2] as they were before the load (__wrap_CKTload snapshots
+ * them; the load itself writes state 0, and state 1 in MODEINITTRAN),
+ * the integration coefficients, gmin, srcFact, and each BSIM4 instance's
+ * BSIM4von (kept between iterations for the gate-voltage limiting), in
+ * the model / instance list order CKTload visits.  Record layout:
+ *   int32 iteration index (0-based, as in ITERS.bin), int32 nstates,
+ *   int32 nvon, int32 0, double ag[2], deltaOld[2], gmin, srcFact,
+ *   nstates x double state0, state1, state2, nvon x double von.
  *
  * Output layout (little-endian):
  *   "NGOR" int32 version=1
@@ -37,6 +49,7 @@
 #include "ngspice/tskdefs.h"
 #include <ctype.h>
 
+#include "bsim4/bsim4def.h"
 #include "oracle_ref.h"
 
 extern IFsimulator *ft_sim;
@@ -52,6 +65,77 @@ static CKTcircuit *iter_ckt = NULL;
 
 int __real_SMPluFac(SMPmatrix *, double, double);
 int __real_SMPreorder(SMPmatrix *, double, double, double);
+int __real_CKTload(CKTcircuit *);
+
+/* linearisation point of the iteration being loaded (--states) */
+static FILE *states_fp = NULL;
+static long states_every = 1;
+static double *pre_st[3];
+static double *pre_von;
+static int pre_nst, pre_nvon, pre_cap_st, pre_cap_von, pre_valid;
+
+static void snapshot_states(CKTcircuit *ckt)
+{
+    int k, nv = 0;
+    int type = INPtypelook("BSIM4");
+    BSIM4model *model;
+    BSIM4instance *here;
+    pre_valid = 0;
+    if (ckt->CKTnumStates > pre_cap_st) {
+        for (k = 0; k < 3; k++)
+            pre_st[k] = TREALLOC(double, pre_st[k], ckt->CKTnumStates);
+        pre_cap_st = ckt->CKTnumStates;
+    }
+    pre_nst = ckt->CKTnumStates;
+    for (k = 0; k < 3; k++)
+        memcpy(pre_st[k], ckt->CKTstates[k], sizeof(double) * (size_t)pre_nst);
+    if (type >= 0)
+        for (model = (BSIM4model *)ckt->CKThead[type]; model; model = BSIM4nextModel(model))
+            for (here = BSIM4instances(model); here; here = BSIM4nextInstance(here)) {
+                if (nv >= pre_cap_von) {
+                    pre_cap_von = 2 * pre_cap_von + 64;
+                    pre_von = TREALLOC(double, pre_von, pre_cap_von);
+                }
+                pre_von[nv++] = here->BSIM4von;
+            }
+    pre_nvon = nv;
+    pre_valid = 1;
+}
+
+int __wrap_CKTload(CKTcircuit *ckt)
+{
+    if (states_fp && ckt == iter_ckt && iter_count < iter_max &&
+        iter_count % states_every == 0)
+        snapshot_states(ckt);
+    else
+        pre_valid = 0;
+    return __real_CKTload(ckt);
+}
+
+static void dump_states(CKTcircuit *ckt, long index)
+{
+    int32_t hdr[4];
+    double d[6];
+    if (!states_fp || !pre_valid)
+        return;
+    pre_valid = 0;
+    hdr[0] = (int32_t)index;
+    hdr[1] = pre_nst;
+    hdr[2] = pre_nvon;
+    hdr[3] = 0;
+    fwrite(hdr, sizeof(int32_t), 4, states_fp);
+    d[0] = ckt->CKTag[0];
+    d[1] = ckt->CKTag[1];
+    d[2] = ckt->CKTdeltaOld[0];
+    d[3] = ckt->CKTdeltaOld[1];
+    d[4] = ckt->CKTgmin;
+    d[5] = ckt->CKTsrcFact;
+    fwrite(d, sizeof(double), 6, states_fp);
+    fwrite(pre_st[0], sizeof(double), (size_t)pre_nst, states_fp);
+    fwrite(pre_st[1], sizeof(double), (size_t)pre_nst, states_fp);
+    fwrite(pre_st[2], sizeof(double), (size_t)pre_nst, states_fp);
+    fwrite(pre_von, sizeof(double), (size_t)pre_nvon, states_fp);
+}
 
 /* Writes one record: time, delta, mode, order, n, nnz, then nnz x
  * (int32 row, int32 col, double value) in external 1-based equation
@@ -99,6 +183,7 @@ static void dump_iteration(SMPmatrix *m, const char *kind)
     }
     fwrite(ckt->CKTrhs, sizeof(double), (size_t)k->KLUmatrixNrhs + 1, iter_fp);
     fwrite(ckt->CKTrhsOld, sizeof(double), (size_t)k->KLUmatrixNrhs + 1, iter_fp);
+    dump_states(ckt, iter_count - 1);
 }
 
 int __wrap_SMPluFac(SMPmatrix *m, double pivtol, double gmin)
@@ -237,6 +322,7 @@ int main(int argc, char **argv)
     TSKtask *task = NULL;
     JOB *opt = NULL;
     const char *iters_path = NULL;
+    const char *states_path = NULL;
 
     if (argc < 3) {
         fprintf(stderr, "usage: %s NETLIST OUT.bin [--iters ITERS.bin] [--max-iters N]\n", argv[0]);
@@ -247,6 +333,10 @@ int main(int argc, char **argv)
             iters_path = argv[++i];
         else if (!strcmp(argv[i], "--max-iters") && i + 1 < argc)
             iter_max = atol(argv[++i]);
+        else if (!strcmp(argv[i], "--states") && i + 1 < argc)
+            states_path = argv[++i];
+        else if (!strcmp(argv[i], "--states-every") && i + 1 < argc)
+            states_every = atol(argv[++i]) > 0 ? atol(argv[i]) : 1;
     }
 
     oracle_init();
@@ -288,10 +378,14 @@ int main(int argc, char **argv)
     if (iters_path) {
         iter_fp = fopen(iters_path, "wb");
         iter_ckt = ckt;
+        if (states_path)
+            states_fp = fopen(states_path, "wb");
     }
     err = ft_sim->doAnalyses(ckt, 1, task);
     if (iter_fp)
         fclose(iter_fp);
+    if (states_fp)
+        fclose(states_fp);
     if (err)
         fprintf(stderr, "oracle: doAnalyses returned %d\n", err);
     write_trace(argv[2], ckt, err);

@@ -36,18 +36,37 @@ from ngspice_gb300 import netlists  # noqa: E402
 
 REF_BIN = os.path.join(ROOT, "oracle", "_ref", "ngspice_ref")
 
-# name -> (netlist text, number of Newton iterations to capture)
+# name -> (netlist text, number of Newton iterations to capture, record the
+# linearisation point of every k-th captured iteration (0: none))
 CASES = {
-    "inverter_chain32": (netlists.inverter_chain(), 400),
-    "mos1_mix": (netlists.mos1_mix(), 300),
-    "rc_ladder": (netlists.rc_ladder(), 200),
-    "diode_rectifier": (netlists.diode_rectifier(), 300),
+    "inverter_chain32": (netlists.inverter_chain(), 400, 0),
+    "mos1_mix": (netlists.mos1_mix(), 300, 0),
+    "rc_ladder": (netlists.rc_ladder(), 200, 0),
+    "diode_rectifier": (netlists.diode_rectifier(), 300, 0),
     "bsim4_logic_s3": (netlists.random_logic(n_transistors=120, seed=3, n_inputs=6,
-                                             tstop="1n"), 200),
-    "bsim4_chain8": (None, 200),
+                                             tstop="1n"), 200, 4),
+    "bsim4_chain8": (None, 200, 1),
     # one Monte Carlo instance: per-device mismatch model cards
     "bsim4_mc_s5": (netlists.random_logic(n_transistors=120, seed=5, n_inputs=6,
-                                          tstop="600p", mismatch=True), 150),
+                                          tstop="600p", mismatch=True), 150, 5),
+}
+
+# Circuits at the sizes the benchmarks run, with no iteration capture:
+# accepted points, statistics, and the waveforms of NPROBE unknowns spread
+# evenly over the equation numbering.
+#   c1_10k_30p   the 10,000-transistor random-logic netlist of the plain
+#                drop-in benchmark, first 30 ps of its transient
+#   mc_1k/2k/3k  Monte Carlo instances (device mismatch) of about 1,000,
+#                2,000 and 3,000 transistors, first 50 ps
+NPROBE = 256
+LARGE_CASES = {
+    "c1_10k_30p": lambda: netlists.random_logic(n_transistors=10000, seed=1, tstop="30p"),
+    "mc_1k_50p": lambda: netlists.random_logic(n_transistors=1000, seed=101, tstop="50p",
+                                               mismatch=True),
+    "mc_2k_50p": lambda: netlists.random_logic(n_transistors=2000, seed=102, tstop="50p",
+                                               mismatch=True),
+    "mc_3k_50p": lambda: netlists.random_logic(n_transistors=3000, seed=103, tstop="50p",
+                                               mismatch=True),
 }
 
 
@@ -121,19 +140,49 @@ def read_iters(path: str) -> dict:
             "it_rhsold": np.stack(rhsold) if rhsold else np.zeros((0, 1))}
 
 
-def run_reference(text: str, iters: int, workdir: str) -> dict:
+def read_states(path: str) -> dict:
+    """Linearisation points of the selected iterations (driver --states)."""
+    b = open(path, "rb").read()
+    o = 0
+    idx, scal, st, von = [], [], [], []
+    while o < len(b):
+        i, nst, nvon, _ = struct.unpack_from("<4i", b, o)
+        o += 16
+        scal.append(struct.unpack_from("<6d", b, o))
+        o += 48
+        st.append(np.frombuffer(b, "<f8", 3 * nst, o).reshape(3, nst).copy())
+        o += 24 * nst
+        von.append(np.frombuffer(b, "<f8", nvon, o).copy())
+        o += 8 * nvon
+        idx.append(i)
+    if not idx:
+        return {}
+    return {"st_iter": np.array(idx, np.int32),
+            "st_scal": np.array(scal),          # ag0, ag1, deltaOld0, deltaOld1, gmin, srcFact
+            "st_states": np.stack(st),          # [k][3][nstates] before the load
+            "st_von": np.stack(von)}            # [k][BSIM4 instances]
+
+
+def run_reference(text: str, iters: int, workdir: str, states_every: int = 0,
+                  keep_iters: bool = True) -> dict:
     cir = os.path.join(workdir, "case.cir")
     out = os.path.join(workdir, "case.bin")
     itf = os.path.join(workdir, "case.iters")
+    stf = os.path.join(workdir, "case.states")
     with open(cir, "w") as f:
         f.write(text)
     cmd = [REF_BIN, cir, out, "--iters", itf, "--max-iters", str(iters)]
+    if states_every > 0:
+        cmd += ["--states", stf, "--states-every", str(states_every)]
     p = subprocess.run(cmd, capture_output=True, text=True,
                        env=dict(os.environ, ORACLE_NUM_THREADS="1"))
     if p.returncode != 0:
         raise RuntimeError(f"reference failed ({p.returncode}): {p.stderr[-2000:]}")
     res = read_trace(out)
-    res.update(read_iters(itf))
+    if keep_iters:
+        res.update(read_iters(itf))
+    if states_every > 0:
+        res.update(read_states(stf))
     return res
 
 
@@ -143,17 +192,32 @@ def main(argv: list[str]) -> int:
         return 2
     only = set(argv[1:])
     with tempfile.TemporaryDirectory() as wd:
-        for name, (text, iters) in CASES.items():
+        for name, (text, iters, every) in CASES.items():
             if only and name not in only:
                 continue
             if text is None:
                 text = bsim4_chain()
-            res = run_reference(text, iters, wd)
+            res = run_reference(text, iters, wd, states_every=every)
             res["netlist"] = np.array(text)
             path = os.path.join(HERE, f"{name}.npz")
             np.savez_compressed(path, **res)
             print(f"{name}: {len(res['times'])} points, stats={res['stats'].tolist()},"
                   f" {len(res['it_kind'])} iterations -> {os.path.getsize(path)} bytes")
+        for name, make in LARGE_CASES.items():
+            if only and name not in only:
+                continue
+            text = make()
+            res = run_reference(text, 0, wd, keep_iters=False)
+            nv = len(res["names"])
+            cols = np.unique(np.linspace(0, nv - 1, min(NPROBE, nv)).round().astype(int))
+            out = {"names": res["names"][cols], "cols": cols.astype(np.int32),
+                   "nvars": np.int32(nv), "times": res["times"],
+                   "values": res["values"][:, cols], "stats": res["stats"],
+                   "cpu_seconds": res["cpu_seconds"], "netlist": np.array(text)}
+            path = os.path.join(HERE, f"{name}.npz")
+            np.savez_compressed(path, **out)
+            print(f"{name}: {nv} unknowns, {len(res['times'])} points,"
+                  f" stats={res['stats'].tolist()} -> {os.path.getsize(path)} bytes")
     return 0
 
 

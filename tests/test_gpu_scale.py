@@ -1,0 +1,60 @@
+"""GPU: the CUDA engine against reference fixtures at benchmark scale.
+
+Same fixtures as tests/test_oracle_port_scale.py (the reference ngspice
+compiled from its own sources): the 10,000-transistor random-logic netlist
+over its first 30 ps -- alone in its call it runs over the whole grid --
+and Monte Carlo instances of about 1,000, 2,000 and 3,000 transistors over
+50 ps, each alone and all three together in one batched launch.  The
+engine must reproduce the reference's Newton and step counts, and every
+recorded waveform must stay within reltol=1e-3, vntol=1 uV, abstol=1 pA at
+every reference time point (the worst error is printed)."""
+import numpy as np
+import pytest
+
+from conftest import golden
+from tolerances import waveform_violation
+
+pytestmark = pytest.mark.gpu
+
+MC = ["mc_1k_50p", "mc_2k_50p", "mc_3k_50p"]
+
+
+@pytest.fixture(scope="module")
+def E(built_lib):
+    from ngspice_gb300 import engine
+    return engine
+
+
+def check(E, g, c, name):
+    r = c.results()
+    ref = g["stats"]
+    assert r[E.R_STATUS] == 0
+    assert (r[E.R_NUMITER], r[E.R_TRANITER], r[E.R_ACCEPTED], r[E.R_REJECTED]) == \
+        (ref[0], ref[1], ref[3], ref[4])
+    t, v = c.points()
+    assert len(t) == len(g["times"])
+    assert np.max(np.abs(t - g["times"])) <= 1e-9 * g["times"][-1]
+    w = waveform_violation(list(g["names"]), g["times"], g["values"], t, v)
+    print(f"{name}: worst waveform error {w:.2e} of the tolerance")
+    assert w < 1.0
+
+
+@pytest.mark.parametrize("name", MC + ["c1_10k_30p"])
+def test_engine_matches_reference_at_scale(E, name):
+    g = golden(name)
+    c = E.Circuit(str(g["netlist"]), probes=[str(x) for x in g["names"]], outcap=4096)
+    E.run([c])
+    check(E, g, c, name)
+
+
+def test_batched_instances_match_reference(E, monkeypatch):
+    """The three Monte Carlo instances in one batched launch (with the
+    early finishers held while the others re-pivot), against the
+    reference."""
+    monkeypatch.setenv("NGSF_HOLD", "1")
+    gs = [golden(n) for n in MC]
+    cs = [E.Circuit(str(g["netlist"]), probes=[str(x) for x in g["names"]], outcap=4096)
+          for g in gs]
+    E.run(cs)
+    for n, g, c in zip(MC, gs, cs):
+        check(E, g, c, n)

@@ -14,7 +14,7 @@ def declared_symbols():
     names = set()
     for h in ("sharedspice.h", "ngspice_gb300.h"):
         text = open(os.path.join(ROOT, "include", h)).read()
-        names |= set(re.findall(r"\b(ng[A-Za-z_]+)\s*\(", text))
+        names |= set(re.findall(r"\b(ng[A-Za-z0-9_]+)\s*\(", text))
     return {n for n in names if not n.startswith("ngcomplex")}
 
 

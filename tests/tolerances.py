@@ -58,3 +58,21 @@ def matrix_violation_dense(ref_rows, ref_cols, ref_vals, a):
     rowscale = np.max(np.abs(r), axis=1, keepdims=True)
     scale = np.maximum(np.maximum(np.abs(m), np.abs(r)), np.maximum(rowscale, 1e-300))
     return float(np.max(np.abs(m - r) / (1e-12 * scale)))
+
+
+def rhs_violation_rowscaled(ref_rows, ref_vals, ref_rhs, rhs, rhs_old):
+    """Largest |a-b| / (1e-12 * scale_i) over the right-hand-side entries
+    1..n, scale_i = max(|a_i|, |b_i|, rowscale_i * max|rhsOld|): a device's
+    right-hand-side term is a current such as cdreq = cd - gds*vds - gm*vgs,
+    a sum of conductance x voltage products, so the row's largest
+    conductance times the largest voltage bounds the terms that cancel.
+    ref_rows are the 0-based equation indices of the reference's matrix
+    entries; ref_rhs / rhs / rhs_old hold equations 1..n."""
+    n = len(ref_rhs)
+    rowscale = np.zeros(n)
+    np.maximum.at(rowscale, np.asarray(ref_rows), np.abs(np.asarray(ref_vals)))
+    vmax = max(float(np.max(np.abs(rhs_old))), 1e-300)
+    scale = np.maximum(np.maximum(np.abs(ref_rhs), np.abs(rhs)), rowscale * vmax)
+    scale = np.maximum(scale, 1e-300)
+    return float(np.max(np.abs(ref_rhs - rhs) / (1e-12 * scale)))
+
