@@ -275,6 +275,50 @@ def plain_sample(texts: list[str], sizes: list[int] | None, k: int) -> list[int]
     return [order[(2 * j + 1) * n // (2 * k)] for j in range(k)]
 
 
+class Windows:
+    """Steps of a windowed batched transient: step j advances every circuit
+    to the end of window j of the transient (ngsf_run_window), cycling: the
+    step after the last window starts fresh runs.  Returns per step the
+    device seconds and, per circuit, the accepted steps, Newton iterations
+    and rejected steps made in the window."""
+
+    def __init__(self, E, circuits, dt: float, tstop: float):
+        self.E, self.cs, self.dt, self.tstop = E, circuits, dt, tstop
+        self.nw = max(1, int(round(tstop / dt)))
+        self.j = 0
+        n = len(circuits)
+        self.prev = [(0, 0, 0)] * n
+        self.fresh = [True] * n
+
+    def step(self):
+        E = self.E
+        w = self.j % self.nw
+        t_end = (w + 1) * self.dt if w < self.nw - 1 else 2.0 * self.tstop
+        sec = E.run_window(self.cs, t_end)
+        gained = []
+        for i, c in enumerate(self.cs):
+            r = c.results()
+            st = int(r[E.R_STATUS])
+            if st not in (0, E.PAUSED):
+                raise SystemExit(f"engine status {st} on instance {i}")
+            now = (int(r[E.R_ACCEPTED]), int(r[E.R_NUMITER]), int(r[E.R_REJECTED]))
+            base = (0, 0, 0) if self.fresh[i] else self.prev[i]
+            gained.append(tuple(x - y for x, y in zip(now, base)))
+            self.prev[i] = now
+            self.fresh[i] = st == 0
+        self.j += 1
+        return sec, gained
+
+
+def seconds_of(t: str) -> float:
+    """A time with a SPICE scale suffix ("25p", "2n", "1e-9")."""
+    scale = {"f": 1e-15, "p": 1e-12, "n": 1e-9, "u": 1e-6, "m": 1e-3}
+    t = t.strip().lower()
+    if t and t[-1] in scale:
+        return float(t[:-1]) * scale[t[-1]]
+    return float(t)
+
+
 def engine_arm(args, texts, wdesc, rank, world) -> dict | None:
     from ngspice_gb300 import engine as E
     mc = args.workload in ("c2", "c4")
@@ -298,27 +342,42 @@ def engine_arm(args, texts, wdesc, rank, world) -> dict | None:
     circuits = open_all(texts)
     wls = [c.workload() for c in circuits]
     progress(f"compiled and uploaded {len(circuits)} circuits in {time.perf_counter() - tb:.1f} s")
+    tstop = seconds_of(args.tstop or DEFAULT_WINDOW[args.workload])
+    dt = seconds_of(args.window) if mc else tstop
+    win = Windows(E, circuits, dt, tstop) if mc else None
+
+    def one_step():
+        if win:
+            return win.step()
+        sec = E.run(circuits)
+        g = []
+        for i, c in enumerate(circuits):
+            r = c.results()
+            if r[E.R_STATUS] != 0:
+                raise SystemExit(f"engine status {r[E.R_STATUS]} on instance {i}")
+            g.append((int(r[E.R_ACCEPTED]), int(r[E.R_NUMITER]), int(r[E.R_REJECTED])))
+        return sec, g
+
     for k in range(args.warmup):
         tw = time.perf_counter()
-        sec = E.run(circuits)
+        sec, _ = one_step()
         progress(f"warm-up {k}: {sec:.3f} s device, {time.perf_counter() - tw:.1f} s wall,"
                  f" {E.last_launches()} launches")
+    first_timed_window = win.j if win else 0
     clocks = Clocks()
     dev_times, accepted, launches, rejected = [], 0, 0, 0
     iters_of = [0] * len(circuits)
     for _ in range(args.steps):
         flush_l2()
-        sec = E.run(circuits)
+        sec, g = one_step()
         dev_times.append(sec)
         launches += E.last_launches()
-        progress(f"step {len(dev_times) - 1}: {sec:.3f} s device, {E.last_launches()} launches")
-        for i, c in enumerate(circuits):
-            r = c.results()
-            if r[E.R_STATUS] != 0:
-                raise SystemExit(f"engine status {r[E.R_STATUS]} on instance {i}")
-            accepted += int(r[E.R_ACCEPTED])
-            rejected += int(r[E.R_REJECTED])
-            iters_of[i] += int(r[E.R_NUMITER])
+        for i, (a, it, rj) in enumerate(g):
+            accepted += a
+            iters_of[i] += it
+            rejected += rj
+        progress(f"step {len(dev_times) - 1}: {sec:.3f} s device, {E.last_launches()} launches,"
+                 f" {sum(x[0] for x in g)} accepted steps")
     clk = clocks.stop()
     iters = sum(iters_of)
     moved = sum(bytes_per_iteration(w) * k for w, k in zip(wls, iters_of))
@@ -334,67 +393,88 @@ def engine_arm(args, texts, wdesc, rank, world) -> dict | None:
     else:
         accepted_all = accepted
     value = accepted_all / total
+    lu_madds = [c.lu_flops() for c in circuits]
     del circuits
 
-    # e2e: host netlist text -> compile/upload -> run -> accepted points on host
-    t0 = time.perf_counter()
-    h2d = d2h = 0
-    e2e_acc = 0
-    cs = open_all(texts)
-    E.run(cs)
-    for c in cs:
-        tt, vv = c.points()
-        d2h += tt.nbytes + vv.nbytes
-        e2e_acc += int(c.results()[E.R_ACCEPTED])
-        h2d += c.device_bytes()
-    del cs
-    e2e_time = time.perf_counter() - t0
-    progress(f"end-to-end pass: {e2e_time:.1f} s wall")
+    # e2e: host netlist text -> compile/upload -> run -> accepted points on
+    # host, through the public C ABI (a Monte Carlo batch over the first
+    # e2e_window of its transient, operating point included)
+    def e2e_run(txts):
+        t0 = time.perf_counter()
+        h2d = d2h = acc = 0
+        cs = open_all(txts)
+        if mc:
+            E.run_window(cs, seconds_of(args.e2e_window))
+        else:
+            E.run(cs)
+        for c in cs:
+            tt, vv = c.points()
+            d2h += tt.nbytes + vv.nbytes
+            acc += int(c.results()[E.R_ACCEPTED])
+            h2d += c.device_bytes()
+        del cs
+        return acc, time.perf_counter() - t0, h2d, d2h
+
+    e2e_acc, e2e_time, h2d, d2h = e2e_run(texts)
+    progress(f"end-to-end pass: {e2e_time:.1f} s wall, {e2e_acc} accepted steps")
     e2e = {"value": world * e2e_acc / e2e_time, "unit": UNIT,
            "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-           "includes": "netlist compile, symbolic analysis, upload, run, read-back"}
+           "includes": "netlist compile, symbolic analysis, upload, run, read-back"
+                       + (f"; the first {args.e2e_window} of every instance's transient"
+                          if mc else "")}
 
     out_extra = {}
     if mc and args.plain_sample > 0:
         # the plain drop-in on a sample of the same instances: one circuit
         # per call through the same C ABI (a circuit of >= 1024 transistors
-        # alone in a call runs over the whole grid), device time and wall
-        # time from netlist text
+        # alone in a call runs over the whole grid), timed over the same
+        # windows as the batched steps; and end to end over e2e_window
         os.environ["NGSF_HOLD"] = "0"
         idx = plain_sample(texts, wdesc.get("_sizes"), args.plain_sample)
-        p_acc = p_dev = p_wall = 0.0
+        p_acc = p_dev = 0.0
         p_iters = 0
-        for j, i in enumerate(idx):
-            tw = time.perf_counter()
+        pe_acc = pe_wall = 0.0
+        for i in idx:
             c = open_all([texts[i]])[0]
-            sec = E.run([c])
-            c.points()
-            wall = time.perf_counter() - tw
-            r = c.results()
-            if r[E.R_STATUS] != 0:
-                raise SystemExit(f"engine status {r[E.R_STATUS]} on plain instance {i}")
-            if j == 0:
-                # first call pays module warm-up: run it again for the time
-                sec = E.run([c])
-            p_acc += int(r[E.R_ACCEPTED])
-            p_iters += int(r[E.R_NUMITER])
-            p_dev += sec
-            p_wall += wall
-            progress(f"plain instance {i} ({wdesc['_sizes'][i]} transistors): {sec:.3f} s device,"
-                     f" {wall:.1f} s wall, {int(r[E.R_ACCEPTED])} steps")
+            pw = Windows(E, [c], dt, tstop)
+            for _ in range(first_timed_window):
+                pw.step()
+            sec_i = acc_i = 0
+            for _ in range(args.steps):
+                sec, g = pw.step()
+                sec_i += sec
+                acc_i += g[0][0]
+                p_iters += g[0][1]
             c.close()
+            a2, w2, _, _ = e2e_run([texts[i]])
+            p_acc += acc_i
+            p_dev += sec_i
+            pe_acc += a2
+            pe_wall += w2
+            progress(f"plain instance {i} ({wdesc['_sizes'][i]} transistors): {sec_i:.3f} s"
+                     f" device for {acc_i} steps; end to end {w2:.1f} s for {a2} steps")
+        os.environ["NGSF_HOLD"] = "1"
         plain = p_acc / p_dev
+        plain_e2e = pe_acc / pe_wall
         out_extra["forms"] = {
             "batched": {"value": value, "e2e": e2e["value"], "instances": len(texts)},
-            "plain_gpu": {"value": plain, "e2e": p_acc / p_wall, "instances": len(idx),
+            "plain_gpu": {"value": plain, "e2e": plain_e2e, "instances": len(idx),
                           "newton_iterations_per_accepted_step": p_iters / max(p_acc, 1),
                           "sample": f"{len(idx)} instances spread over the sorted sizes, each"
-                                    " alone in its own call (device time; e2e: wall time from"
-                                    " netlist text)"},
+                                    " alone in its own call, timed over the same windows as the"
+                                    " batched steps (device time); e2e from netlist text over"
+                                    f" the first {args.e2e_window}"},
             "batched_vs_plain": value / plain,
-            "batched_vs_plain_e2e": e2e["value"] / (p_acc / p_wall)}
+            "batched_vs_plain_e2e": e2e["value"] / plain_e2e}
+    if mc:
+        out_extra["windows"] = {
+            "window": args.window, "transient": args.tstop or DEFAULT_WINDOW[args.workload],
+            "timed": f"windows {first_timed_window}..{first_timed_window + args.steps - 1}"
+                     f" (cycling over {win.nw} windows of the transient; the window after the"
+                     " last one starts fresh runs)"}
 
     pk = peaks()
+    fp64_peak = E.fp64_peak()
     achieved = moved / total / 1e9
     kernel = "tran_wide_kernel" if (len(texts) <= 4 and wls[0]["bsim4"] + wls[0]["mos1"] >= 1024) \
         else "tran_kernel"
@@ -408,13 +488,25 @@ def engine_arm(args, texts, wdesc, rank, world) -> dict | None:
             "traffic": traffic, "traffic_unit": "bytes per Newton iteration" if traffic else None,
             "peak_source": pk["src"], "kernel": kernel,
             "algorithmic_bytes_per_newton_iteration": moved // max(iters, 1)}
+    # the binding roof: FP64.  Flops per Newton iteration: the BSIM4
+    # evaluations (FLOPS_BSIM4 each), the refactorization (2 per
+    # multiply-add of the circuit's pivot plan) and the two triangular
+    # solves (2 per L+U entry)
+    flops = sum(k * (FLOPS_BSIM4 * w["bsim4"] + 2.0 * lf + 2.0 * w["nlu"])
+                for w, k, lf in zip(wls, iters_of, lu_madds))
+    roof_fp64 = {"bound": "fp64", "achieved": flops / total / 1e12, "peak": fp64_peak / 1e12,
+                 "unit": "TFLOP/s", "frac": flops / total / fp64_peak, "traffic": None,
+                 "peak_source": "measured in this run: FP64 fused multiply-add chains on every"
+                                " SM (ngsf_fp64_peak); MEASURED_PEAKS.json holds no FP64 figure",
+                 "kernel": kernel, "flops_per_newton_iteration": flops / max(iters, 1),
+                 "flops_per_bsim4_evaluation": FLOPS_BSIM4}
     cfg = {k: v for k, v in wdesc.items() if not k.startswith("_")}
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
            "steps": args.steps, "warmup": args.warmup,
            "ms_per_step": 1e3 * total / args.steps,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
            "data": "synthetic", "config": cfg, "clocks": clk, "e2e": e2e,
-           "gpu_launches": launches, "roofline": roof,
+           "gpu_launches": launches, "roofline": roof_fp64, "roofline_hbm": roof,
            "newton_iterations_per_s": iters * world / total,
            "newton_iterations_per_accepted_step": iters / max(accepted, 1),
            "rejected_steps": rejected}
@@ -428,10 +520,13 @@ def engine_arm(args, texts, wdesc, rank, world) -> dict | None:
 
 # FP64 operations of one BSIM4 evaluation (default selectors, transient
 # Newton iteration): counted once with ncu over the grid-wide evaluation
-# kernel (sm__sass_thread_inst_executed_op_{dadd,dmul,dfma}_pred_on, fma
-# counted as 2) on the 10,000-transistor netlist, divided by the
-# evaluations; None until measured.
-FLOPS_BSIM4 = None
+# kernel on the 10,000-transistor netlist (python bench.py
+# --device-eval-only --eval-reps 1; sm__sass_thread_inst_executed_op_
+# {dadd,dmul,dfma}_pred_on = 7,974,223 + 11,682,109 + 23,174,884 FP64
+# instructions over 10,002 evaluations, a fused multiply-add counted as 2
+# flops): 6,599 flops in 4,282 FP64 instructions per evaluation.
+FLOPS_BSIM4 = 6599
+DP_INSTRUCTIONS_BSIM4 = 4282
 
 
 def device_eval(args) -> dict:
@@ -496,7 +591,12 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
     ap.add_argument("--workload", default="c2", choices=["c0", "c1", "c2", "c4"])
-    ap.add_argument("--plain-sample", type=int, default=8,
+    ap.add_argument("--window", default="25p",
+                    help="Monte Carlo workloads: a step advances every instance by this much of"
+                         " its transient")
+    ap.add_argument("--e2e-window", default="200p",
+                    help="Monte Carlo workloads: transient span of the end-to-end pass")
+    ap.add_argument("--plain-sample", type=int, default=4,
                     help="instances of a Monte Carlo workload timed through the plain drop-in")
     ap.add_argument("--instances", type=int, default=0,
                     help="instances per launch (default: 1216 for c0, 1 for c1, 1024 for c2)")
@@ -522,8 +622,10 @@ def main():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     args.instances = args.instances or DEFAULT_INSTANCES[args.workload]
     texts, tdesc = workload_texts(args.workload, args.tstop, args.instances)
+    steps_desc = (f", a step advances every instance by a {args.window} window of its"
+                  " transient" if args.workload in ("c2", "c4") else "")
     wdesc = {"workload": f"{args.workload.upper()}: {tdesc['circuit']}, {tdesc['tran']},"
-                         f" {args.instances} independent instance(s) per launch",
+                         f" {args.instances} independent instance(s) per launch{steps_desc}",
              "instances_per_gpu": args.instances, "l2": "flushed between timed steps",
              "parallelism": f"replicas x{world}", "_sizes": tdesc.get("sizes")}
     if args.impl == "reference":

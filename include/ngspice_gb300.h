@@ -69,6 +69,17 @@ NGSF_API int ngsf_probes(const ngsf_handle *h, int *eqs, int max);
 NGSF_API int ngsf_run(ngsf_handle *const *hs, int count, long long max_steps,
                       double *seconds);
 
+/* Windowed run (the reference's `stop when` / `resume`, src/spicelib/
+ * analysis/dctran.c:334-353 and :454-458): advance each circuit's
+ * transient to its first accepted point at or after t_until, then stop,
+ * keeping the whole run state on the device.  A circuit stopped by an
+ * earlier window continues where it stopped; any other starts a fresh
+ * run.  A stopped circuit reports status -3 (paused) in ngsf_results,
+ * with the points so far in ngsf_points; one that reached tstop reports
+ * 0.  ngsf_run always starts fresh. */
+NGSF_API int ngsf_run_window(ngsf_handle *const *hs, int count, double t_until,
+                             long long max_steps, double *seconds);
+
 /* results: ires[14] (status, npoints, accepted, rejected, numIter,
  * tranIter, timePts, ncap, opIter, badPivot, reorders, and with a Newton
  * predictor: steps started from its guess, of those accepted after the
@@ -116,9 +127,10 @@ NGSF_API long long ngsf_device_bytes(const ngsf_handle *h);
  * - nothing in the static array has to start at zero: the launch clears the
  *   state vectors, right-hand sides and per-instance memories itself, and
  *   every device rewrites all of its stamp slots;
- * - the first call on a device looks the static array up
- *   (cudaGetSymbolAddress, with that device current) and keeps the address;
- *   make that first call before any stream capture begins;
+ * - every call looks the static array up on the current device
+ *   (cudaGetSymbolAddress), so the address is right after a device reset
+ *   too; every call copies its results with blocking cudaMemcpy and ends
+ *   with cudaDeviceSynchronize, so make calls outside any stream capture;
  * - there is one static array per device: calls that overlap in time (from
  *   several threads, or while an earlier call's work is still running)
  *   race on it and must be serialised by the caller.

@@ -125,9 +125,12 @@ NGSF_API int ngsf_open_many(const char *const *netlists, int count, const char *
                                          (unsigned)std::max(1, count));
         std::vector<std::thread> pool;
         try {
+            /* room for every thread first: emplace_back then never
+             * reallocates while started threads are joinable */
+            pool.reserve(nt);
             for (unsigned k = 1; k < nt; k++)
                 pool.emplace_back(work);
-        } catch (const std::system_error &) {
+        } catch (...) {
             /* fewer threads: the calling thread takes the rest */
         }
         work();
@@ -215,6 +218,26 @@ NGSF_API int ngsf_run(ngsf_handle *const *hs, int count, long long max_steps, do
             cs.push_back(&hs[i]->p);
         }
         run_batch(cs, max_steps > 0 ? max_steps : 100000000LL, seconds, &g_launches);
+        return 0;
+    } catch (const std::exception &e) {
+        return fail(e.what());
+    }
+}
+
+NGSF_API int ngsf_run_window(ngsf_handle *const *hs, int count, double t_until,
+                            long long max_steps, double *seconds)
+{
+    try {
+        std::vector<Prepared *> cs;
+        for (int i = 0; i < count; i++) {
+            if (!hs[i])
+                return fail("null handle");
+            if (!hs[i]->p.dev)
+                return fail("circuit was compiled without a device (ngsf_compile)");
+            cs.push_back(&hs[i]->p);
+        }
+        run_batch(cs, max_steps > 0 ? max_steps : 100000000LL, seconds, &g_launches, t_until,
+                  true);
         return 0;
     } catch (const std::exception &e) {
         return fail(e.what());

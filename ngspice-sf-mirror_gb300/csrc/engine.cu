@@ -94,7 +94,7 @@ __device__ int block_or(Ctl &s, int v)
         s.redi[threadIdx.x >> 5] = m != 0;
     __syncthreads();
     int r = 0;
-    for (int w = 0; w < NGSF_WARPS; w++)
+    for (int w = 0; w < (int)(blockDim.x >> 5); w++)
         r |= s.redi[w];
     __syncthreads();
     return r;
@@ -108,7 +108,7 @@ __device__ double block_min(Ctl &s, double v)
         s.redd[threadIdx.x >> 5] = v;
     __syncthreads();
     double r = s.redd[0];
-    for (int w = 1; w < NGSF_WARPS; w++)
+    for (int w = 1; w < (int)(blockDim.x >> 5); w++)
         r = fmin(r, s.redd[w]);
     __syncthreads();
     return r;
@@ -908,6 +908,7 @@ __device__ void wide_issue(const ngsf_ckt_t &C, const Ctl &s, int cmd)
     w->done = 0;
     w->noncon = 0;
     w->bad = 0;
+    w->tmin = (unsigned long long)__double_as_longlong(1e300);
     const unsigned long long *src = (const unsigned long long *)&s;
     for (int k = 0; k < (int)((sizeof(Ctl) + 7) / 8); k++)
         w->ctl[k] = src[k];
@@ -1008,7 +1009,8 @@ __device__ int load_phase(const ngsf_ckt_t &C, Ctl &s, const Iter &it, int b, in
         prof_add(C, NGSF_P_LOAD, t0);
     const long long t1 = master ? prof_t(C) : 0;
     const int warp = threadIdx.x >> 5;
-    gather(C, it, t, T, b * NGSF_WARPS + warp, nb * NGSF_WARPS);
+    const int nw = blockDim.x >> 5;
+    gather(C, it, t, T, b * nw + warp, nb * nw);
     grid_sync(C, nb);
     if (master)
         prof_add(C, NGSF_P_GATHER, t1);
@@ -1016,6 +1018,8 @@ __device__ int load_phase(const ngsf_ckt_t &C, Ctl &s, const Iter &it, int b, in
 }
 
 __device__ int lu_factor_rl(const ngsf_ckt_t &C, Ctl &s, int b, int nb);
+__device__ double trunc_share(const ngsf_ckt_t &C, const Ctl &s, int t0, int T);
+__device__ void trunc_publish(const ngsf_ckt_t &C, double t);
 
 /* worker blocks: serve block 0's commands until EXIT (or a timeout) */
 __device__ void wide_worker(const ngsf_ckt_t &C, Ctl &s)
@@ -1052,6 +1056,10 @@ __device__ void wide_worker(const ngsf_ckt_t &C, Ctl &s)
             load_phase(C, s, it, blockIdx.x, gridDim.x, false);
         } else if (cmd == NGSF_WIDE_FACTOR) {
             lu_factor_rl(C, s, blockIdx.x, gridDim.x);
+        } else if (cmd == NGSF_WIDE_TRUNC) {
+            trunc_publish(C, block_min(s, trunc_share(C, s, blockIdx.x * blockDim.x + threadIdx.x,
+                                                      gridDim.x * blockDim.x)));
+            grid_sync(C, gridDim.x);
         }
         __syncthreads();
     }
@@ -1115,6 +1123,7 @@ __device__ __forceinline__ int rl_phase_work(const ngsf_ckt_t &C, int p)
     return w;
 }
 
+#define NGSF_RL_ILP 4
 __device__ int rl_phase(const ngsf_ckt_t &C, int p, int t, int T, double growth)
 {
     int bad = 0;
@@ -1124,20 +1133,65 @@ __device__ int rl_phase(const ngsf_ckt_t &C, int p, int t, int T, double growth)
             if (!(fabs(piv) > 0.0) || !isfinite(piv))
                 bad = 1;
         }
-        for (int d = C.ud_ptr[p] + t; d < C.ud_ptr[p + 1]; d += T) {
-            const int dst = C.ud_dst[d];
-            double acc = C.lux[dst];
-            for (int c = C.ud_cptr[d]; c < C.ud_cptr[d + 1]; c++)
-                acc -= (C.lux[C.ud_l[c]] / C.lux[C.ud_p[c]]) * C.lux[C.ud_u[c]];
-            C.lux[dst] = acc;
+        /* packed destinations, NGSF_RL_ILP of them in flight per thread:
+         * no destination of a phase is read by another entry of it */
+        const int d0 = C.ud_ptr[p], d1 = C.ud_ptr[p + 1];
+        for (int d = d0 + t; d < d1; d += NGSF_RL_ILP * T) {
+            int4 q[NGSF_RL_ILP];
+            int dst[NGSF_RL_ILP];
+            double a[NGSF_RL_ILP], x[NGSF_RL_ILP], v[NGSF_RL_ILP], y[NGSF_RL_ILP];
+#pragma unroll
+            for (int j = 0; j < NGSF_RL_ILP; j++) {
+                const int dj = d + j * T;
+                q[j] = dj < d1 ? ((const int4 *)C.ud_pk)[dj] : make_int4(0, 0, 0, 0);
+            }
+#pragma unroll
+            for (int j = 0; j < NGSF_RL_ILP; j++) {
+                dst[j] = q[j].x >= 0 ? q[j].x : -q[j].x - 1;
+                if (d + j * T < d1) {
+                    a[j] = C.lux[dst[j]];
+                    x[j] = C.lux[q[j].y];
+                    v[j] = C.lux[q[j].w];
+                    y[j] = C.lux[q[j].z];
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < NGSF_RL_ILP; j++)
+                if (d + j * T < d1) {
+                    double acc = a[j] - (x[j] / v[j]) * y[j];
+                    if (q[j].x < 0) {
+                        const int dj = d + j * T;
+                        for (int c = C.ud_cptr[dj] + 1; c < C.ud_cptr[dj + 1]; c++)
+                            acc -= (C.lux[C.ud_l[c]] / C.lux[C.ud_p[c]]) * C.lux[C.ud_u[c]];
+                    }
+                    C.lux[dst[j]] = acc;
+                }
         }
     }
     if (p > 0) {
-        for (int e = C.sc_ptr[p - 1] + t; e < C.sc_ptr[p]; e += T) {
-            double l_ik = C.lux[C.sc_pos[e]] / C.lux[C.sc_piv[e]];
-            C.lux[C.sc_pos[e]] = l_ik;
-            if (!(fabs(l_ik) <= growth))
-                bad = 1;
+        const int e0 = C.sc_ptr[p - 1], e1 = C.sc_ptr[p];
+        for (int e = e0 + t; e < e1; e += NGSF_RL_ILP * T) {
+            int2 q[NGSF_RL_ILP];
+            double x[NGSF_RL_ILP], v[NGSF_RL_ILP];
+#pragma unroll
+            for (int j = 0; j < NGSF_RL_ILP; j++) {
+                const int ej = e + j * T;
+                q[j] = ej < e1 ? ((const int2 *)C.sc_pk)[ej] : make_int2(-1, -1);
+            }
+#pragma unroll
+            for (int j = 0; j < NGSF_RL_ILP; j++)
+                if (q[j].x >= 0) {
+                    x[j] = C.lux[q[j].x];
+                    v[j] = C.lux[q[j].y];
+                }
+#pragma unroll
+            for (int j = 0; j < NGSF_RL_ILP; j++)
+                if (q[j].x >= 0) {
+                    const double l_ik = x[j] / v[j];
+                    C.lux[q[j].x] = l_ik;
+                    if (!(fabs(l_ik) <= growth))
+                        bad = 1;
+                }
         }
     }
     return bad;
@@ -1145,28 +1199,79 @@ __device__ int rl_phase(const ngsf_ckt_t &C, int p, int t, int T, double growth)
 
 /* One block: per level, the L entries of its pivots are divided first
  * (one division per entry), then the updates use the stored quotients;
- * the same quotients and products as rl_phase, two barriers per level. */
+ * the same quotients and products as rl_phase, two barriers per level.
+ * The packed descriptors (sc_pk, ud_pk) carry every index an entry needs
+ * in one load, and each thread keeps NGSF_RL_ILP entries' loads in flight
+ * before it stores: within a level no destination is read by another
+ * entry of the level, so the reordering changes no value. */
 __device__ int rl_level_block(const ngsf_ckt_t &C, int l, double growth)
 {
     int bad = 0;
-    for (int c = C.rl_ptr[l] + threadIdx.x; c < C.rl_ptr[l + 1]; c += blockDim.x) {
+    const int t = threadIdx.x, T = blockDim.x;
+    for (int c = C.rl_ptr[l] + t; c < C.rl_ptr[l + 1]; c += T) {
         double piv = C.lux[C.cdiag[C.rl_col[c]]];
         if (!(fabs(piv) > 0.0) || !isfinite(piv))
             bad = 1;
     }
-    for (int e = C.sc_ptr[l] + threadIdx.x; e < C.sc_ptr[l + 1]; e += blockDim.x) {
-        double l_ik = C.lux[C.sc_pos[e]] / C.lux[C.sc_piv[e]];
-        C.lux[C.sc_pos[e]] = l_ik;
-        if (!(fabs(l_ik) <= growth))
-            bad = 1;
+    {
+        const int e0 = C.sc_ptr[l], e1 = C.sc_ptr[l + 1];
+        for (int e = e0 + t; e < e1; e += NGSF_RL_ILP * T) {
+            int2 q[NGSF_RL_ILP];
+            double x[NGSF_RL_ILP], p[NGSF_RL_ILP];
+#pragma unroll
+            for (int j = 0; j < NGSF_RL_ILP; j++) {
+                const int ej = e + j * T;
+                q[j] = ej < e1 ? ((const int2 *)C.sc_pk)[ej] : make_int2(-1, -1);
+            }
+#pragma unroll
+            for (int j = 0; j < NGSF_RL_ILP; j++)
+                if (q[j].x >= 0) {
+                    x[j] = C.lux[q[j].x];
+                    p[j] = C.lux[q[j].y];
+                }
+#pragma unroll
+            for (int j = 0; j < NGSF_RL_ILP; j++)
+                if (q[j].x >= 0) {
+                    const double l_ik = x[j] / p[j];
+                    C.lux[q[j].x] = l_ik;
+                    if (!(fabs(l_ik) <= growth))
+                        bad = 1;
+                }
+        }
     }
     __syncthreads();
-    for (int d = C.ud_ptr[l] + threadIdx.x; d < C.ud_ptr[l + 1]; d += blockDim.x) {
-        const int dst = C.ud_dst[d];
-        double acc = C.lux[dst];
-        for (int c = C.ud_cptr[d]; c < C.ud_cptr[d + 1]; c++)
-            acc -= C.lux[C.ud_l[c]] * C.lux[C.ud_u[c]];
-        C.lux[dst] = acc;
+    {
+        const int d0 = C.ud_ptr[l], d1 = C.ud_ptr[l + 1];
+        for (int d = d0 + t; d < d1; d += NGSF_RL_ILP * T) {
+            int4 q[NGSF_RL_ILP];
+            int dst[NGSF_RL_ILP];
+            double a[NGSF_RL_ILP], x[NGSF_RL_ILP], y[NGSF_RL_ILP];
+#pragma unroll
+            for (int j = 0; j < NGSF_RL_ILP; j++) {
+                const int dj = d + j * T;
+                q[j] = dj < d1 ? ((const int4 *)C.ud_pk)[dj] : make_int4(0, 0, 0, 0);
+            }
+#pragma unroll
+            for (int j = 0; j < NGSF_RL_ILP; j++) {
+                dst[j] = q[j].x >= 0 ? q[j].x : -q[j].x - 1;
+                if (d + j * T < d1) {
+                    a[j] = C.lux[dst[j]];
+                    x[j] = C.lux[q[j].y];
+                    y[j] = C.lux[q[j].z];
+                }
+            }
+#pragma unroll
+            for (int j = 0; j < NGSF_RL_ILP; j++)
+                if (d + j * T < d1) {
+                    double acc = a[j] - x[j] * y[j];
+                    if (q[j].x < 0) {
+                        const int dj = d + j * T;
+                        for (int c = C.ud_cptr[dj] + 1; c < C.ud_cptr[dj + 1]; c++)
+                            acc -= C.lux[C.ud_l[c]] * C.lux[C.ud_u[c]];
+                    }
+                    C.lux[dst[j]] = acc;
+                }
+        }
     }
     __syncthreads();
     return bad;
@@ -1278,11 +1383,11 @@ __device__ int lu_factor(const ngsf_ckt_t &C, Ctl &s)
                 C.lux[C.a_lupos[C.a_diag[j]]] += s.diagGmin;
         __syncthreads();
     }
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
     const double growth = growth_limit(s);
     int bad = 0;
     for (int l = 0; l < C.nlevels; l++) {
-        for (int c = C.lvl_ptr[l] + warp; c < C.lvl_ptr[l + 1]; c += NGSF_WARPS) {
+        for (int c = C.lvl_ptr[l] + warp; c < C.lvl_ptr[l + 1]; c += nwarps) {
             int k = C.lvl_col[c];
             for (int t = C.kptr[k]; t < C.kptr[k + 1]; t++) {
                 double xk = C.lux[C.kpos[t]];
@@ -1319,6 +1424,96 @@ __device__ void solve_buffers_init(const ngsf_ckt_t &C, unsigned char *dyn, int 
     __syncthreads();
 }
 
+/* One thread's row of a triangular-solve level: its descriptor, the first
+ * NGSF_SOLVE_PF terms (factor value, column) and, for the backward solve,
+ * the pivot.  None of these change during a solve, so a row of level l+1
+ * is fetched before the barrier that ends level l, and the level itself
+ * then waits only on shared-memory reads of w. */
+#define NGSF_SOLVE_PF 6
+struct SolveRow {
+    int row, q0, q1;
+    double piv;
+    double v[NGSF_SOLVE_PF];
+    int c[NGSF_SOLVE_PF];
+};
+
+__device__ __forceinline__ void solve_fetch(SolveRow &p, const int4 *desc, int r, int rEnd,
+                                            const double *val, const int *col,
+                                            const double *lux, const int *cdiag, bool back)
+{
+    p.row = -1;
+    if (r < rEnd) {
+        const int4 d = desc[r];
+        if (d.z - d.y <= 32) {   /* longer rows are reduced by a warp */
+            p.row = d.x;
+            p.q0 = d.y;
+            p.q1 = d.z;
+#pragma unroll
+            for (int k = 0; k < NGSF_SOLVE_PF; k++)
+                if (d.y + k < d.z) {
+                    p.v[k] = val[d.y + k];
+                    p.c[k] = col[d.y + k];
+                }
+            if (back)
+                p.piv = lux[cdiag[d.x]];
+        }
+    }
+}
+
+/* w[row] -= the row's terms, in term order (then / pivot) */
+__device__ __forceinline__ void solve_apply(const SolveRow &p, double *w, const double *val,
+                                            const int *col, bool back)
+{
+    if (p.row < 0)
+        return;
+    double acc = w[p.row];
+#pragma unroll
+    for (int k = 0; k < NGSF_SOLVE_PF; k++)
+        if (p.q0 + k < p.q1)
+            acc -= p.v[k] * w[p.c[k]];
+    for (int q = p.q0 + NGSF_SOLVE_PF; q < p.q1; q++)
+        acc -= val[q] * w[col[q]];
+    w[p.row] = back ? acc / p.piv : acc;
+}
+
+/* One sweep (forward over L, or backward over U with the division by the
+ * pivot): per level, rows of up to 32 terms by one thread each, terms in
+ * order; longer rows (listed per level in hptr/hrow) by a warp, with
+ * lane-strided partial sums and a fixed butterfly. */
+__device__ void solve_sweep(const ngsf_ckt_t &C, double *w, int nlev, const int *lptr,
+                            const int4 *desc, const double *val, const int *col,
+                            const int *rptr, const int *hptr, const int *hrow, bool back)
+{
+    const int t = threadIdx.x, T = blockDim.x;
+    const int warp = t >> 5, lane = t & 31, nwarps = T >> 5;
+    SolveRow p;
+    p.row = -1;
+    if (nlev > 0)
+        solve_fetch(p, desc, lptr[0] + t, lptr[1], val, col, C.lux, C.cdiag, back);
+    for (int l = 0; l < nlev; l++) {
+        const int r1 = lptr[l + 1];
+        solve_apply(p, w, val, col, back);
+        for (int r = lptr[l] + t + T; r < r1; r += T) {
+            SolveRow q;
+            solve_fetch(q, desc, r, r1, val, col, C.lux, C.cdiag, back);
+            solve_apply(q, w, val, col, back);
+        }
+        for (int h = hptr[l] + warp; h < hptr[l + 1]; h += nwarps) {
+            const int k = hrow[h];
+            double acc = 0.0;
+            for (int q = rptr[k] + lane; q < rptr[k + 1]; q += 32)
+                acc += val[q] * w[col[q]];
+            for (int o = 16; o > 0; o >>= 1)
+                acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == 0)
+                w[k] = back ? (w[k] - acc) / C.lux[C.cdiag[k]] : w[k] - acc;
+        }
+        if (l + 1 < nlev)
+            solve_fetch(p, desc, r1 + t, lptr[l + 2], val, col, C.lux, C.cdiag, back);
+        __syncthreads();
+    }
+}
+
 /* SMPsolve: x = A^-1 b, in place on rhs (row-oriented, level scheduled). */
 __device__ void lu_solve(const ngsf_ckt_t &C, Ctl &s, double *rhs)
 {
@@ -1326,57 +1521,10 @@ __device__ void lu_solve(const ngsf_ckt_t &C, Ctl &s, double *rhs)
     for (int k = threadIdx.x; k < C.n; k += blockDim.x)
         w[k] = rhs[C.prow[k]];
     __syncthreads();
-    /* rows of up to 32 terms: one thread, terms in order; longer rows
-     * (listed per level in fh/bh): a warp, lane-strided partial sums and a
-     * fixed butterfly.  Row descriptors and values in term order keep the
-     * chain of dependent loads per row short. */
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int4 *fd = (const int4 *)C.fdesc, *bd = (const int4 *)C.bdesc;
-    for (int l = 0; l < C.nflevels; l++) {
-        for (int r = C.fl_ptr[l] + threadIdx.x; r < C.fl_ptr[l + 1]; r += blockDim.x) {
-            const int4 d = fd[r];
-            if (d.z - d.y > 32)
-                continue;
-            double acc = w[d.x];
-            for (int q = d.y; q < d.z; q++)
-                acc -= C.lval[q] * w[C.lr_col[q]];
-            w[d.x] = acc;
-        }
-        for (int h = C.fh_ptr[l] + warp; h < C.fh_ptr[l + 1]; h += NGSF_WARPS) {
-            int k = C.fh_row[h];
-            double acc = 0.0;
-            for (int q = C.lr_ptr[k] + lane; q < C.lr_ptr[k + 1]; q += 32)
-                acc += C.lval[q] * w[C.lr_col[q]];
-            for (int o = 16; o > 0; o >>= 1)
-                acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (lane == 0)
-                w[k] = w[k] - acc;
-        }
-        __syncthreads();
-    }
-    for (int l = 0; l < C.nblevels; l++) {
-        for (int r = C.bl_ptr[l] + threadIdx.x; r < C.bl_ptr[l + 1]; r += blockDim.x) {
-            const int4 d = bd[r];
-            if (d.z - d.y > 32)
-                continue;
-            const double piv = C.lux[C.cdiag[d.x]];
-            double acc = w[d.x];
-            for (int q = d.y; q < d.z; q++)
-                acc -= C.uval[q] * w[C.ur_col[q]];
-            w[d.x] = acc / piv;
-        }
-        for (int h = C.bh_ptr[l] + warp; h < C.bh_ptr[l + 1]; h += NGSF_WARPS) {
-            int k = C.bh_row[h];
-            double acc = 0.0;
-            for (int q = C.ur_ptr[k] + lane; q < C.ur_ptr[k + 1]; q += 32)
-                acc += C.uval[q] * w[C.ur_col[q]];
-            for (int o = 16; o > 0; o >>= 1)
-                acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (lane == 0)
-                w[k] = (w[k] - acc) / C.lux[C.cdiag[k]];
-        }
-        __syncthreads();
-    }
+    solve_sweep(C, w, C.nflevels, C.fl_ptr, (const int4 *)C.fdesc, C.lval, C.lr_col, C.lr_ptr,
+                C.fh_ptr, C.fh_row, false);
+    solve_sweep(C, w, C.nblevels, C.bl_ptr, (const int4 *)C.bdesc, C.uval, C.ur_col, C.ur_ptr,
+                C.bh_ptr, C.bh_row, true);
     for (int k = threadIdx.x; k < C.n; k += blockDim.x)
         rhs[C.pcol[k]] = w[k];
     __syncthreads();
@@ -1441,27 +1589,59 @@ __device__ double ckt_terr(const ngsf_ckt_t &C, const Ctl &s, int qcap, double t
     return NG_MIN(timeStep, del);
 }
 
-/* CKTtrunc: DEVtrunc over all charges, min-reduced. */
-__device__ double ckt_trunc(const ngsf_ckt_t &C, Ctl &s, double timeStep)
+/* DEVtrunc of the charges this thread owns (thread t0 of T): the smallest
+ * CKTterr step among them */
+__device__ double trunc_share(const ngsf_ckt_t &C, const Ctl &s, int t0, int T)
 {
     double t = 1e300;   /* HUGE */
-    for (int i = threadIdx.x; i < C.cap.n; i += blockDim.x)
+    for (int i = t0; i < C.cap.n; i += T)
         t = ckt_terr(C, s, C.cap.st[i], t);
-    for (int i = threadIdx.x; i < C.dio.n; i += blockDim.x)
+    for (int i = t0; i < C.dio.n; i += T)
         t = ckt_terr(C, s, C.dio.st[i] + DIS_CAPCHARGE, t);
-    for (int i = threadIdx.x; i < C.bsim4.n; i += blockDim.x) {
+    for (int i = t0; i < C.bsim4.n; i += T) {
         int b = C.bsim4.st[i];
         t = ckt_terr(C, s, b + B4S_QB, t);
         t = ckt_terr(C, s, b + B4S_QG, t);
         t = ckt_terr(C, s, b + B4S_QD, t);
     }
-    for (int i = threadIdx.x; i < C.mos1.n; i += blockDim.x) {
+    for (int i = t0; i < C.mos1.n; i += T) {
         int b = C.mos1.st[i];
         t = ckt_terr(C, s, b + M1S_QGS, t);
         t = ckt_terr(C, s, b + M1S_QGD, t);
         t = ckt_terr(C, s, b + M1S_QGB, t);
     }
-    t = block_min(s, t);
+    return t;
+}
+
+/* the block's smallest step folded into the grid's (wide launch) */
+__device__ void trunc_publish(const ngsf_ckt_t &C, double t)
+{
+    if (threadIdx.x == 0)
+        atomicMin(&C.wide->tmin, (unsigned long long)__double_as_longlong(t));
+}
+
+/* CKTtrunc: DEVtrunc over all charges, min-reduced (a minimum is exact,
+ * so the result does not depend on how the charges are shared out); in a
+ * wide launch every block takes its share. */
+__device__ double ckt_trunc(const ngsf_ckt_t &C, Ctl &s, double timeStep)
+{
+    double t;
+    if (C.wide) {
+        if (threadIdx.x == 0)
+            wide_issue(C, s, NGSF_WIDE_TRUNC);
+        t = block_min(s, trunc_share(C, s, threadIdx.x, gridDim.x * blockDim.x));
+        trunc_publish(C, t);
+        grid_sync(C, gridDim.x);
+        __shared__ double tmin;
+        if (threadIdx.x == 0)
+            tmin = __longlong_as_double(
+                (long long)*(volatile unsigned long long *)&C.wide->tmin);
+        __syncthreads();
+        t = tmin;
+        __syncthreads();
+    } else {
+        t = block_min(s, trunc_share(C, s, threadIdx.x, blockDim.x));
+    }
     return NG_MIN(2 * timeStep, t);
 }
 
@@ -2098,7 +2278,7 @@ __device__ int dc_tran(const ngsf_ckt_t &C, Ctl &s, long long maxSteps, bool res
 
     for (;;) {
         if (s.phase == PH_HELD) {
-            if (hold)
+            if (hold || s.time >= C.pause_at)
                 return NGSF_HELD;
             resume = false;
         } else if (s.phase == PH_NEXTTIME) {
@@ -2122,6 +2302,14 @@ __device__ int dc_tran(const ngsf_ckt_t &C, Ctl &s, long long maxSteps, bool res
                 return NGSF_OK;
             if (s.steps + 1 > maxSteps)
                 return NGSF_E_WATCHDOG;
+            if (s.time >= C.pause_at) {
+                /* end of a window: stop here; the next window resumes */
+                __syncthreads();   /* every warp has read time */
+                if (threadIdx.x == 0)
+                    s.phase = PH_HELD;
+                __syncthreads();
+                return NGSF_HELD;
+            }
             if (hold && s.accepted == 2) {
                 __syncthreads();   /* every warp has read accepted */
                 if (threadIdx.x == 0)
@@ -2355,6 +2543,8 @@ __device__ void run_circuit(const ngsf_ckt_t &C, Ctl &s, int runMode, long long 
 {
     const bool hold = (runMode & RUN_HOLD) != 0;
     runMode &= ~RUN_HOLD;
+    if (runMode == RUN_FRESH && C.run_resume)
+        runMode = RUN_RESUME;   /* the next window of a paused run */
     if (C.prof && threadIdx.x == 0 && runMode == RUN_FRESH)
         for (int k = 0; k < NGSF_P_COUNT; k++)
             C.prof[k] = 0;
@@ -2542,7 +2732,7 @@ __device__ int op_load(const ngsf_ckt_t &C, Ctl &s, const Iter &it, int types)
             for (int q = st[k] + t; q < st[k + 1]; q += T)
                 C.stampv[q] = 0.0;
     nc = block_or(s, nc);   /* includes __syncthreads: stamps visible */
-    gather(C, it, t, T, t >> 5, NGSF_WARPS);
+    gather(C, it, t, T, t >> 5, (int)(blockDim.x >> 5));
     __syncthreads();
     gather_heavy_combine(C, it);
     __syncthreads();
@@ -2709,27 +2899,19 @@ extern "C" void ngsf_internal_set_error(const char *msg);
 
 namespace {
 
-/* Device address of g_static_scratch, looked up once per device (with
- * that device current) and kept for later calls. */
-void *static_scratch(int dev, std::string &err)
+/* Device address of g_static_scratch on the current device, looked up on
+ * every call (cudaGetSymbolAddress allocates nothing and is cheap): a
+ * cached address would go stale when the module is reloaded after a
+ * cudaDeviceReset. */
+void *static_scratch(std::string &err)
 {
-    static std::mutex mu;
-    static void *addr[64] = {nullptr};
-    if (dev < 0 || dev >= 64) {
-        err = "device ordinal out of range";
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+    if (e != cudaSuccess) {
+        err = std::string("cudaGetSymbolAddress(static scratch): ") + cudaGetErrorString(e);
         return nullptr;
     }
-    std::lock_guard<std::mutex> lock(mu);
-    if (!addr[dev]) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
-        if (e != cudaSuccess) {
-            err = std::string("cudaGetSymbolAddress(static scratch): ") + cudaGetErrorString(e);
-            return nullptr;
-        }
-        addr[dev] = p;
-    }
-    return addr[dev];
+    return p;
 }
 
 }  // namespace
@@ -2768,14 +2950,8 @@ extern "C" NGSF_API int ngsf_stamp_initial_static(const ngsf_handle *h, double *
         ngsf_internal_set_error(m.c_str());
         return -1;
     }
-    int dev = 0;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) {
-        ngsf_internal_set_error(cudaGetErrorString(e));
-        return -1;
-    }
     std::string err;
-    unsigned char *base = (unsigned char *)static_scratch(dev, err);
+    unsigned char *base = (unsigned char *)static_scratch(err);
     if (!base) {
         ngsf_internal_set_error(err.c_str());
         return -1;
@@ -2797,8 +2973,10 @@ extern "C" NGSF_API int ngsf_stamp_initial_static(const ngsf_handle *h, double *
     c.wide = nullptr;
     c.pred.kind = 0;
     c.prof = nullptr;
+    c.pause_at = INFINITY;
+    c.run_resume = 0;
     stamp_static_kernel<<<1, NGSF_THREADS>>>(c);
-    e = cudaGetLastError();
+    cudaError_t e = cudaGetLastError();
     if (e == cudaSuccess && ax)
         e = cudaMemcpy(ax, c.ax, (size_t)d->nnz * sizeof(double), cudaMemcpyDeviceToHost);
     if (e == cudaSuccess && rhs)
@@ -2864,16 +3042,23 @@ extern "C" cudaError_t ngsf_launch_tran_wide(const ngsf_ckt_t *d_ckt, int nblock
                                        (size_t)solveCap + (size_t)gnnBytes, stream);
 }
 
+/* threads: 64, 128 or 256 per circuit block.  Every loop of the kernel is
+ * strided by the block size and every sum keeps its order, so the result
+ * does not depend on it; fewer threads let several circuits share an SM
+ * (255 registers a thread: two 128-thread blocks, or four 64-thread
+ * blocks). */
 extern "C" cudaError_t ngsf_launch_tran(const ngsf_ckt_t *d_ckts, const int *d_order, int nckt,
                                         int runMode, long long maxSteps, int solveCap,
-                                        int gnnBytes, cudaStream_t stream)
+                                        int gnnBytes, int threads, cudaStream_t stream)
 {
     if (nckt <= 0)
         return cudaSuccess;
+    if (threads != 64 && threads != 128)
+        threads = NGSF_THREADS;
     cudaError_t e = allow_dyn_smem((const void *)tran_kernel);
     if (e != cudaSuccess)
         return e;
-    tran_kernel<<<nckt, NGSF_THREADS, (size_t)solveCap + (size_t)gnnBytes, stream>>>(
+    tran_kernel<<<nckt, threads, (size_t)solveCap + (size_t)gnnBytes, stream>>>(
         d_ckts, d_order, nckt, runMode, maxSteps, solveCap, gnnBytes);
     return cudaGetLastError();
 }

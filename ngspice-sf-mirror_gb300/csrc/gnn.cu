@@ -134,6 +134,13 @@ gnn_gemm_kernel(const __nv_bfloat16 *A, int lda, const __nv_bfloat16 *B, int ldb
         if (failed)
             break;
     }
+    if (failed) {
+        /* a wait ran out while the committed products may still be
+         * running: wait for them once more (bounded) before the block
+         * frees the tensor memory they write; the result is discarded
+         * either way (err is set) */
+        __syncthreads_and(tc05_mbar_wait(bar, phase ^ 1u) ? 1 : 0);
+    }
     tc05_fence_after();
     if (!failed && any) {
         const int r = row0 + warp * 32 + lane;

@@ -160,7 +160,7 @@ typedef struct {
  * with device-scope release/acquire; every wait is bounded. */
 #define NGSF_WIDE_CTL_BYTES 1024
 #define NGSF_HCHUNK 1024
-enum { NGSF_WIDE_LOAD = 1, NGSF_WIDE_EXIT = 2, NGSF_WIDE_FACTOR = 3 };
+enum { NGSF_WIDE_LOAD = 1, NGSF_WIDE_EXIT = 2, NGSF_WIDE_FACTOR = 3, NGSF_WIDE_TRUNC = 4 };
 typedef struct {
     int seq;              /* command number, bumped by block 0 (release) */
     int cmd;              /* NGSF_WIDE_* */
@@ -171,6 +171,8 @@ typedef struct {
     unsigned long long bar;  /* grid barrier: arrivals since the launch */
     unsigned long long gen;  /* grid barrier: generations completed (last arriver) */
     unsigned long long fbar, fgen;  /* the same for the refactorization's block group */
+    unsigned long long tmin;        /* CKTtrunc: bits of the smallest step (positive doubles
+                                     * order like their bit patterns) */
     unsigned long long ctl[NGSF_WIDE_CTL_BYTES / 8];  /* block 0's control words */
 } ngsf_wide_t;
 
@@ -272,6 +274,13 @@ typedef struct {
     int rl_blocks, rl_small;
     const int *rl_ptr, *rl_col, *sc_ptr, *sc_pos, *sc_piv;
     const int *ud_ptr, *ud_dst, *ud_cptr, *ud_l, *ud_u, *ud_p;  /* ud_p: pivot pos */
+    /* the same schedule packed: per destination {lux pos, or -(pos + 1)
+     * when it receives more than one product, the first product's L pos,
+     * its U pos, its pivot pos}, further products at ud_l/ud_u/ud_p
+     * [ud_cptr[d] + 1 ..]; per L entry to divide {pos, pivot pos} (16- and
+     * 8-byte aligned groups of ints, read as int4 / int2) */
+    const int *ud_pk;
+    const int *sc_pk;
     double *work;         /* [n] solve workspace */
     /* matrix cells / rhs rows with more than NGSF_HEAVY contributions
      * (heavy[]) are summed in chunks of NGSF_HCHUNK contributions: chunk c
@@ -313,6 +322,11 @@ typedef struct {
     /* per-phase SM clock cycles of the circuit's block (NGSF_P_*), summed
      * over a run; null = not recorded */
     long long *prof;
+    /* windowed runs: the transient stops (NGSF_HELD) at the first accepted
+     * point at or after pause_at (+inf: runs to tstop); run_resume makes a
+     * launch continue the saved run instead of starting a fresh one */
+    double pause_at;
+    int run_resume;
 } ngsf_ckt_t;
 
 /* phases of the per-phase clock record */

@@ -27,6 +27,7 @@ __shared__ uint32_t g_tmem;                    /* 128 accumulator columns */
 __shared__ __align__(8) unsigned long long g_pbar;
 __shared__ unsigned char *g_psm;               /* staging, or null */
 __shared__ uint32_t g_pphase;
+__shared__ int g_ptmem;                        /* the block holds tensor memory */
 
 /* kernel start, all threads: tensor memory and the completion barrier for
  * a block that may run a circuit with a trained network (sm: the staging
@@ -37,6 +38,7 @@ __device__ void pred_block_init(unsigned char *sm)
     if (threadIdx.x == 0) {
         g_psm = sm;
         g_pphase = 0;
+        g_ptmem = on;
         if (on)
             tc05_mbar_init(tc05_smem_u32(&g_pbar), 1);
     }
@@ -52,7 +54,7 @@ __device__ void pred_block_fini()
 {
     tc05_fence_before();
     __syncthreads();
-    if (g_psm && threadIdx.x < 32)
+    if (g_ptmem && threadIdx.x < 32)
         tc05_tmem_dealloc(g_tmem, 128);
 }
 
@@ -99,6 +101,16 @@ __device__ bool pred_mma(int n, int kt)
     /* every thread waits on its own count: the block agrees on the
      * outcome, so all threads leave the product loops together */
     const bool ok = __syncthreads_and(tc05_mbar_wait(bar, g_pphase) ? 1 : 0) != 0;
+    if (!ok) {
+        /* the committed products may still be running: wait for them once
+         * more (bounded) before anything reuses the staging or the tensor
+         * memory; if they still have not finished, the network stays off
+         * for the rest of the launch (the plain start is used) */
+        const bool late = __syncthreads_and(tc05_mbar_wait(bar, g_pphase) ? 1 : 0) != 0;
+        if (!late && threadIdx.x == 0)
+            g_psm = nullptr;
+    }
+    __syncthreads();
     if (threadIdx.x == 0)
         g_pphase ^= 1u;
     tc05_fence_after();

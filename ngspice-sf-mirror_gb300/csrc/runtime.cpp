@@ -43,7 +43,7 @@ extern "C" cudaError_t ngsf_launch_tran_wide(const ngsf_ckt_t *d_ckt, int nblock
                                              cudaStream_t stream);
 extern "C" cudaError_t ngsf_launch_tran(const ngsf_ckt_t *d_ckts, const int *d_order, int nckt,
                                         int runMode, long long maxSteps, int solveCap,
-                                        int gnnBytes, cudaStream_t stream);
+                                        int gnnBytes, int threads, cudaStream_t stream);
 extern "C" int ngsf_ctl_bytes(void);
 
 namespace ngsf {
@@ -281,6 +281,8 @@ void DeviceCircuit::upload(const Image &img, const std::vector<int> &probes, int
     /* NGSF_PHASES=1: record per-phase clock cycles (ngsf_phase_cycles) */
     const char *ph = getenv("NGSF_PHASES");
     h.prof = (ph && atoi(ph) != 0) ? (long long *)(b + o.prof) : nullptr;
+    h.pause_at = INFINITY;
+    h.run_resume = 0;
     if (!impl->d_desc)
         ck(cudaMalloc(&impl->d_desc, sizeof(ngsf_ckt_t)), "cudaMalloc(desc)");
     ck(cudaMemcpy(impl->d_desc, &h, sizeof(h), cudaMemcpyHostToDevice), "cudaMemcpy(desc)");
@@ -288,6 +290,16 @@ void DeviceCircuit::upload(const Image &img, const std::vector<int> &probes, int
     nnz_ = nnz;
     outcap_ = outcap;
     capmax_ = capmax;
+}
+
+void DeviceCircuit::set_run(double pause_at, bool resume)
+{
+    ngsf_ckt_t &h = impl->h;
+    if (h.pause_at == pause_at && h.run_resume == (resume ? 1 : 0))
+        return;
+    h.pause_at = pause_at;
+    h.run_resume = resume ? 1 : 0;
+    ck(cudaMemcpy(impl->d_desc, &h, sizeof(h), cudaMemcpyHostToDevice), "cudaMemcpy(desc)");
 }
 
 void DeviceCircuit::set_factor_shape(int blocks, int small)
@@ -531,12 +543,13 @@ void DeviceCircuit::upload_lu(const Image &img)
     size_t o_fdesc = puti(fdesc), o_bdesc = puti(bdesc);
     size_t o_lval = put(nullptr, std::max<size_t>(1, img.lr_col.size()) * sizeof(double));
     size_t o_uval = put(nullptr, std::max<size_t>(1, img.ur_col.size()) * sizeof(double));
-    /* the right-looking schedule is used for large matrices (its two
-     * barriers per level beat a column's dependency chain); small ones keep
-     * the left-looking order.  NGSF_LU=rl / ll overrides. */
-    bool rl = img.n > 1000;
+    /* the right-looking schedule (two barriers per level, every
+     * destination of a level in parallel) is faster than the left-looking
+     * one (a column's dependency chain per warp) at every size measured;
+     * NGSF_LU=ll selects the left-looking one */
+    bool rl = img.n > 0;
     if (const char *e = getenv("NGSF_LU"))
-        rl = std::string(e) == "rl";
+        rl = std::string(e) != "ll";
     const std::vector<int> none;
     size_t o_rl_ptr = puti(rl ? img.rl_ptr : none), o_rl_col = puti(rl ? img.rl_col : none),
            o_sc_ptr = puti(rl ? img.sc_ptr : none), o_sc_pos = puti(rl ? img.sc_pos : none),
@@ -544,6 +557,25 @@ void DeviceCircuit::upload_lu(const Image &img)
            o_ud_dst = puti(rl ? img.ud_dst : none), o_ud_cptr = puti(rl ? img.ud_cptr : none),
            o_ud_l = puti(rl ? img.ud_l : none), o_ud_u = puti(rl ? img.ud_u : none),
            o_ud_p = puti(rl ? img.ud_p : none);
+    /* packed form of the right-looking schedule */
+    std::vector<int> ud_pk, sc_pk;
+    if (rl) {
+        ud_pk.resize(4 * img.ud_dst.size());
+        for (size_t d = 0; d < img.ud_dst.size(); d++) {
+            const int c0 = img.ud_cptr[d];
+            const bool more = img.ud_cptr[d + 1] - c0 > 1;
+            ud_pk[4 * d] = more ? -(img.ud_dst[d] + 1) : img.ud_dst[d];
+            ud_pk[4 * d + 1] = img.ud_l[c0];
+            ud_pk[4 * d + 2] = img.ud_u[c0];
+            ud_pk[4 * d + 3] = img.ud_p[c0];
+        }
+        sc_pk.resize(2 * img.sc_pos.size());
+        for (size_t e = 0; e < img.sc_pos.size(); e++) {
+            sc_pk[2 * e] = img.sc_pos[e];
+            sc_pk[2 * e + 1] = img.sc_piv[e];
+        }
+    }
+    size_t o_ud_pk = puti(ud_pk), o_sc_pk = puti(sc_pk);
     if (impl->lubase)
         cudaFree(impl->lubase);
     impl->lubase = nullptr;
@@ -606,6 +638,8 @@ void DeviceCircuit::upload_lu(const Image &img)
     h.ud_l = I(o_ud_l);
     h.ud_u = I(o_ud_u);
     h.ud_p = I(o_ud_p);
+    h.ud_pk = I(o_ud_pk);
+    h.sc_pk = I(o_sc_pk);
     ck(cudaMemcpy(impl->d_desc, &h, sizeof(h), cudaMemcpyHostToDevice), "cudaMemcpy(desc)");
 }
 
@@ -711,9 +745,16 @@ void prepare_device(Prepared &p, int outcap, int capmax)
  * get new pivots from the matrix they stamped and resume in the next
  * launch, until every circuit has finished. */
 int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *seconds,
-              int *launches)
+              int *launches, double pause_at, bool continuing)
 {
     std::vector<Prepared *> pending(cs.begin(), cs.end());
+    bool anyFresh = false;
+    for (auto *c : pending) {
+        const bool resume = continuing && c->paused;
+        anyFresh |= !resume;
+        c->dev->set_run(pause_at, resume);
+        c->paused = false;
+    }
     int mode = 0;   /* RUN_FRESH */
     /* a batch of many circuits fills the device with one block per
      * circuit; only a batch of a few runs its large circuits wide */
@@ -737,7 +778,8 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
      * the whole batch cost short launches; the batch then runs its time
      * loops together.  Off by default. */
     const bool holdPolicy = getenv("NGSF_HOLD") && atoi(getenv("NGSF_HOLD")) != 0;
-    bool holdNow = holdPolicy;
+    /* holding only matters while some circuit is still in its first step */
+    bool holdNow = holdPolicy && anyFresh;
     try {
         while (!pending.empty()) {
             if (nl > 256 + 8 * (int)cs.size())
@@ -771,9 +813,18 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
                               cudaMemcpyHostToDevice), "cudaMemcpy(order)");
                 const int solveCap = ngsf_solve_smem_bytes(maxn);
                 const int gnnBytes = ngsf_pred_smem_bytes(learned);
+                /* one 256-thread block per circuit (measured faster than
+                 * two 128-thread or four 64-thread circuits sharing an SM:
+                 * the refactorization and solves need the threads more than
+                 * the FP64-bound device evaluation needs a second circuit
+                 * to overlap with).  NGSF_BATCH_THREADS (64, 128, 256)
+                 * overrides; the result is the same */
+                int threads = 256;
+                if (const char *bt = getenv("NGSF_BATCH_THREADS"))
+                    threads = atoi(bt);
                 cudaEventRecord(e0, 0);
                 ck(ngsf_launch_tran(d, d_order, (int)descs.size(), mode | (holdNow ? 4 : 0),
-                                   maxSteps, solveCap, gnnBytes, 0), "launch(tran)");
+                                   maxSteps, solveCap, gnnBytes, threads, 0), "launch(tran)");
                 cudaEventRecord(e1, 0);
                 ck(cudaEventSynchronize(e1), "tran");
                 float ms = 0;
@@ -781,8 +832,8 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
                 total += ms * 1e-3;
                 nl++;
                 if (trace)
-                    fprintf(stderr, "ngsf: launch %d: %zu circuits, largest n %d,%s %.3f ms\n",
-                            nl, descs.size(), maxn, holdNow ? " hold," : "", ms);
+                    fprintf(stderr, "ngsf: launch %d: %zu circuits, largest n %d, %d threads,%s %.3f ms\n",
+                            nl, descs.size(), maxn, threads, holdNow ? " hold," : "", ms);
             }
             for (auto *c : wide) {
                 /* a fresh hand-over block per launch: command numbers start at 0 */
@@ -822,9 +873,12 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
                                 ax[c->img.a_diag[j]] += dg;
                     replan.push_back(c);
                     axs.push_back(std::move(ax));
-                } else if (c->ires[NGSF_R_STATUS] == NGSF_HELD) {
-                    next.push_back(c);
+                } else if (c->ires[NGSF_R_STATUS] == NGSF_HELD &&
+                           !(c->fres[NGSF_F_TIME] >= pause_at)) {
+                    next.push_back(c);   /* held after its first step */
                 } else {
+                    /* finished, failed, or stopped at the end of the window */
+                    c->paused = c->ires[NGSF_R_STATUS] == NGSF_HELD;
                     c->dev->read_points(c->ires[NGSF_R_NPOINTS], c->points);
                 }
             }
@@ -851,9 +905,12 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
                                                  (unsigned)std::max<size_t>(1, replan.size()));
                 std::vector<std::thread> pool;
                 try {
+                    /* room for every thread first: emplace_back then never
+                     * reallocates while started threads are joinable */
+                    pool.reserve(nt);
                     for (unsigned k = 1; k < nt; k++)
                         pool.emplace_back(work);
-                } catch (const std::system_error &) {
+                } catch (...) {
                     /* fewer threads: the calling thread takes the rest */
                 }
                 work();

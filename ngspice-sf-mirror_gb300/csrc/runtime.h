@@ -2,6 +2,7 @@
 #ifndef NGSF_RUNTIME_H
 #define NGSF_RUNTIME_H
 
+#include <math.h>
 #include <memory>
 #include <string>
 #include <vector>
@@ -28,6 +29,9 @@ public:
     void set_pred(const Image &img, int kind, const float *params);
     /* refactorization shape of a wide launch (0 = default) */
     void set_factor_shape(int blocks, int small);
+    /* windowed runs: stop at the first accepted point at or after pause_at;
+     * resume: continue the saved run instead of starting a fresh one */
+    void set_run(double pause_at, bool resume);
     const ngsf_ckt_t &desc() const;
     ngsf_ckt_t *device_desc() const;
     size_t bytes() const;
@@ -60,6 +64,7 @@ struct Prepared {
     std::vector<double> points;   /* [npoints][1 + nprobe] */
     bool wide = false;            /* run alone over a cooperative grid */
     int wide_blocks = 0;
+    bool paused = false;          /* stopped at the end of a window, resumable */
 };
 
 void prepare(Prepared &p, const std::string &netlist, const std::vector<std::string> &probes,
@@ -69,8 +74,12 @@ void prepare(Prepared &p, const std::string &netlist, const std::vector<std::str
  * allocate and upload on the calling thread's device */
 void prepare_host(Prepared &p, const std::string &netlist, const std::vector<std::string> &probes);
 void prepare_device(Prepared &p, int outcap, int capmax);
+/* Run the transients of cs.  pause_at: stop each circuit at its first
+ * accepted point at or after this time (+inf: run to tstop); continuing:
+ * circuits paused by an earlier window resume where they stopped, the
+ * others start fresh (otherwise every circuit starts fresh). */
 int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *seconds,
-              int *launches = nullptr);
+              int *launches = nullptr, double pause_at = INFINITY, bool continuing = false);
 
 }  // namespace ngsf
 

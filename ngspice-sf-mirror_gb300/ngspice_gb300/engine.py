@@ -24,7 +24,7 @@ F_COUNT = 3
 # C-ABI symbols declared in include/*.h
 EXPORTS = [
     "ngsf_open", "ngsf_open_many", "ngsf_compile", "ngsf_close", "ngsf_last_error", "ngsf_info",
-    "ngsf_eq_name", "ngsf_pattern", "ngsf_probes", "ngsf_run", "ngsf_results",
+    "ngsf_eq_name", "ngsf_pattern", "ngsf_probes", "ngsf_run", "ngsf_run_window", "ngsf_results",
     "ngsf_points", "ngsf_capture", "ngsf_lu_flops", "ngsf_device_bytes",
     "ngsf_last_launches", "ngsf_workload", "ngsf_stamp_initial_static",
     "ngsf_gnn_param_count", "ngsf_gnn_create", "ngsf_gnn_destroy", "ngsf_gnn_set_params",
@@ -109,6 +109,7 @@ def lib(path: str | None = None) -> C.CDLL:
     L.ngsf_pattern.argtypes = [vp, ip, ip]
     L.ngsf_probes.argtypes = [vp, ip, C.c_int]
     L.ngsf_run.argtypes = [C.POINTER(vp), C.c_int, C.c_longlong, dp]
+    L.ngsf_run_window.argtypes = [C.POINTER(vp), C.c_int, C.c_double, C.c_longlong, dp]
     L.ngsf_results.argtypes = [vp, ip, dp]
     L.ngsf_points.argtypes = [vp, dp, C.c_int]
     L.ngsf_capture.argtypes = [vp, dp, dp, dp, dp, C.c_int]
@@ -437,10 +438,25 @@ def tune_factor_shape(circuit: Circuit, blocks=(16, 24, 32, 48, 64, 96, 152),
     return {"blocks": best[0], "small_work": best[1], "timings": timings}
 
 
+# status of a circuit stopped at the end of a window (ngsf_run_window)
+PAUSED = -3
+
+
 def run(circuits: list[Circuit], max_steps: int = 0) -> float:
     """Run .tran on all circuits in one GPU launch; returns device seconds."""
     arr = (C.c_void_p * len(circuits))(*[c.handle for c in circuits])
     sec = C.c_double(0)
     if lib().ngsf_run(arr, len(circuits), int(max_steps), C.byref(sec)):
+        raise EngineError(last_error())
+    return sec.value
+
+
+def run_window(circuits: list[Circuit], t_until: float, max_steps: int = 0) -> float:
+    """Advance every circuit's transient to t_until (ngsf_run_window):
+    circuits stopped by an earlier window continue, the others start
+    fresh.  Returns device seconds."""
+    arr = (C.c_void_p * len(circuits))(*[c.handle for c in circuits])
+    sec = C.c_double(0)
+    if lib().ngsf_run_window(arr, len(circuits), float(t_until), int(max_steps), C.byref(sec)):
         raise EngineError(last_error())
     return sec.value

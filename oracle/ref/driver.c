@@ -382,6 +382,19 @@ int main(int argc, char **argv)
             states_fp = fopen(states_path, "wb");
     }
     err = ft_sim->doAnalyses(ckt, 1, task);
+    if (getenv("ORACLE_KLU_STATS") && ckt->CKTmatrix && ckt->CKTmatrix->CKTkluMODE &&
+        ckt->CKTmatrix->SMPkluMatrix) {
+        /* fill and flops of KLU's last factorization (BTF + AMD ordering) */
+        KLUmatrix *km = ckt->CKTmatrix->SMPkluMatrix;
+        if (km->KLUmatrixSymbolic && km->KLUmatrixNumeric) {
+            klu_flops(km->KLUmatrixSymbolic, km->KLUmatrixNumeric, km->KLUmatrixCommon);
+            fprintf(stderr, "oracle: klu n=%d nnz=%d nblocks=%d maxblock=%d nzoff=%d lnz=%d unz=%d"
+                    " flops=%.0f\n", (int)km->KLUmatrixN, (int)km->KLUmatrixNZ,
+                    km->KLUmatrixSymbolic->nblocks, km->KLUmatrixSymbolic->maxblock,
+                    km->KLUmatrixSymbolic->nzoff, km->KLUmatrixNumeric->lnz,
+                    km->KLUmatrixNumeric->unz, km->KLUmatrixCommon->flops);
+        }
+    }
     if (iter_fp)
         fclose(iter_fp);
     if (states_fp)

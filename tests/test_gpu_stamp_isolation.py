@@ -94,7 +94,7 @@ def test_smp_reorder_lufac_solve(E):
     ref = {(int(r), int(cc)): v for r, cc, v in zip(g["it_rows"][p0:p1], g["it_cols"][p0:p1],
                                                     g["it_vals"][p0:p1])}
     ax = np.array([ref[(int(ri[p]), j)] for j in range(n) for p in range(cp[j], cp[j + 1])])
-    b = g["it_rhs"][k].copy()
+    b = g["it_rhs"][k][:n + 1].copy()
 
     def dense(vals):
         A = np.zeros((n, n))
@@ -131,7 +131,7 @@ def test_convtest_and_trunc(E):
     x = g["it_rhsold"][-1]
     assert c.ni_convtest(x, x) == 0
     y = x.copy()
-    y[1] += 1e-3
+    y[1] += 1e-2 * max(1.0, abs(x[1]))
     assert c.ni_convtest(y, x) == 1
     # a transient iteration: the truncation-error step is positive and at
     # most twice the current step

@@ -130,9 +130,12 @@ def test_number_evaluation_matches_reference_rules():
 def test_port_sparse_planner_is_deterministic_and_pinned():
     """A 600-transistor Monte Carlo instance (612 unknowns) takes the
     port's sparse path, i.e. the same host pivot planner the engine uses
-    at every re-pivot.  Two runs are bit-identical, and the Newton, step
-    and re-pivot counts stay pinned: a planner change that alters a pivot
-    choice shows up here."""
+    at every re-pivot.  Two runs are bit-identical.  The Newton and step
+    counts (160 Newton iterations, 116 of them transient, 59 accepted
+    steps, none rejected) are the reference's own on this netlist (the
+    compiled reference ngspice-KLU gives exactly these); the re-pivot count
+    (6) is the port's and is a regression pin: a planner change that
+    alters how often the pivots are chosen shows up here."""
     from ngspice_gb300 import netlists
     text = netlists.random_logic(n_transistors=600, seed=7, tstop="15p", mismatch=True)
     a = port.simulate(text)
