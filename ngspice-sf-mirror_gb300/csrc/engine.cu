@@ -1104,175 +1104,107 @@ __device__ __forceinline__ double growth_limit(const Ctl &s)
 }
 
 /* Right-looking refactorization on the fixed pivot sequence, level by
- * level of the column dependency graph (large matrices).  Phase p applies
- * the updates of level p's pivot columns, each L entry divided by its
- * pivot where it is used, and stores the scaled L entries of level p-1
- * (which no update of level p reads or writes); one barrier per phase.
- * The quotient and products are the ones a divide-then-update sweep
- * computes, in the same order.  Over nb blocks of a wide launch (this is
- * block b) a phase with little work runs in block 0 alone and only the
- * change to a grid-wide phase costs a grid barrier. */
+ * level of the column dependency graph.  Level l first checks its pivots
+ * and scales the L entries of its pivot columns by the pivots' inverses,
+ * then every later entry receives the products L(i,k) * U(k,j) of the
+ * level's pivots, one thread per destination, products in a fixed order.
+ * FP64 is scarce on GB300 (a warp's division is about ten dependent
+ * fused multiply-adds), so a pivot is inverted once -- by the thread that
+ * writes its last update, or at the start when nothing updates it -- and
+ * the L entries and the backward solve multiply by the inverse; the
+ * products are fused multiply-adds.  The packed descriptors (sc_pk,
+ * ud_pk) carry every index an entry needs in one load, and each thread
+ * keeps NGSF_RL_ILP entries' loads in flight before it stores: within a
+ * level no destination is read by another entry of the level, so the
+ * reordering changes no value. */
 #define NGSF_RL_SMALL 1024
-__device__ __forceinline__ int rl_phase_work(const ngsf_ckt_t &C, int p)
-{
-    int w = 0;
-    if (p < C.rl_levels)
-        w += C.ud_ptr[p + 1] - C.ud_ptr[p] + C.rl_ptr[p + 1] - C.rl_ptr[p];
-    if (p > 0)
-        w += C.sc_ptr[p] - C.sc_ptr[p - 1];
-    return w;
-}
-
 #define NGSF_RL_ILP 4
-__device__ int rl_phase(const ngsf_ckt_t &C, int p, int t, int T, double growth)
+__device__ __forceinline__ int rl_level_work(const ngsf_ckt_t &C, int l)
 {
-    int bad = 0;
-    if (p < C.rl_levels) {
-        for (int c = C.rl_ptr[p] + t; c < C.rl_ptr[p + 1]; c += T) {
-            double piv = C.lux[C.cdiag[C.rl_col[c]]];
-            if (!(fabs(piv) > 0.0) || !isfinite(piv))
-                bad = 1;
-        }
-        /* packed destinations, NGSF_RL_ILP of them in flight per thread:
-         * no destination of a phase is read by another entry of it */
-        const int d0 = C.ud_ptr[p], d1 = C.ud_ptr[p + 1];
-        for (int d = d0 + t; d < d1; d += NGSF_RL_ILP * T) {
-            int4 q[NGSF_RL_ILP];
-            int dst[NGSF_RL_ILP];
-            double a[NGSF_RL_ILP], x[NGSF_RL_ILP], v[NGSF_RL_ILP], y[NGSF_RL_ILP];
-#pragma unroll
-            for (int j = 0; j < NGSF_RL_ILP; j++) {
-                const int dj = d + j * T;
-                q[j] = dj < d1 ? ((const int4 *)C.ud_pk)[dj] : make_int4(0, 0, 0, 0);
-            }
-#pragma unroll
-            for (int j = 0; j < NGSF_RL_ILP; j++) {
-                dst[j] = q[j].x >= 0 ? q[j].x : -q[j].x - 1;
-                if (d + j * T < d1) {
-                    a[j] = C.lux[dst[j]];
-                    x[j] = C.lux[q[j].y];
-                    v[j] = C.lux[q[j].w];
-                    y[j] = C.lux[q[j].z];
-                }
-            }
-#pragma unroll
-            for (int j = 0; j < NGSF_RL_ILP; j++)
-                if (d + j * T < d1) {
-                    double acc = a[j] - (x[j] / v[j]) * y[j];
-                    if (q[j].x < 0) {
-                        const int dj = d + j * T;
-                        for (int c = C.ud_cptr[dj] + 1; c < C.ud_cptr[dj + 1]; c++)
-                            acc -= (C.lux[C.ud_l[c]] / C.lux[C.ud_p[c]]) * C.lux[C.ud_u[c]];
-                    }
-                    C.lux[dst[j]] = acc;
-                }
-        }
-    }
-    if (p > 0) {
-        const int e0 = C.sc_ptr[p - 1], e1 = C.sc_ptr[p];
-        for (int e = e0 + t; e < e1; e += NGSF_RL_ILP * T) {
-            int2 q[NGSF_RL_ILP];
-            double x[NGSF_RL_ILP], v[NGSF_RL_ILP];
-#pragma unroll
-            for (int j = 0; j < NGSF_RL_ILP; j++) {
-                const int ej = e + j * T;
-                q[j] = ej < e1 ? ((const int2 *)C.sc_pk)[ej] : make_int2(-1, -1);
-            }
-#pragma unroll
-            for (int j = 0; j < NGSF_RL_ILP; j++)
-                if (q[j].x >= 0) {
-                    x[j] = C.lux[q[j].x];
-                    v[j] = C.lux[q[j].y];
-                }
-#pragma unroll
-            for (int j = 0; j < NGSF_RL_ILP; j++)
-                if (q[j].x >= 0) {
-                    const double l_ik = x[j] / v[j];
-                    C.lux[q[j].x] = l_ik;
-                    if (!(fabs(l_ik) <= growth))
-                        bad = 1;
-                }
-        }
-    }
-    return bad;
+    return C.ud_ptr[l + 1] - C.ud_ptr[l] + C.sc_ptr[l + 1] - C.sc_ptr[l];
 }
 
-/* One block: per level, the L entries of its pivots are divided first
- * (one division per entry), then the updates use the stored quotients;
- * the same quotients and products as rl_phase, two barriers per level.
- * The packed descriptors (sc_pk, ud_pk) carry every index an entry needs
- * in one load, and each thread keeps NGSF_RL_ILP entries' loads in flight
- * before it stores: within a level no destination is read by another
- * entry of the level, so the reordering changes no value. */
-__device__ int rl_level_block(const ngsf_ckt_t &C, int l, double growth)
+/* level l, first half (threads t of T): pivot checks, L(:,k) *= 1/U(k,k) */
+__device__ int rl_scale(const ngsf_ckt_t &C, int l, int t, int T, double growth)
 {
     int bad = 0;
-    const int t = threadIdx.x, T = blockDim.x;
     for (int c = C.rl_ptr[l] + t; c < C.rl_ptr[l + 1]; c += T) {
         double piv = C.lux[C.cdiag[C.rl_col[c]]];
         if (!(fabs(piv) > 0.0) || !isfinite(piv))
             bad = 1;
     }
-    {
-        const int e0 = C.sc_ptr[l], e1 = C.sc_ptr[l + 1];
-        for (int e = e0 + t; e < e1; e += NGSF_RL_ILP * T) {
-            int2 q[NGSF_RL_ILP];
-            double x[NGSF_RL_ILP], p[NGSF_RL_ILP];
+    const int e0 = C.sc_ptr[l], e1 = C.sc_ptr[l + 1];
+    for (int e = e0 + t; e < e1; e += NGSF_RL_ILP * T) {
+        int2 q[NGSF_RL_ILP];
+        double x[NGSF_RL_ILP], v[NGSF_RL_ILP];
 #pragma unroll
-            for (int j = 0; j < NGSF_RL_ILP; j++) {
-                const int ej = e + j * T;
-                q[j] = ej < e1 ? ((const int2 *)C.sc_pk)[ej] : make_int2(-1, -1);
+        for (int j = 0; j < NGSF_RL_ILP; j++) {
+            const int ej = e + j * T;
+            q[j] = ej < e1 ? ((const int2 *)C.sc_pk)[ej] : make_int2(-1, 0);
+        }
+#pragma unroll
+        for (int j = 0; j < NGSF_RL_ILP; j++)
+            if (q[j].x >= 0) {
+                x[j] = C.lux[q[j].x];
+                v[j] = C.uinv[q[j].y];
             }
 #pragma unroll
-            for (int j = 0; j < NGSF_RL_ILP; j++)
-                if (q[j].x >= 0) {
-                    x[j] = C.lux[q[j].x];
-                    p[j] = C.lux[q[j].y];
-                }
-#pragma unroll
-            for (int j = 0; j < NGSF_RL_ILP; j++)
-                if (q[j].x >= 0) {
-                    const double l_ik = x[j] / p[j];
-                    C.lux[q[j].x] = l_ik;
-                    if (!(fabs(l_ik) <= growth))
-                        bad = 1;
-                }
-        }
+        for (int j = 0; j < NGSF_RL_ILP; j++)
+            if (q[j].x >= 0) {
+                const double l_ik = x[j] * v[j];
+                C.lux[q[j].x] = l_ik;
+                if (!(fabs(l_ik) <= growth))
+                    bad = 1;
+            }
     }
+    return bad;
+}
+
+/* level l, second half: the updates (and the inverse of every pivot whose
+ * last update this is) */
+__device__ void rl_update(const ngsf_ckt_t &C, int l, int t, int T)
+{
+    const int d0 = C.ud_ptr[l], d1 = C.ud_ptr[l + 1];
+    for (int d = d0 + t; d < d1; d += NGSF_RL_ILP * T) {
+        int4 q[NGSF_RL_ILP];
+        int dst[NGSF_RL_ILP];
+        double a[NGSF_RL_ILP], x[NGSF_RL_ILP], y[NGSF_RL_ILP];
+#pragma unroll
+        for (int j = 0; j < NGSF_RL_ILP; j++) {
+            const int dj = d + j * T;
+            q[j] = dj < d1 ? ((const int4 *)C.ud_pk)[dj] : make_int4(0, 0, 0, -1);
+        }
+#pragma unroll
+        for (int j = 0; j < NGSF_RL_ILP; j++) {
+            dst[j] = q[j].x >= 0 ? q[j].x : -q[j].x - 1;
+            if (d + j * T < d1) {
+                a[j] = C.lux[dst[j]];
+                x[j] = C.lux[q[j].y];
+                y[j] = C.lux[q[j].z];
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < NGSF_RL_ILP; j++)
+            if (d + j * T < d1) {
+                double acc = fma(-x[j], y[j], a[j]);
+                if (q[j].x < 0) {
+                    const int dj = d + j * T;
+                    for (int c = C.ud_cptr[dj] + 1; c < C.ud_cptr[dj + 1]; c++)
+                        acc = fma(-C.lux[C.ud_l[c]], C.lux[C.ud_u[c]], acc);
+                }
+                C.lux[dst[j]] = acc;
+                if (q[j].w >= 0)
+                    C.uinv[q[j].w] = 1.0 / acc;
+            }
+    }
+}
+
+/* One block: a whole level, two barriers. */
+__device__ int rl_level_block(const ngsf_ckt_t &C, int l, double growth)
+{
+    const int bad = rl_scale(C, l, threadIdx.x, blockDim.x, growth);
     __syncthreads();
-    {
-        const int d0 = C.ud_ptr[l], d1 = C.ud_ptr[l + 1];
-        for (int d = d0 + t; d < d1; d += NGSF_RL_ILP * T) {
-            int4 q[NGSF_RL_ILP];
-            int dst[NGSF_RL_ILP];
-            double a[NGSF_RL_ILP], x[NGSF_RL_ILP], y[NGSF_RL_ILP];
-#pragma unroll
-            for (int j = 0; j < NGSF_RL_ILP; j++) {
-                const int dj = d + j * T;
-                q[j] = dj < d1 ? ((const int4 *)C.ud_pk)[dj] : make_int4(0, 0, 0, 0);
-            }
-#pragma unroll
-            for (int j = 0; j < NGSF_RL_ILP; j++) {
-                dst[j] = q[j].x >= 0 ? q[j].x : -q[j].x - 1;
-                if (d + j * T < d1) {
-                    a[j] = C.lux[dst[j]];
-                    x[j] = C.lux[q[j].y];
-                    y[j] = C.lux[q[j].z];
-                }
-            }
-#pragma unroll
-            for (int j = 0; j < NGSF_RL_ILP; j++)
-                if (d + j * T < d1) {
-                    double acc = a[j] - x[j] * y[j];
-                    if (q[j].x < 0) {
-                        const int dj = d + j * T;
-                        for (int c = C.ud_cptr[dj] + 1; c < C.ud_cptr[dj + 1]; c++)
-                            acc -= C.lux[C.ud_l[c]] * C.lux[C.ud_u[c]];
-                    }
-                    C.lux[dst[j]] = acc;
-                }
-        }
-    }
+    rl_update(C, l, threadIdx.x, blockDim.x);
     __syncthreads();
     return bad;
 }
@@ -1293,6 +1225,7 @@ __device__ void solve_pack(const ngsf_ckt_t &C, int t, int T)
 __device__ int lu_factor_rl(const ngsf_ckt_t &C, Ctl &s, int b, int nbAll)
 {
     int bad = 0;
+    const double growth = growth_limit(s);
     if (nbAll <= 1) {
         for (int q = threadIdx.x; q < C.nlu; q += blockDim.x)
             C.lux[q] = 0.0;
@@ -1307,12 +1240,17 @@ __device__ int lu_factor_rl(const ngsf_ckt_t &C, Ctl &s, int b, int nbAll)
                     C.lux[C.a_lupos[C.a_diag[j]]] += s.diagGmin;
             __syncthreads();
         }
-        const double growth = growth_limit(s);
+        for (int k = threadIdx.x; k < C.n; k += blockDim.x)
+            C.uinv[k] = 1.0 / C.lux[C.cdiag[k]];
+        __syncthreads();
         for (int l = 0; l < C.rl_levels; l++)
             bad |= rl_level_block(C, l, growth);
         solve_pack(C, threadIdx.x, blockDim.x);
         return block_or(s, bad);
     }
+    /* wide launch: a level with little work runs in block 0 alone (two
+     * block barriers); a larger one over the refactorization group (two
+     * group barriers), after one barrier that publishes block 0's levels */
     const int nb = min(nbAll, C.rl_blocks > 0 ? C.rl_blocks : NGSF_RL_BLOCKS);
     const int smallWork = C.rl_small > 0 ? C.rl_small : NGSF_RL_SMALL;
     if (b < nb) {
@@ -1331,24 +1269,27 @@ __device__ int lu_factor_rl(const ngsf_ckt_t &C, Ctl &s, int b, int nbAll)
                     C.lux[C.a_lupos[C.a_diag[j]]] += s.diagGmin;
             gsync();
         }
-        const int L = C.rl_levels;
-        const double growth = growth_limit(s);
-        bool small = rl_phase_work(C, 0) <= smallWork;
-        for (int p = 0; p <= L; p++) {
-            const bool nextSmall = p < L && rl_phase_work(C, p + 1) <= smallWork;
-            if (small) {
-                if (b == 0) {
-                    bad |= rl_phase(C, p, threadIdx.x, blockDim.x, growth);
-                    __syncthreads();
-                }
-                if (!nextSmall)
-                    gsync();
+        for (int k = t; k < C.n; k += T)
+            C.uinv[k] = 1.0 / C.lux[C.cdiag[k]];
+        gsync();
+        bool pending = false;   /* block 0 ran levels since the last group barrier */
+        for (int l = 0; l < C.rl_levels; l++) {
+            if (rl_level_work(C, l) <= smallWork) {
+                if (b == 0)
+                    bad |= rl_level_block(C, l, growth);
+                pending = true;
             } else {
-                bad |= rl_phase(C, p, t, T, growth);
+                if (pending)
+                    gsync();
+                pending = false;
+                bad |= rl_scale(C, l, t, T, growth);
+                gsync();
+                rl_update(C, l, t, T);
                 gsync();
             }
-            small = nextSmall;
         }
+        if (pending)
+            gsync();
         solve_pack(C, t, T);
     }
     bad = block_or(s, bad);
@@ -1408,6 +1349,8 @@ __device__ int lu_factor(const ngsf_ckt_t &C, Ctl &s)
         }
         __syncthreads();
     }
+    for (int k = threadIdx.x; k < C.n; k += blockDim.x)
+        C.uinv[k] = 1.0 / C.lux[C.cdiag[k]];
     solve_pack(C, threadIdx.x, blockDim.x);
     return block_or(s, bad);
 }
@@ -1426,7 +1369,7 @@ __device__ void solve_buffers_init(const ngsf_ckt_t &C, unsigned char *dyn, int 
 
 /* One thread's row of a triangular-solve level: its descriptor, the first
  * NGSF_SOLVE_PF terms (factor value, column) and, for the backward solve,
- * the pivot.  None of these change during a solve, so a row of level l+1
+ * pivot's inverse.  None of these change during a solve, so a row of level l+1
  * is fetched before the barrier that ends level l, and the level itself
  * then waits only on shared-memory reads of w. */
 #define NGSF_SOLVE_PF 6
@@ -1439,7 +1382,7 @@ struct SolveRow {
 
 __device__ __forceinline__ void solve_fetch(SolveRow &p, const int4 *desc, int r, int rEnd,
                                             const double *val, const int *col,
-                                            const double *lux, const int *cdiag, bool back)
+                                            const double *uinv, bool back)
 {
     p.row = -1;
     if (r < rEnd) {
@@ -1455,12 +1398,12 @@ __device__ __forceinline__ void solve_fetch(SolveRow &p, const int4 *desc, int r
                     p.c[k] = col[d.y + k];
                 }
             if (back)
-                p.piv = lux[cdiag[d.x]];
+                p.piv = uinv[d.x];
         }
     }
 }
 
-/* w[row] -= the row's terms, in term order (then / pivot) */
+/* w[row] -= the row's terms, in term order, fused (then x 1/pivot) */
 __device__ __forceinline__ void solve_apply(const SolveRow &p, double *w, const double *val,
                                             const int *col, bool back)
 {
@@ -1470,10 +1413,10 @@ __device__ __forceinline__ void solve_apply(const SolveRow &p, double *w, const 
 #pragma unroll
     for (int k = 0; k < NGSF_SOLVE_PF; k++)
         if (p.q0 + k < p.q1)
-            acc -= p.v[k] * w[p.c[k]];
+            acc = fma(-p.v[k], w[p.c[k]], acc);
     for (int q = p.q0 + NGSF_SOLVE_PF; q < p.q1; q++)
-        acc -= val[q] * w[col[q]];
-    w[p.row] = back ? acc / p.piv : acc;
+        acc = fma(-val[q], w[col[q]], acc);
+    w[p.row] = back ? acc * p.piv : acc;
 }
 
 /* One sweep (forward over L, or backward over U with the division by the
@@ -1489,27 +1432,27 @@ __device__ void solve_sweep(const ngsf_ckt_t &C, double *w, int nlev, const int 
     SolveRow p;
     p.row = -1;
     if (nlev > 0)
-        solve_fetch(p, desc, lptr[0] + t, lptr[1], val, col, C.lux, C.cdiag, back);
+        solve_fetch(p, desc, lptr[0] + t, lptr[1], val, col, C.uinv, back);
     for (int l = 0; l < nlev; l++) {
         const int r1 = lptr[l + 1];
         solve_apply(p, w, val, col, back);
         for (int r = lptr[l] + t + T; r < r1; r += T) {
             SolveRow q;
-            solve_fetch(q, desc, r, r1, val, col, C.lux, C.cdiag, back);
+            solve_fetch(q, desc, r, r1, val, col, C.uinv, back);
             solve_apply(q, w, val, col, back);
         }
         for (int h = hptr[l] + warp; h < hptr[l + 1]; h += nwarps) {
             const int k = hrow[h];
             double acc = 0.0;
             for (int q = rptr[k] + lane; q < rptr[k + 1]; q += 32)
-                acc += val[q] * w[col[q]];
+                acc = fma(val[q], w[col[q]], acc);
             for (int o = 16; o > 0; o >>= 1)
                 acc += __shfl_xor_sync(0xffffffffu, acc, o);
             if (lane == 0)
-                w[k] = back ? (w[k] - acc) / C.lux[C.cdiag[k]] : w[k] - acc;
+                w[k] = back ? (w[k] - acc) * C.uinv[k] : w[k] - acc;
         }
         if (l + 1 < nlev)
-            solve_fetch(p, desc, r1 + t, lptr[l + 2], val, col, C.lux, C.cdiag, back);
+            solve_fetch(p, desc, r1 + t, lptr[l + 2], val, col, C.uinv, back);
         __syncthreads();
     }
 }
@@ -3040,6 +2983,17 @@ extern "C" cudaError_t ngsf_launch_tran_wide(const ngsf_ckt_t *d_ckt, int nblock
     return cudaLaunchCooperativeKernel((const void *)tran_wide_kernel, dim3(nblocks),
                                        dim3(NGSF_THREADS), args,
                                        (size_t)solveCap + (size_t)gnnBytes, stream);
+}
+
+/* circuit blocks of the batched launch one SM holds at once */
+extern "C" int ngsf_tran_occupancy(int threads, int dynSmem)
+{
+    int per = 0;
+    if (allow_dyn_smem((const void *)tran_kernel) != cudaSuccess ||
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, tran_kernel, threads, dynSmem) !=
+            cudaSuccess)
+        return 0;
+    return per;
 }
 
 /* threads: 64, 128 or 256 per circuit block.  Every loop of the kernel is

@@ -276,12 +276,14 @@ typedef struct {
     const int *ud_ptr, *ud_dst, *ud_cptr, *ud_l, *ud_u, *ud_p;  /* ud_p: pivot pos */
     /* the same schedule packed: per destination {lux pos, or -(pos + 1)
      * when it receives more than one product, the first product's L pos,
-     * its U pos, its pivot pos}, further products at ud_l/ud_u/ud_p
-     * [ud_cptr[d] + 1 ..]; per L entry to divide {pos, pivot pos} (16- and
-     * 8-byte aligned groups of ints, read as int4 / int2) */
+     * its U pos, the pivot k when the destination is U(k,k) and this is its
+     * last update, else -1}, further products at ud_l/ud_u [ud_cptr[d] + 1
+     * ..]; per L entry to scale {pos, its column's pivot k} (16- and 8-byte
+     * aligned groups of ints, read as int4 / int2) */
     const int *ud_pk;
     const int *sc_pk;
     double *work;         /* [n] solve workspace */
+    double *uinv;         /* [n] 1 / U(k,k), written by the refactorization */
     /* matrix cells / rhs rows with more than NGSF_HEAVY contributions
      * (heavy[]) are summed in chunks of NGSF_HCHUNK contributions: chunk c
      * belongs to heavy entry hch_cell[c]; hch_ptr[h] is entry h's first

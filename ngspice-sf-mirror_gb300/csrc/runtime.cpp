@@ -45,6 +45,7 @@ extern "C" cudaError_t ngsf_launch_tran(const ngsf_ckt_t *d_ckts, const int *d_o
                                         int runMode, long long maxSteps, int solveCap,
                                         int gnnBytes, int threads, cudaStream_t stream);
 extern "C" int ngsf_ctl_bytes(void);
+extern "C" int ngsf_tran_occupancy(int threads, int dynSmem);
 
 namespace ngsf {
 
@@ -560,22 +561,30 @@ void DeviceCircuit::upload_lu(const Image &img)
     /* packed form of the right-looking schedule */
     std::vector<int> ud_pk, sc_pk;
     if (rl) {
+        /* column of each diagonal position, and each position's last
+         * destination entry (the schedule lists levels in order) */
+        std::vector<int> diagcol(std::max(1, img.nlu), -1), last(std::max(1, img.nlu), -1);
+        for (size_t k = 0; k < img.cdiag.size(); k++)
+            diagcol[img.cdiag[k]] = (int)k;
+        for (size_t d = 0; d < img.ud_dst.size(); d++)
+            last[img.ud_dst[d]] = (int)d;
         ud_pk.resize(4 * img.ud_dst.size());
         for (size_t d = 0; d < img.ud_dst.size(); d++) {
-            const int c0 = img.ud_cptr[d];
+            const int c0 = img.ud_cptr[d], dst = img.ud_dst[d];
             const bool more = img.ud_cptr[d + 1] - c0 > 1;
-            ud_pk[4 * d] = more ? -(img.ud_dst[d] + 1) : img.ud_dst[d];
+            ud_pk[4 * d] = more ? -(dst + 1) : dst;
             ud_pk[4 * d + 1] = img.ud_l[c0];
             ud_pk[4 * d + 2] = img.ud_u[c0];
-            ud_pk[4 * d + 3] = img.ud_p[c0];
+            ud_pk[4 * d + 3] = (diagcol[dst] >= 0 && last[dst] == (int)d) ? diagcol[dst] : -1;
         }
         sc_pk.resize(2 * img.sc_pos.size());
         for (size_t e = 0; e < img.sc_pos.size(); e++) {
             sc_pk[2 * e] = img.sc_pos[e];
-            sc_pk[2 * e + 1] = img.sc_piv[e];
+            sc_pk[2 * e + 1] = diagcol[img.sc_piv[e]];
         }
     }
     size_t o_ud_pk = puti(ud_pk), o_sc_pk = puti(sc_pk);
+    size_t o_uinv = put(nullptr, (size_t)std::max(1, img.n) * sizeof(double));
     if (impl->lubase)
         cudaFree(impl->lubase);
     impl->lubase = nullptr;
@@ -640,6 +649,7 @@ void DeviceCircuit::upload_lu(const Image &img)
     h.ud_p = I(o_ud_p);
     h.ud_pk = I(o_ud_pk);
     h.sc_pk = I(o_sc_pk);
+    h.uinv = (double *)(b + o_uinv);
     ck(cudaMemcpy(impl->d_desc, &h, sizeof(h), cudaMemcpyHostToDevice), "cudaMemcpy(desc)");
 }
 
@@ -832,8 +842,10 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
                 total += ms * 1e-3;
                 nl++;
                 if (trace)
-                    fprintf(stderr, "ngsf: launch %d: %zu circuits, largest n %d, %d threads,%s %.3f ms\n",
-                            nl, descs.size(), maxn, threads, holdNow ? " hold," : "", ms);
+                    fprintf(stderr, "ngsf: launch %d: %zu circuits, largest n %d, %d threads"
+                            " (%d blocks per SM),%s %.3f ms\n", nl, descs.size(), maxn, threads,
+                            ngsf_tran_occupancy(threads, solveCap + gnnBytes),
+                            holdNow ? " hold," : "", ms);
             }
             for (auto *c : wide) {
                 /* a fresh hand-over block per launch: command numbers start at 0 */
