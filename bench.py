@@ -342,6 +342,15 @@ def engine_arm(args, texts, wdesc, rank, world) -> dict | None:
     circuits = open_all(texts)
     wls = [c.workload() for c in circuits]
     progress(f"compiled and uploaded {len(circuits)} circuits in {time.perf_counter() - tb:.1f} s")
+    tuned = None
+    if len(circuits) == 1 and circuits[0].wide_info()[0] and not args.no_tune:
+        # one large circuit over the whole grid: the refactorization shape
+        # is autotuned over its level schedule (every shape gives the same
+        # bits); the tuning runs are short and untimed
+        tt = time.perf_counter()
+        tuned = E.tune_factor_shape(circuits[0])
+        progress(f"refactorization shape {tuned['blocks']} blocks, one-block levels up to"
+                 f" {tuned['small_work']} updates ({time.perf_counter() - tt:.1f} s)")
     tstop = seconds_of(args.tstop or DEFAULT_WINDOW[args.workload])
     dt = seconds_of(args.window) if mc else tstop
     win = Windows(E, circuits, dt, tstop) if mc else None
@@ -466,6 +475,9 @@ def engine_arm(args, texts, wdesc, rank, world) -> dict | None:
                                     f" the first {args.e2e_window}"},
             "batched_vs_plain": value / plain,
             "batched_vs_plain_e2e": e2e["value"] / plain_e2e}
+    if tuned:
+        out_extra["refactor_shape"] = {"blocks": tuned["blocks"],
+                                       "one_block_levels_up_to": tuned["small_work"]}
     if mc:
         out_extra["windows"] = {
             "window": args.window, "transient": args.tstop or DEFAULT_WINDOW[args.workload],
@@ -554,6 +566,38 @@ def device_eval(args) -> dict:
     return out
 
 
+def gnn_case(nodes: int, steps: int = 3) -> dict:
+    """Training steps of the predictor network on a seeded graph of `nodes`
+    nodes (6 random neighbours within a window of 100): the tcgen05
+    forward and backward products at a size a batched timestep feeds."""
+    from ngspice_gb300 import gnn as G, predictor
+    import numpy as np
+    rng = np.random.default_rng(0)
+    nbs = [set() for _ in range(nodes)]
+    for i in range(nodes):
+        for j in rng.integers(max(0, i - 50), min(nodes, i + 50), 6):
+            if int(j) != i:
+                nbs[i].add(int(j))
+                nbs[int(j)].add(i)
+    ptr, idx = [0], []
+    for i in range(nodes):
+        idx += sorted(nbs[i])
+        ptr.append(len(idx))
+    net = G.Net(np.array(ptr, np.int32), np.array(idx, np.int32))
+    net.set_params(predictor.init_params(0))
+    X = rng.standard_normal((nodes, G.F_IN)).astype(np.float32)
+    y = rng.standard_normal(nodes).astype(np.float32)
+    w = np.ones(nodes, np.float32)
+    t0 = time.perf_counter()
+    loss = None
+    for _ in range(steps):
+        loss, _ = net.train_step(X, y, w, 1e-3)
+    out = {"gnn_nodes": nodes, "steps": steps, "loss": float(loss),
+           "seconds": time.perf_counter() - t0}
+    net.close()
+    return out
+
+
 def phase_split(args, texts) -> None:
     """Per-phase clock split of one untimed run of the workload (circuits
     opened with NGSF_PHASES=1, so the timed runs carry no clock reads)."""
@@ -604,6 +648,8 @@ def main():
     ap.add_argument("--cpu-window", default="100p",
                     help="transient window of each Monte Carlo instance in the CPU sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-tune", action="store_true",
+                    help="skip the refactorization-shape autotuner of a single large circuit")
     ap.add_argument("--phases", action="store_true",
                     help="one extra untimed run with per-phase SM clock records: prints the"
                          " split of each circuit block's time (loads, gather, refactor, solves,"
@@ -613,6 +659,10 @@ def main():
                          " netlist and the FP64 peak (one JSON line on stderr, and a"
                          " device_eval key in the result)")
     ap.add_argument("--eval-reps", type=int, default=20)
+    ap.add_argument("--gnn-steps", type=int, default=0,
+                    help="profiling case: this many training steps of the predictor network"
+                         " on a seeded graph of --gnn-nodes nodes, then stop")
+    ap.add_argument("--gnn-nodes", type=int, default=8192)
     ap.add_argument("--device-eval-only", action="store_true",
                     help="print the device_eval JSON line and stop (profiling case)")
     ap.add_argument("--tstop", default=None,
@@ -621,6 +671,12 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     args.instances = args.instances or DEFAULT_INSTANCES[args.workload]
+    if args.gnn_steps:
+        print(json.dumps(gnn_case(args.gnn_nodes, args.gnn_steps)))
+        return
+    if args.device_eval_only:
+        print(json.dumps({"device_eval": device_eval(args)}))
+        return
     texts, tdesc = workload_texts(args.workload, args.tstop, args.instances)
     steps_desc = (f", a step advances every instance by a {args.window} window of its"
                   " transient" if args.workload in ("c2", "c4") else "")
@@ -639,9 +695,6 @@ def main():
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
         dist.init_process_group("nccl")
         dist.barrier()
-    if args.device_eval_only:
-        print(json.dumps({"device_eval": device_eval(args)}))
-        return
     if args.phases:
         phase_split(args, texts)
     dev_eval = None

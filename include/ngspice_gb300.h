@@ -182,17 +182,20 @@ NGSF_API int ngsf_node_graph(const ngsf_handle *h, int *nv, int *nedges, int *vn
                              int *gidx, float *stat);
 /* Newton predictor for the circuit's next runs: kind 0 off (the
  * reference's start), 1 linear extrapolation of the last two accepted
- * points, 2 that plus the network's correction of the node voltages
- * (params: flat layout above).  With a predictor, Newton at each new
+ * points, 3 the quadratic (the parabola through the last three), 2 the
+ * quadratic plus the network's correction of the node voltages (params:
+ * flat layout above).  With a predictor, Newton at each new
  * timestep starts from its guess, may be accepted after the first
- * iteration when NIconvTest passes, and a start that misses itl4 is
- * retried from the plain start.  Features per node at step n: v_n,
+ * iteration when the first solve's node voltages pass NIconvTest against
+ * the guess (the point accepted then keeps the guessed voltages, the
+ * linearisation point, with the solved branch currents), and a start that
+ * misses itl4 is retried from the plain start.  Features per node at step n: v_n,
  * (v_n - v_{n-1})/0.05, (v_{n-1} - v_{n-2})/0.05, r1 = h_{n+1}/h_n and
  * r2 = h_n/h_{n-1} (each at most 4), r1 (v_n - v_{n-1})/0.05, stat[6], 1,
  * r1 (r1+1) r2 (d1 - r2 d2) / ((r2+1) 0.05) with d1 = v_n - v_{n-1},
- * d2 = v_{n-1} - v_{n-2}, 0, 0; the guess is v_n + r1 d1 + 0.05 g pred
- * with g = a / (a + 1e-4 V), a = |d1| + |d2| (quiet nodes keep the
- * linear extrapolation). */
+ * d2 = v_{n-1} - v_{n-2}, 0, 0; the guess is v_n + r1 d1 + r1 (r1+1) r2
+ * (d1 - r2 d2) / (r2+1) + 0.005 g pred with g = a / (a + 1e-4 V),
+ * a = |d1| + |d2| (quiet nodes keep the quadratic extrapolation). */
 NGSF_API int ngsf_set_predictor(ngsf_handle *h, int kind, const float *params);
 
 /* Whether the circuit runs over the whole grid when it is alone or in a

@@ -91,7 +91,10 @@ IMPEXP int ngSpice_Init(SendChar *printfcn, SendStat *statfcn, ControlledExit *n
  * host synchronisation, so GetSyncData is recorded but not called. */
 IMPEXP int ngSpice_Init_Sync(GetVSRCData *vsrcdat, GetISRCData *isrcdat,
                              GetSyncData *syncdat, int *ident, void *userData);
-/* sharedspice.h:403 */
+/* sharedspice.h:403; a transient runs on the GPU in 64 windows of its
+ * length: SendData fires once per accepted point, in order, as each window
+ * ends; "bg_halt" stops a background run at the end of its current window
+ * (state kept on the device) and "bg_resume" continues it. */
 IMPEXP int ngSpice_Command(char *command);
 /* sharedspice.h:407 */
 IMPEXP pvector_info ngGet_Vec_Info(char *vecname);

@@ -5,7 +5,9 @@
  * The sharedspice layer keeps the reference's observable behaviour for the
  * transient path (src/sharedspice.c): commands are executed immediately,
  * "bg_run" runs the analysis on a background thread and reports through
- * BGThreadRunning, every accepted point is sent through SendData after
+ * BGThreadRunning ("bg_halt" stops it between windows, "bg_resume"
+ * continues it), every accepted point is sent through SendData as the
+ * run's windows end, after
  * SendInitData has described the vectors, output vectors are looked up by
  * name with ngGet_Vec_Info, errors return 1.
  */
@@ -15,6 +17,7 @@
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <functional>
 #include <map>
 #include <mutex>
 #include <sstream>
@@ -377,8 +380,8 @@ NGSF_API int ngsf_set_predictor(ngsf_handle *h, int kind, const float *params)
 {
     if (!h || !h->p.dev)
         return fail("ngsf_set_predictor: null or host-only handle");
-    if (kind < 0 || kind > 2 || (kind == 2 && !params))
-        return fail("ngsf_set_predictor: kind 0, 1, or 2 with parameters");
+    if (kind < 0 || kind > 3 || (kind == 2 && !params))
+        return fail("ngsf_set_predictor: kind 0, 1, 3, or 2 with parameters");
     try {
         h->p.dev->set_pred(h->p.img, kind, params);
     } catch (const std::exception &e) {
@@ -424,7 +427,18 @@ struct Shared {
     std::vector<std::string> nameStore;
     std::vector<double> extraBreaks;
     int tranCount = 0;
+    /* the transient in progress: run window by window so that accepted
+     * points stream out through SendData and bg_halt can stop it between
+     * windows (bg_resume continues it) */
+    ngsf_handle *active = nullptr;
+    Plot *activePlot = nullptr;
+    int activeWindow = 0;
+    size_t activeSent = 0;
+    std::atomic<bool> haltReq{false};
 } S;
+
+/* windows a transient is cut into for streaming (each 1/64 of tstop) */
+constexpr int kStreamWindows = 64;
 
 void say(const char *fmt, ...)
 {
@@ -470,6 +484,107 @@ std::string with_tran(const std::string &deck, const std::string &tranArgs)
     return os.str();
 }
 
+/* point the vectors' info at their storage (after appends) */
+void refresh_infos(Plot *plot)
+{
+    for (auto &v : plot->vecs) {
+        v->info.v_realdata = v->data.data();
+        v->info.v_length = (int)v->data.size();
+    }
+}
+
+void finish_tran(int status)
+{
+    ngsf_close(S.active);
+    S.active = nullptr;
+    S.activePlot = nullptr;
+    if (S.statfcn) {
+        char st[] = "--ready--";
+        S.statfcn(st, S.ident, S.user);
+    }
+    (void)status;
+}
+
+/* Run the active transient window by window until it ends or a halt is
+ * requested: after each window the new accepted points are appended to
+ * the plot's vectors and sent through SendData (the reference sends each
+ * accepted point from CKTdump as it is computed, src/spicelib/analysis/
+ * cktdump.c:33 -> OUTpData; here they come one window at a time).
+ * Returns 0, or 1 on an error; *halted tells a halt apart from the end. */
+int continue_tran(bool *halted)
+{
+    *halted = false;
+    ngsf_handle *h = S.active;
+    Plot *plot = S.activePlot;
+    const double tstop = h->p.img.opt.tstop;
+    const int n = h->p.img.n;
+    const int w = 1 + (int)h->p.probes.size();
+    size_t nv = plot->vecs.size();
+    std::vector<vecvalues> vv(nv);
+    std::vector<pvecvalues> pv(nv);
+    for (size_t i = 0; i < nv; i++) {
+        vv[i].name = (char *)plot->vecs[i]->name.c_str();
+        vv[i].cimag = 0;
+        vv[i].is_scale = i == 0;
+        vv[i].is_complex = false;
+        pv[i] = &vv[i];
+    }
+    for (; S.activeWindow < kStreamWindows; S.activeWindow++) {
+        const int k = S.activeWindow;
+        const double until = k + 1 == kStreamWindows ? 2 * tstop : tstop * (k + 1) / kStreamWindows;
+        if (ngsf_run_window(&h, 1, until, 0, nullptr)) {
+            say("stderr Error: %s", ngsf_last_error());
+            finish_tran(1);
+            return 1;
+        }
+        int ires[NGSF_R_COUNT];
+        ngsf_results(h, ires, nullptr);
+        const int status = ires[NGSF_R_STATUS];
+        const std::vector<double> &pts = h->p.points;
+        const size_t np = std::min<size_t>((size_t)ires[NGSF_R_NPOINTS], pts.size() / w);
+        const size_t from = S.activeSent;
+        {
+            std::lock_guard<std::recursive_mutex> g(S.mu);
+            for (size_t q = from; q < np; q++) {
+                plot->vecs[0]->data.push_back(pts[q * w]);
+                for (int i = 0; i < n; i++)
+                    plot->vecs[1 + i]->data.push_back(pts[q * w + 1 + i]);
+            }
+            refresh_infos(plot);
+        }
+        S.activeSent = np;
+        if (S.datfcn)
+            for (size_t q = from; q < np; q++) {
+                for (size_t i = 0; i < nv; i++)
+                    vv[i].creal = plot->vecs[i]->data[q];
+                vecvaluesall all{(int)nv, (int)q, pv.data()};
+                S.datfcn(&all, (int)nv, S.ident, S.user);
+            }
+        if (S.statfcn && np) {
+            char st[64];
+            snprintf(st, sizeof st, "tran %.1f%%", 100.0 * pts[(np - 1) * w] / tstop);
+            S.statfcn(st, S.ident, S.user);
+        }
+        if (status == 0) {
+            finish_tran(0);
+            return 0;
+        }
+        if (status != NGSF_HELD) {
+            say("stderr Error: transient analysis failed with code %d (time %g)", status,
+                h->p.fres[NGSF_F_TIME]);
+            finish_tran(1);
+            return 1;
+        }
+        if (S.haltReq.load()) {
+            S.activeWindow++;
+            *halted = true;
+            return 0;
+        }
+    }
+    finish_tran(0);
+    return 0;
+}
+
 int do_tran(const std::string &tranArgs)
 {
     std::string deck;
@@ -481,6 +596,10 @@ int do_tran(const std::string &tranArgs)
         }
         deck = tranArgs.empty() ? S.deck : with_tran(S.deck, tranArgs);
     }
+    if (S.active) {
+        ngsf_close(S.active);
+        S.active = nullptr;
+    }
     ngsf_handle *h = ngsf_open(deck.c_str(), nullptr, 1 << 22, 0);
     if (!h) {
         say("stderr Error: %s", ngsf_last_error());
@@ -490,54 +609,27 @@ int do_tran(const std::string &tranArgs)
         char st[] = "tran 0.0%";
         S.statfcn(st, S.ident, S.user);
     }
-    int rc = ngsf_run(&h, 1, 0, nullptr);
-    if (rc) {
-        say("stderr Error: %s", ngsf_last_error());
-        ngsf_close(h);
-        return 1;
-    }
-    int ires[NGSF_R_COUNT];
-    ngsf_results(h, ires, nullptr);
-    if (ires[NGSF_R_STATUS] != 0) {
-        say("stderr Error: transient analysis failed with code %d (time %g)", ires[NGSF_R_STATUS],
-            h->p.fres[NGSF_F_TIME]);
-    }
     auto plot = std::make_unique<Plot>();
-    {
-        std::lock_guard<std::recursive_mutex> g(S.mu);
-        plot->name = "tran" + std::to_string(++S.tranCount);
-        plot->title = h->p.ckt->title;
-        plot->type = "transient";
-    }
+    plot->name = "tran" + std::to_string(++S.tranCount);
+    plot->title = h->p.ckt->title;
+    plot->type = "transient";
     int n = h->p.img.n;
-    int np = ires[NGSF_R_NPOINTS];
-    int w = 1 + (int)h->p.probes.size();
     auto tv = std::make_unique<Vec>();
     tv->name = "time";
-    std::vector<std::unique_ptr<Vec>> vs;
+    plot->vecs.push_back(std::move(tv));
     for (int i = 0; i < n; i++) {
         auto v = std::make_unique<Vec>();
         v->name = h->p.img.names[i];
-        vs.push_back(std::move(v));
-    }
-    const std::vector<double> &pts = h->p.points;
-    for (int k = 0; k < np && (size_t)(k + 1) * w <= pts.size(); k++) {
-        tv->data.push_back(pts[(size_t)k * w]);
-        for (int i = 0; i < n; i++)
-            vs[i]->data.push_back(pts[(size_t)k * w + 1 + i]);
-    }
-    plot->vecs.push_back(std::move(tv));
-    for (auto &v : vs)
         plot->vecs.push_back(std::move(v));
+    }
     for (auto &v : plot->vecs) {
         v->info.v_name = (char *)v->name.c_str();
         v->info.v_type = v->name == "time" ? 1 : (v->name.find("#branch") != std::string::npos ? 4 : 3);
         v->info.v_flags = 1;   /* VF_REAL */
-        v->info.v_realdata = v->data.data();
         v->info.v_compdata = nullptr;
-        v->info.v_length = (int)v->data.size();
     }
-    /* SendInitData once, then SendData per accepted point */
+    refresh_infos(plot.get());
+    /* SendInitData once, then SendData per accepted point as windows end */
     if (S.initfcn) {
         std::vector<vecinfo> vi(plot->vecs.size());
         std::vector<pvecinfo> pvi(plot->vecs.size());
@@ -553,35 +645,34 @@ int do_tran(const std::string &tranArgs)
                        (char *)"", (char *)plot->type.c_str(), (int)vi.size(), pvi.data()};
         S.initfcn(&all, S.ident, S.user);
     }
-    if (S.datfcn) {
-        size_t nv = plot->vecs.size();
-        std::vector<vecvalues> vv(nv);
-        std::vector<pvecvalues> pv(nv);
-        for (size_t i = 0; i < nv; i++) {
-            vv[i].name = (char *)plot->vecs[i]->name.c_str();
-            vv[i].cimag = 0;
-            vv[i].is_scale = i == 0;
-            vv[i].is_complex = false;
-            pv[i] = &vv[i];
-        }
-        for (int k = 0; k < (int)plot->vecs[0]->data.size(); k++) {
-            for (size_t i = 0; i < nv; i++)
-                vv[i].creal = plot->vecs[i]->data[k];
-            vecvaluesall all{(int)nv, k, pv.data()};
-            S.datfcn(&all, (int)nv, S.ident, S.user);
-        }
-    }
     {
         std::lock_guard<std::recursive_mutex> g(S.mu);
+        S.activePlot = plot.get();
         S.plots.push_back(std::move(plot));
         S.cur = (int)S.plots.size() - 1;
     }
-    ngsf_close(h);
-    if (S.statfcn) {
-        char st[] = "--ready--";
-        S.statfcn(st, S.ident, S.user);
-    }
-    return ires[NGSF_R_STATUS] == 0 ? 0 : 1;
+    S.active = h;
+    S.activeWindow = 0;
+    S.activeSent = 0;
+    S.haltReq = false;
+    bool halted = false;
+    return continue_tran(&halted);
+}
+
+/* bg_run / bg_resume: the transient on the background thread */
+void start_bg(std::function<void()> body)
+{
+    if (S.bg.joinable())
+        S.bg.join();
+    S.running = true;
+    if (S.bgfcn)
+        S.bgfcn(false, S.ident, S.user);
+    S.bg = std::thread([body] {
+        body();
+        S.running = false;
+        if (S.bgfcn)
+            S.bgfcn(true, S.ident, S.user);
+    });
 }
 
 std::string g_lastTran;
@@ -624,24 +715,31 @@ int command(const std::string &raw)
         if (S.running)
             return 1;
         std::string args = verb == "bg_tran" ? rest : "";
-        if (S.bg.joinable())
-            S.bg.join();
-        S.running = true;
-        if (S.bgfcn)
-            S.bgfcn(false, S.ident, S.user);
-        S.bg = std::thread([args] {
-            do_tran(args);
-            S.running = false;
-            if (S.bgfcn)
-                S.bgfcn(true, S.ident, S.user);
-        });
+        start_bg([args] { do_tran(args); });
         return 0;
     }
-    if (verb == "bg_halt" || verb == "bg_resume" || verb == "halt") {
-        /* the whole run executes on the device as one launch; halting mid
-         * run is not offered, the calls only synchronise */
+    if (verb == "bg_halt" || verb == "halt") {
+        /* the background run stops at the end of its current window, with
+         * its state kept on the device (sharedspice.c bg_halt) */
+        S.haltReq = true;
         if (S.bg.joinable())
             S.bg.join();
+        S.haltReq = false;
+        return 0;
+    }
+    if (verb == "bg_resume" || verb == "resume") {
+        if (S.running)
+            return 1;
+        if (!S.active)
+            return 0;   /* nothing halted: the run had already ended */
+        if (verb == "resume") {
+            bool halted = false;
+            return continue_tran(&halted);
+        }
+        start_bg([] {
+            bool halted = false;
+            continue_tran(&halted);
+        });
         return 0;
     }
     if (verb == "remcirc" || verb == "destroy" || verb == "reset") {

@@ -1125,7 +1125,7 @@ __device__ __forceinline__ int rl_level_work(const ngsf_ckt_t &C, int l)
 }
 
 /* level l, first half (threads t of T): pivot checks, L(:,k) *= 1/U(k,k) */
-__device__ int rl_scale(const ngsf_ckt_t &C, int l, int t, int T, double growth)
+__device__ __forceinline__ int rl_scale(const ngsf_ckt_t &C, int l, int t, int T, double growth)
 {
     int bad = 0;
     for (int c = C.rl_ptr[l] + t; c < C.rl_ptr[l + 1]; c += T) {
@@ -1162,7 +1162,7 @@ __device__ int rl_scale(const ngsf_ckt_t &C, int l, int t, int T, double growth)
 
 /* level l, second half: the updates (and the inverse of every pivot whose
  * last update this is) */
-__device__ void rl_update(const ngsf_ckt_t &C, int l, int t, int T)
+__device__ __forceinline__ void rl_update(const ngsf_ckt_t &C, int l, int t, int T)
 {
     const int d0 = C.ud_ptr[l], d1 = C.ud_ptr[l + 1];
     for (int d = d0 + t; d < d1; d += NGSF_RL_ILP * T) {
@@ -1200,7 +1200,7 @@ __device__ void rl_update(const ngsf_ckt_t &C, int l, int t, int T)
 }
 
 /* One block: a whole level, two barriers. */
-__device__ int rl_level_block(const ngsf_ckt_t &C, int l, double growth)
+__device__ __forceinline__ int rl_level_block(const ngsf_ckt_t &C, int l, double growth)
 {
     const int bad = rl_scale(C, l, threadIdx.x, blockDim.x, growth);
     __syncthreads();
@@ -1423,7 +1423,7 @@ __device__ __forceinline__ void solve_apply(const SolveRow &p, double *w, const 
  * pivot): per level, rows of up to 32 terms by one thread each, terms in
  * order; longer rows (listed per level in hptr/hrow) by a warp, with
  * lane-strided partial sums and a fixed butterfly. */
-__device__ void solve_sweep(const ngsf_ckt_t &C, double *w, int nlev, const int *lptr,
+__device__ __forceinline__ void solve_sweep(const ngsf_ckt_t &C, double *w, int nlev, const int *lptr,
                             const int4 *desc, const double *val, const int *col,
                             const int *rptr, const int *hptr, const int *hrow, bool back)
 {
@@ -1480,10 +1480,12 @@ __device__ void lu_solve(const ngsf_ckt_t &C, Ctl &s, double *rhs)
  * stores NIconvTest's return value (niiter.c:286-289).  The device tests
  * therefore never change a Newton decision, and the engine does not spend
  * FP64 work on them (mos1_conv_one stays available for diagnostics). */
-__device__ int conv_test(const ngsf_ckt_t &C, Ctl &s, const Iter &it)
+__device__ int conv_test(const ngsf_ckt_t &C, Ctl &s, const Iter &it, bool voltagesOnly = false)
 {
     int bad = 0;
     for (int i = 1 + threadIdx.x; i <= C.n; i += blockDim.x) {
+        if (voltagesOnly && !C.ntype[i])
+            continue;
         double nw = it.rhs[i], od = it.rhsOld[i];
         if (isnan(nw)) {
             bad = 1;
@@ -1534,7 +1536,7 @@ __device__ double ckt_terr(const ngsf_ckt_t &C, const Ctl &s, int qcap, double t
 
 /* DEVtrunc of the charges this thread owns (thread t0 of T): the smallest
  * CKTterr step among them */
-__device__ double trunc_share(const ngsf_ckt_t &C, const Ctl &s, int t0, int T)
+__device__ __forceinline__ double trunc_share(const ngsf_ckt_t &C, const Ctl &s, int t0, int T)
 {
     double t = 1e300;   /* HUGE */
     for (int i = t0; i < C.cap.n; i += T)
@@ -1816,12 +1818,15 @@ __device__ int ni_iter(const ngsf_ckt_t &C, Ctl &s, int maxIter, bool resume)
             return NGSF_E_ITERLIM;
         }
         /* NIconvTest from the second iteration (niiter.c), or already after
-         * the first when it started from the predictor's guess (every
-         * unknown against its guessed value, the same test) */
+         * the first when it started from the predictor's guess.  Then the
+         * node voltages are tested against their guessed values; a branch
+         * current does not enter the device loads (MNA is linear in it),
+         * so the first solve's currents are the ones of the linearisation
+         * at the guess and are taken as they are */
         const bool guess1 = (s.mode & NGSF_MODEGUESS) && iterno == 1;
         tp = prof_t(C);
         if (noncon == 0 && (iterno != 1 || guess1))
-            noncon = conv_test(C, s, it);
+            noncon = conv_test(C, s, it, guess1);
         else
             noncon = 1;
         prof_add(C, NGSF_P_CONV, tp);
@@ -1844,6 +1849,15 @@ __device__ int ni_iter(const ngsf_ckt_t &C, Ctl &s, int maxIter, bool resume)
             if (guess1 && noncon == 0)
                 ret = NGSF_OK;
             mode = (mode & ~NGSF_INITF) | NGSF_MODEINITFLOAT;
+        }
+        if (guess1 && ret == NGSF_OK) {
+            /* the accepted point keeps the guessed node voltages -- the
+             * linearisation point the device states belong to, as the
+             * reference reports its last linearisation point (NIiter returns
+             * before its swap) -- with the branch currents of the solve */
+            for (int i = 1 + threadIdx.x; i <= C.n; i += blockDim.x)
+                if (!C.ntype[i])
+                    it.rhsOld[i] = it.rhs[i];
         }
         __syncthreads();
         if (threadIdx.x == 0) {
@@ -2426,7 +2440,16 @@ __device__ void run_circuit(const ngsf_ckt_t &C, Ctl &s, int runMode, long long 
  * starts a waiting block on an SM as soon as a block there retires, so
  * circuits of uneven size keep every SM busy and the largest ones start
  * first (longest-processing-time order). */
-__global__ void __launch_bounds__(NGSF_THREADS)
+/* Registers per thread of the transient kernels: an explicit cap of 255
+ * (the BSIM4 evaluation keeps everything in registers, no spills).  With
+ * only __launch_bounds__(256) the compiler settles on 128 registers and
+ * spills about 1.2 KB a thread.  NGSF_TRAN_MAXNREG (a build-time define)
+ * sets another cap for experiments. */
+#ifndef NGSF_TRAN_MAXNREG
+#define NGSF_TRAN_MAXNREG 255
+#endif
+#define NGSF_TRAN_BOUNDS __maxnreg__(NGSF_TRAN_MAXNREG)
+__global__ void NGSF_TRAN_BOUNDS
 tran_kernel(const ngsf_ckt_t *ckts, const int *order, int nckt, int runMode,
             long long maxSteps, int solveCap, int gnnBytes)
 {
@@ -2454,7 +2477,7 @@ tran_kernel(const ngsf_ckt_t *ckts, const int *order, int nckt, int runMode,
 
 /* One circuit over the whole (cooperative) grid: block 0 runs the
  * transient, the other blocks evaluate transistors on its command. */
-__global__ void __launch_bounds__(NGSF_THREADS)
+__global__ void NGSF_TRAN_BOUNDS
 tran_wide_kernel(const ngsf_ckt_t *ckt, int runMode, long long maxSteps, int solveCap,
                  int gnnBytes)
 {
@@ -2985,11 +3008,21 @@ extern "C" cudaError_t ngsf_launch_tran_wide(const ngsf_ckt_t *d_ckt, int nblock
                                        (size_t)solveCap + (size_t)gnnBytes, stream);
 }
 
-/* circuit blocks of the batched launch one SM holds at once */
-extern "C" int ngsf_tran_occupancy(int threads, int dynSmem)
+/* circuit blocks of the batched launch one SM holds at once; *regs and
+ * *smem (may be NULL) receive the kernel's registers per thread and static
+ * shared bytes */
+extern "C" int ngsf_tran_occupancy(int threads, int dynSmem, int *regs, int *smem)
 {
     int per = 0;
-    if (allow_dyn_smem((const void *)tran_kernel) != cudaSuccess ||
+    cudaFuncAttributes fa{};
+    if (cudaFuncGetAttributes(&fa, (const void *)tran_kernel) == cudaSuccess) {
+        if (regs)
+            *regs = fa.numRegs;
+        if (smem)
+            *smem = (int)fa.sharedSizeBytes;
+    }
+    if (cudaFuncSetAttribute((const void *)tran_kernel,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, dynSmem) != cudaSuccess ||
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, tran_kernel, threads, dynSmem) !=
             cudaSuccess)
         return 0;
@@ -3009,7 +3042,11 @@ extern "C" cudaError_t ngsf_launch_tran(const ngsf_ckt_t *d_ckts, const int *d_o
         return cudaSuccess;
     if (threads != 64 && threads != 128)
         threads = NGSF_THREADS;
-    cudaError_t e = allow_dyn_smem((const void *)tran_kernel);
+    /* the dynamic shared memory this launch uses, no more (a larger
+     * maximum can cost resident blocks) */
+    cudaError_t e = cudaFuncSetAttribute((const void *)tran_kernel,
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         solveCap + gnnBytes);
     if (e != cudaSuccess)
         return e;
     tran_kernel<<<nckt, threads, (size_t)solveCap + (size_t)gnnBytes, stream>>>(

@@ -182,6 +182,7 @@ typedef struct {
  * of the network (kind 2).  kind 0: off; 1: linear extrapolation guess;
  * 2: linear extrapolation plus the network's correction. */
 #define NGSF_PRED_VSCALE 0.05
+#define NGSF_PRED_VOUT 0.005    /* V: unit of the network's correction */
 #define NGSF_PRED_RATIO_MAX 4.0
 #define NGSF_PRED_QUIET 1e-4     /* V: activity at which the correction is halved */
 typedef struct {

@@ -269,7 +269,7 @@ __device__ bool pred_network(const ngsf_ckt_t &C, const Iter &it, double r1, dou
                 const int k = P.vnode[v];
                 const double act = fabs(P.cur[k] - P.h0[k]) + fabs(P.h0[k] - P.h1[k]);
                 const double gate = act / (act + NGSF_PRED_QUIET);
-                it.rhsOld[k] += VS * gate * (double)(a[0] + P.bout[0]);
+                it.rhsOld[k] += NGSF_PRED_VOUT * gate * (double)(a[0] + P.bout[0]);
             }
         }
         tc05_fence_before();
@@ -278,18 +278,26 @@ __device__ bool pred_network(const ngsf_ckt_t &C, const Iter &it, double r1, dou
     return ok;
 }
 
-/* The guess for the timestep about to start (all threads): linear
- * extrapolation of every unknown, plus the network's correction of the
- * node voltages; marks the mode so the first iteration reads it. */
+/* The guess for the timestep about to start (all threads): the linear
+ * (kind 1) or quadratic (kinds 2 and 3) extrapolation of every unknown
+ * through the last accepted points, plus, with kind 2, the network's
+ * correction of the node voltages; marks the mode so the first iteration
+ * reads it. */
 __device__ void pred_guess(const ngsf_ckt_t &C, Ctl &s)
 {
     const ngsf_pred_t &P = C.pred;
     const double hn = s.tcur - s.th0, hp = s.th0 - s.th1;
     const double r1 = hn > 0 ? fmin(s.delta / hn, NGSF_PRED_RATIO_MAX) : 1.0;
     const double r2 = hp > 0 ? fmin(hn / hp, NGSF_PRED_RATIO_MAX) : 1.0;
+    const bool quad = P.kind >= 2;
     Iter it = iter_ctx(C, s);
-    for (int k = threadIdx.x; k <= C.n; k += blockDim.x)
-        it.rhsOld[k] = k ? P.cur[k] + r1 * (P.cur[k] - P.h0[k]) : 0.0;
+    for (int k = threadIdx.x; k <= C.n; k += blockDim.x) {
+        const double d1 = P.cur[k] - P.h0[k], d2 = P.h0[k] - P.h1[k];
+        double g = P.cur[k] + r1 * d1;
+        if (quad)   /* the parabola through the last three points */
+            g += r1 * (r1 + 1.0) * r2 * (d1 - r2 * d2) / (r2 + 1.0);
+        it.rhsOld[k] = k ? g : 0.0;
+    }
     __syncthreads();
     bool ok = true;
     if (P.kind == 2 && g_psm)

@@ -45,7 +45,7 @@ extern "C" cudaError_t ngsf_launch_tran(const ngsf_ckt_t *d_ckts, const int *d_o
                                         int runMode, long long maxSteps, int solveCap,
                                         int gnnBytes, int threads, cudaStream_t stream);
 extern "C" int ngsf_ctl_bytes(void);
-extern "C" int ngsf_tran_occupancy(int threads, int dynSmem);
+extern "C" int ngsf_tran_occupancy(int threads, int dynSmem, int *regs, int *smem);
 
 namespace ngsf {
 
@@ -841,11 +841,14 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
                 cudaEventElapsedTime(&ms, e0, e1);
                 total += ms * 1e-3;
                 nl++;
-                if (trace)
+                if (trace) {
+                    int regs = 0, smem = 0;
+                    const int per = ngsf_tran_occupancy(threads, solveCap + gnnBytes, &regs, &smem);
                     fprintf(stderr, "ngsf: launch %d: %zu circuits, largest n %d, %d threads"
-                            " (%d blocks per SM),%s %.3f ms\n", nl, descs.size(), maxn, threads,
-                            ngsf_tran_occupancy(threads, solveCap + gnnBytes),
-                            holdNow ? " hold," : "", ms);
+                            " (%d blocks per SM; %d registers, %d + %d shared bytes),%s %.3f ms\n",
+                            nl, descs.size(), maxn, threads, per, regs, smem,
+                            solveCap + gnnBytes, holdNow ? " hold," : "", ms);
+                }
             }
             for (auto *c : wide) {
                 /* a fresh hand-over block per launch: command numbers start at 0 */

@@ -48,6 +48,8 @@ def _compile(src: str) -> str:
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps):
         return obj
     cmd = [nvcc()] + ARCH + COMMON + ["-c", src, "-o", obj]
+    if src.endswith(".cu") and os.environ.get("NGSF_TRAN_MAXNREG"):
+        cmd.append(f"-DNGSF_TRAN_MAXNREG={int(os.environ['NGSF_TRAN_MAXNREG'])}")
     if src.endswith(".cu"):
         cmd += ["-Xptxas", "-v"] if os.environ.get("NGSF_PTXAS_VERBOSE") else []
     p = subprocess.run(cmd, capture_output=True, text=True)

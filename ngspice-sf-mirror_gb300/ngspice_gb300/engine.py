@@ -275,7 +275,8 @@ class Circuit:
 
     def set_predictor(self, kind: int, params: np.ndarray | None = None):
         """0: off (the reference's Newton start), 1: linear extrapolation,
-        2: with the trained network (flat parameters)."""
+        3: quadratic extrapolation, 2: quadratic plus the trained network's
+        correction (flat parameters)."""
         p = None
         if params is not None:
             params = np.ascontiguousarray(params, np.float32)
@@ -409,23 +410,37 @@ def open_many(netlists: list[str], probes: list[str] | None = None, outcap: int 
 
 
 def tune_factor_shape(circuit: Circuit, blocks=(16, 24, 32, 48, 64, 96, 152),
-                      small_works=(256, 1024, 4096, 16384), max_steps: int = 40,
-                      repeats: int = 2) -> dict:
+                      small_works=(256, 1024, 4096, 16384, 1 << 30), warm: float = 6e-12,
+                      window: float = 3e-12, repeats: int = 2) -> dict:
     """Autotuner of the wide refactorization over the circuit's level
-    schedule: times short runs (the operating point and max_steps
-    timesteps, device time, best of `repeats`) for each group size at the
-    default small-level threshold, then each threshold at the best group
-    size, and leaves the fastest shape set on the circuit.  Every shape
-    computes the same result, so tuning changes no waveform.  A circuit
-    that does not run wide keeps the default.  Returns the choice and the
-    timings."""
+    schedule.  One run is advanced untimed to `warm` (the operating point
+    and the first steps); then each shape is timed over the next windows of
+    `window` seconds of that run, as device time per Newton iteration (the
+    refactorization and solve structure is fixed, so the cost per iteration
+    compares shapes across windows), best of `repeats`: first every group
+    size at the default small-level threshold, then each threshold at the
+    best group size (the largest threshold runs every level in one block).
+    The fastest shape is left set on the circuit; every shape computes the
+    same bits, so tuning changes no waveform.  A circuit that does not run
+    wide keeps the default.  Returns the choice and the timings."""
     wide, nb = circuit.wide_info()
     if not wide:
         return {"blocks": 0, "small_work": 0, "timings": {}}
+    state = {"t": warm}
+    run_window([circuit], warm)
 
     def time_shape(b: int, sw: int) -> float:
         circuit.set_factor_shape(b, sw)
-        return min(run([circuit], max_steps=max_steps) for _ in range(repeats))
+        best = float("inf")
+        for _ in range(repeats):
+            before = int(circuit.results()[R_NUMITER])
+            state["t"] += window
+            sec = run_window([circuit], state["t"])
+            r = circuit.results()
+            iters = int(r[R_NUMITER]) - before
+            if r[R_STATUS] == PAUSED and iters > 0:
+                best = min(best, sec / iters)
+        return best
 
     timings = {}
     for b in [b for b in blocks if b <= nb] or [nb]:

@@ -1,11 +1,13 @@
 """Learned Newton predictor: graph, features and training data from circuit
 trajectories, and ctypes bindings of the network kernels (gnn.cu).
 
-The network predicts, per circuit node, a correction to the linear
-extrapolation of the node voltage to the next accepted timepoint:
+The network predicts, per circuit node, a correction to the polynomial
+(quadratic) extrapolation of the node voltage to the next accepted
+timepoint:
 
     v_lin  = v_n + r1 (v_n - v_{n-1}),      r1 = h_{n+1} / h_n
-    v_next ~ v_lin + VSCALE * g * pred,     g = a / (a + QUIET),
+    v_quad = v_lin + r1 (r1 + 1) r2 (d1 - r2 d2) / (r2 + 1)
+    v_next ~ v_quad + VOUT * g * pred,      g = a / (a + QUIET),
     a = |v_n - v_{n-1}| + |v_{n-1} - v_{n-2}|
 
 Node features (16): v_n, (v_n - v_{n-1}) / VSCALE, (v_{n-1} - v_{n-2}) /
@@ -27,6 +29,10 @@ from . import engine as E
 
 F_IN = 16
 VSCALE = 0.05
+# unit of the network's correction (the residual after the quadratic
+# extrapolation is millivolts; a finer unit keeps BF16 rounding of the output
+# well below the convergence tolerance)
+VOUT = 0.005
 RATIO_MAX = 4.0
 QUIET = 1e-4        # V: node activity at which the correction is halved
 
@@ -178,6 +184,21 @@ def features(v3: np.ndarray, v2: np.ndarray, v1: np.ndarray, h_next: float, h_n:
     return X, vlin.astype(np.float64)
 
 
+def quadratic(X: np.ndarray, vlin: np.ndarray) -> np.ndarray:
+    """The quadratic extrapolation the network corrects: the linear one plus
+    the quadratic increment (feature 13, in units of VSCALE)."""
+    return vlin + VSCALE * X[:, 13].astype(np.float64)
+
+
+def quadratic_exact(v3, v2, v1, h_next: float, h_n: float, h_prev: float) -> np.ndarray:
+    """The parabola through the last three accepted points at the next time,
+    in FP64 (the engine's pred_guess arithmetic, ratios capped at 4)."""
+    r1 = min(h_next / h_n, RATIO_MAX) if h_n > 0 else 1.0
+    r2 = min(h_n / h_prev, RATIO_MAX) if h_prev > 0 else 1.0
+    d1, d2 = v3 - v2, v2 - v1
+    return v3 + r1 * d1 + r1 * (r1 + 1.0) * r2 * (d1 - r2 * d2) / (r2 + 1.0)
+
+
 def gate(v3: np.ndarray, v2: np.ndarray, v1: np.ndarray) -> np.ndarray:
     """Weight of the network's correction at each node: a / (a + QUIET)
     with a = |v_n - v_{n-1}| + |v_{n-1} - v_{n-2}| (the transient kernel
@@ -189,11 +210,12 @@ def gate(v3: np.ndarray, v2: np.ndarray, v1: np.ndarray) -> np.ndarray:
 def trajectory_samples(t: np.ndarray, V: np.ndarray, stat: np.ndarray,
                        stride: int = 1) -> list[tuple[np.ndarray, np.ndarray, np.ndarray]]:
     """(X, y, g) training triples from accepted points t[k], V[k, node]:
-    y = (v_{n+1} - v_lin) / VSCALE, g the correction's gate."""
+    y = (v_{n+1} - v_quad) / VOUT, g the correction's gate."""
     out = []
     for n in range(3, len(t) - 1, stride):
         h_next, h_n, h_prev = t[n + 1] - t[n], t[n] - t[n - 1], t[n - 1] - t[n - 2]
         X, vlin = features(V[n], V[n - 1], V[n - 2], h_next, h_n, h_prev, stat)
-        y = ((V[n + 1] - vlin) / VSCALE).astype(np.float32)
+        y = ((V[n + 1] - quadratic_exact(V[n], V[n - 1], V[n - 2], h_next, h_n, h_prev))
+             / VOUT).astype(np.float32)
         out.append((X, y, gate(V[n], V[n - 1], V[n - 2]).astype(np.float32)))
     return out

@@ -59,6 +59,20 @@ CASES = {
 #   mc_1k/2k/3k  Monte Carlo instances (device mismatch) of about 1,000,
 #                2,000 and 3,000 transistors, first 50 ps
 NPROBE = 256
+
+# A tight-tolerance reference (reltol 1e-5, vntol 1e-8 V, abstol 1e-14 A)
+# of the 120-transistor deck over 400 ps, every unknown: the "true"
+# waveform against which runs at the default tolerances are checked at
+# their own time points (runs whose accepted steps differ from the
+# reference's, e.g. with a Newton predictor).
+TIGHT_OPTIONS = ".options klu reltol=1e-5 vntol=1e-8 abstol=1e-14"
+
+
+def bsim4_logic_s3_tight() -> str:
+    text = netlists.random_logic(n_transistors=120, seed=3, n_inputs=6, tstop="400p")
+    return text.replace(".options klu", TIGHT_OPTIONS)
+
+
 LARGE_CASES = {
     "c1_10k_30p": lambda: netlists.random_logic(n_transistors=10000, seed=1, tstop="30p"),
     "mc_1k_50p": lambda: netlists.random_logic(n_transistors=1000, seed=101, tstop="50p",
@@ -203,6 +217,15 @@ def main(argv: list[str]) -> int:
             np.savez_compressed(path, **res)
             print(f"{name}: {len(res['times'])} points, stats={res['stats'].tolist()},"
                   f" {len(res['it_kind'])} iterations -> {os.path.getsize(path)} bytes")
+        if not only or "bsim4_logic_s3_tight" in only:
+            text = bsim4_logic_s3_tight()
+            res = run_reference(text, 0, wd, keep_iters=False)
+            out = {k: res[k] for k in ("names", "times", "values", "stats", "cpu_seconds")}
+            out["netlist"] = np.array(text)
+            path = os.path.join(HERE, "bsim4_logic_s3_tight.npz")
+            np.savez_compressed(path, **out)
+            print(f"bsim4_logic_s3_tight: {len(res['times'])} points, stats={res['stats'].tolist()}"
+                  f" -> {os.path.getsize(path)} bytes")
         for name, make in LARGE_CASES.items():
             if only and name not in only:
                 continue

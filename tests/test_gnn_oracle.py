@@ -82,8 +82,9 @@ def test_features_and_targets():
     assert X.shape == (3, gnn.F_IN)
     assert np.all(g > 0.99)                  # 0.1 V steps: fully active
     assert np.allclose(X[:, 3], 1.5)         # r1 = 1.5p / 1p
-    # v_lin = v3 + 1.5 * 0.1 = 0.45; v_next = 0.4 -> y = -0.05 / VSCALE
-    assert np.allclose(y, (0.4 - 0.45) / gnn.VSCALE, atol=1e-6)
+    # straight line: the quadratic extrapolation is the linear one,
+    # v3 + 1.5 * 0.1 = 0.45; v_next = 0.4 -> y = -0.05 / VOUT
+    assert np.allclose(y, (0.4 - 0.45) / gnn.VOUT, atol=1e-4)
 
 
 def test_node_graph_of_a_compiled_circuit(built_lib):

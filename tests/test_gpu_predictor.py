@@ -18,20 +18,39 @@ def E(built_lib):
     return engine
 
 
-def test_linear_guess_keeps_reference_tolerances(E):
-    g = golden("bsim4_logic_s3")
-    text = str(g["netlist"])
-    plain = E.Circuit(text)
-    E.run([plain], max_steps=200000)
-    c = E.Circuit(text)
-    c.set_predictor(1)
-    E.run([c], max_steps=200000)
-    r, rp = c.results(), plain.results()
-    assert r[E.R_STATUS] == 0
-    assert r[E.R_GUESSES] > 0.9 * r[E.R_ACCEPTED]
-    assert r[E.R_TRANITER] <= rp[E.R_TRANITER]
-    t, v = c.points()
-    assert waveform_violation(c.names(), g["times"], g["values"], t, v) < 1.0
+def test_guess_keeps_the_accuracy_of_the_reference_start(E):
+    """A start from the linear (1) or quadratic (3) guess, accepted after
+    one Newton iteration when the node voltages agree with the guess,
+    moves the accepted time points, so it cannot be compared point by
+    point with the reference's run.  Both it and the reference's own start
+    (0) are compared at their own time points with a tight-tolerance
+    reference run of the same deck (reltol 1e-5, vntol 1e-8 V, abstol
+    1e-14 A).  Neither is within the default tolerances of that true
+    waveform everywhere (the tolerances bound each step's Newton and
+    truncation error, not the global error, and an edge that moves by a
+    fraction of a step shows as a large pointwise error), so the guessed
+    starts must stay within twice the error of the reference's start."""
+    tight = golden("bsim4_logic_s3_tight")
+    text = str(tight["netlist"]).replace(
+        ".options klu reltol=1e-5 vntol=1e-8 abstol=1e-14", ".options klu")
+    worst, ips = {}, {}
+    for kind in (0, 1, 3):
+        c = E.Circuit(text)
+        if kind:
+            c.set_predictor(kind)
+        E.run([c], max_steps=200000)
+        r = c.results()
+        assert r[E.R_STATUS] == 0
+        if kind:
+            assert r[E.R_GUESSES] > 0.9 * r[E.R_ACCEPTED]
+        t, v = c.points()
+        worst[kind] = waveform_violation(c.names(), t, v, tight["times"], tight["values"])
+        ips[kind] = r[E.R_TRANITER] / r[E.R_ACCEPTED]
+        print(f"start {kind}: {ips[kind]:.3f} iterations per step, worst error"
+              f" {worst[kind]:.1f} of the tolerance against the tight reference")
+    for kind in (1, 3):
+        assert ips[kind] <= ips[0]
+        assert worst[kind] <= 2.0 * worst[0]
 
 
 def test_in_kernel_network_equals_standalone_forward(E):
@@ -61,7 +80,9 @@ def test_in_kernel_network_equals_standalone_forward(E):
         X, vlin = gnn.features(V[n], V[n - 1], V[n - 2], dl, t[n] - t[n - 1],
                                t[n - 1] - t[n - 2], g["stat"])
         gate = gnn.gate(V[n], V[n - 1], V[n - 2])
-        expect = vlin + gnn.VSCALE * gate * net.forward(X).astype(np.float64)
+        vquad = gnn.quadratic_exact(V[n], V[n - 1], V[n - 2], dl, t[n] - t[n - 1],
+                                    t[n - 1] - t[n - 2])
+        expect = vquad + gnn.VOUT * gate * net.forward(X).astype(np.float64)
         got = cap["rhsold"][k][g["vnode"] + 1]
         assert np.max(np.abs(got - expect)) <= 1e-6
         checked += 1
@@ -69,22 +90,24 @@ def test_in_kernel_network_equals_standalone_forward(E):
 
 
 def test_trained_network_against_linear_guess(E):
-    """Trains on the GPU on plain trajectories of six circuits and runs two
-    held-out circuits three ways.  Every run meets the reference tolerances
-    (status 0, same accepted-step count order); the measured iterations per
-    step of the three starts are printed and the network must stay within
-    10 % of the linear guess."""
+    """Trains on the GPU on plain trajectories of twelve circuits and runs
+    three held-out circuits four ways: the reference's start, the linear
+    guess, the quadratic (polynomial) guess, and the quadratic guess with
+    the trained network's correction.  Every run meets the reference
+    tolerances (status 0); the iterations per step of the four starts are
+    printed, and the network must need fewer Newton iterations per
+    accepted step than the linear guess."""
     from ngspice_gb300 import netlists, predictor
-    train = [netlists.random_logic(n_transistors=200 + 20 * s, seed=500 + s, tstop="120p")
-             for s in range(6)]
+    train = [netlists.random_logic(n_transistors=150 + 25 * s, seed=500 + s, tstop="150p")
+             for s in range(12)]
     data = predictor.collect(train)
-    params, losses = predictor.train(data, steps=600)
+    params, losses = predictor.train(data, steps=1200)
     assert np.mean(losses[-50:]) < losses[0]
-    test = [netlists.random_logic(n_transistors=250, seed=600 + s, tstop="120p") for s in range(2)]
-    res = predictor.evaluate(test, params, kinds=(0, 1, 2))
-    for k in (0, 1, 2):
-        assert res[k]["status"] == [0, 0]
-    print("iterations per step: plain %.3f linear %.3f network %.3f" %
-          (res[0]["iterations_per_step"], res[1]["iterations_per_step"],
-           res[2]["iterations_per_step"]))
-    assert res[2]["iterations_per_step"] <= 1.10 * res[1]["iterations_per_step"]
+    test = [netlists.random_logic(n_transistors=250, seed=600 + s, tstop="150p")
+            for s in range(3)]
+    res = predictor.evaluate(test, params, kinds=(0, 1, 3, 2))
+    for k in (0, 1, 3, 2):
+        assert res[k]["status"] == [0, 0, 0]
+    print("iterations per step: plain %.3f linear %.3f quadratic %.3f network %.3f" %
+          tuple(res[k]["iterations_per_step"] for k in (0, 1, 3, 2)))
+    assert res[2]["iterations_per_step"] < res[1]["iterations_per_step"]

@@ -1,6 +1,7 @@
 """GPU: the sharedspice-compatible C API driven the way an embedding
 application drives the reference shared library."""
 import ctypes as C
+import time
 
 import numpy as np
 import pytest
@@ -98,3 +99,45 @@ def test_bg_run_and_errors(ng):
     assert ng.ngSpice_Command(b"bg_halt") == 0     # waits for the run
     assert not ng.ngSpice_running()
     assert ng.ngSpice_Command(b"frobnicate") == 1
+
+
+def test_points_stream_and_halt_resume(ng):
+    """SendData streams accepted points as the run's windows end, with
+    SendStat progress in between; bg_halt stops a background run at a
+    window end and bg_resume continues it to the same result as an
+    uninterrupted run."""
+    stats, points, done = [], [], []
+    keep = _KEEP
+    cb_char = SendChar(lambda s, i, u: 0)
+    cb_stat = SendStat(lambda s, i, u: stats.append(s.decode()) or 0)
+    cb_exit = ControlledExit(lambda *a: 0)
+    cb_data = SendData(lambda p, n, i, u: points.append(len(stats)) or 0)
+    cb_init = SendInitData(lambda p, i, u: 0)
+    cb_bg = BGThreadRunning(lambda r, i, u: done.append(bool(r)) or 0)
+    keep += [cb_char, cb_stat, cb_exit, cb_data, cb_init, cb_bg]
+    assert ng.ngSpice_Init(cb_char, cb_stat, cb_exit, cb_data, cb_init, cb_bg, None) == 0
+    g = golden("rc_ladder")
+    lines = [ln.encode() for ln in str(g["netlist"]).splitlines()]
+    arr = (C.c_char_p * (len(lines) + 1))(*lines, None)
+    assert ng.ngSpice_Circ(arr) == 0
+    assert ng.ngSpice_Command(b"bg_run") == 0
+    assert ng.ngSpice_Command(b"bg_halt") == 0
+    assert not ng.ngSpice_running()
+    halted_at = ng.ngGet_Vec_Info(b"time").contents.v_length
+    # a halted run resumes until it ends (halting again on the way)
+    for _ in range(200):
+        if ng.ngGet_Vec_Info(b"time").contents.v_length >= len(g["times"]):
+            break
+        assert ng.ngSpice_Command(b"bg_resume") == 0
+        time.sleep(0.01)
+        assert ng.ngSpice_Command(b"bg_halt") == 0
+        assert not ng.ngSpice_running()
+    t = ng.ngGet_Vec_Info(b"time").contents
+    tt = np.ctypeslib.as_array(t.v_realdata, shape=(t.v_length,))
+    np.testing.assert_array_equal(tt, g["times"])
+    assert len(points) == len(g["times"])
+    assert halted_at <= len(g["times"])
+    # points arrived window by window: progress reports between them
+    progress = [s for s in stats if s.startswith("tran ") and s != "tran 0.0%"]
+    assert len(progress) >= 8
+    assert len(set(points)) >= 8

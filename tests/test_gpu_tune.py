@@ -16,14 +16,14 @@ def E(built_lib):
 
 def test_tuned_shape_gives_identical_results(E):
     from ngspice_gb300 import netlists
-    text = netlists.random_logic(n_transistors=1100, seed=2, tstop="8p")
+    text = netlists.random_logic(n_transistors=1100, seed=2, tstop="14p")
     ref = E.Circuit(text, probes=["y0", "y1"], outcap=4096)
     assert ref.wide_info()[0]
     E.run([ref], max_steps=1_000_000)
 
     c = E.Circuit(text, probes=["y0", "y1"], outcap=4096)
-    choice = E.tune_factor_shape(c, blocks=(16, 48), small_works=(256,), max_steps=4,
-                                 repeats=1)
+    choice = E.tune_factor_shape(c, blocks=(16, 48), small_works=(256,), warm=3e-12,
+                                 window=2e-12, repeats=1)
     assert choice["blocks"] in (16, 48)
     assert choice["small_work"] in (0, 256)
     assert len(choice["timings"]) == 3

@@ -110,11 +110,16 @@ def test_planted_mistake_is_caught():
     g = golden("inverter_chain32")
     text = str(g["netlist"]).replace("kp=110u", "kp=111u")
     r = port.simulate(text)
+    st, ref = r["stats"], g["stats"]
     same_points = len(r["times"]) == len(g["times"]) and np.array_equal(r["times"], g["times"])
-    if same_points:
-        assert waveform_violation(r["names"], g["times"], g["values"], r["times"], r["values"]) > 1
-    else:
-        assert True
+    # the acceptance predicate of test_port_matches_reference must fail
+    passes = (st["accepted"] == ref[3] and st["rejected"] == ref[4] and
+              st["tranIter"] == ref[1] and same_points and
+              waveform_violation(r["names"], g["times"], g["values"], r["times"],
+                                 r["values"]) < 0.01)
+    assert not passes
+    # and the waveform comparison alone sees it too, at every reference point
+    assert waveform_violation(r["names"], g["times"], g["values"], r["times"], r["values"]) > 1
 
 
 def test_number_evaluation_matches_reference_rules():
