@@ -1,14 +1,16 @@
 """Benchmark: accepted transient timesteps per second on one GB300.
 
-Workloads: c1 (default) one 10,000-transistor BSIM4 random-logic netlist,
-the plain drop-in at scale, over the first 500 ps of its transient; c2
-1024 Monte Carlo instances of uneven size (100-3000 transistors, device
-mismatch) in one launch, first 100 ps; c0 the 32-stage MOS1 inverter chain,
-1216 instances, full 20 ns.
+Workloads: c2 (default) 1024 Monte Carlo instances of uneven size
+(100-3000 transistors, device mismatch) in one launch, a step advancing
+every instance by one window of its 2 ns transient; c4 the same form with
+4096 instances of 100-5000 transistors; c1 one 10,000-transistor BSIM4
+random-logic netlist, the plain drop-in at scale, over the first 500 ps of
+its transient; c0 the 32-stage MOS1 inverter chain, 1216 instances, full
+20 ns.
 
 Engine arm (default): the GPU transient engine runs `.tran` on the step's
-circuits in one launch; a step is one complete transient window of every
-circuit.  `value` is device-timed (inputs resident in HBM, CUDA events
+circuits in one launch; a step advances every circuit by one window of its
+transient (c0, c1: the whole run).  `value` is device-timed (inputs resident in HBM, CUDA events
 around the launches, L2 flushed between steps); `e2e` is the same metric
 through the public C ABI starting from host netlist text (compile, upload,
 run, read back the accepted points).
@@ -289,23 +291,27 @@ class Windows:
         n = len(circuits)
         self.prev = [(0, 0, 0)] * n
         self.fresh = [True] * n
+        self.failed = {}      # instance -> engine status; failed instances leave the batch
 
     def step(self):
         E = self.E
         w = self.j % self.nw
         t_end = (w + 1) * self.dt if w < self.nw - 1 else 2.0 * self.tstop
-        sec = E.run_window(self.cs, t_end)
-        gained = []
-        for i, c in enumerate(self.cs):
-            r = c.results()
+        live = [i for i in range(len(self.cs)) if i not in self.failed]
+        sec = E.run_window([self.cs[i] for i in live], t_end)
+        gained = [(0, 0, 0)] * len(self.cs)
+        for i in live:
+            r = self.cs[i].results()
             st = int(r[E.R_STATUS])
-            if st not in (0, E.PAUSED):
-                raise SystemExit(f"engine status {st} on instance {i}")
             now = (int(r[E.R_ACCEPTED]), int(r[E.R_NUMITER]), int(r[E.R_REJECTED]))
             base = (0, 0, 0) if self.fresh[i] else self.prev[i]
-            gained.append(tuple(x - y for x, y in zip(now, base)))
+            gained[i] = tuple(x - y for x, y in zip(now, base))
             self.prev[i] = now
             self.fresh[i] = st == 0
+            if st not in (0, E.PAUSED):
+                self.failed[i] = st
+                progress(f"instance {i} stopped with engine status {st} at"
+                         f" {r[E.R_ACCEPTED]} accepted steps; it leaves the batch")
         self.j += 1
         return sec, gained
 
@@ -403,6 +409,11 @@ def engine_arm(args, texts, wdesc, rank, world) -> dict | None:
         accepted_all = accepted
     value = accepted_all / total
     lu_madds = [c.lu_flops() for c in circuits]
+    # free the timed batch (device memory and host images) before the
+    # end-to-end pass opens the workload again
+    failed = dict(win.failed) if win else {}
+    n_windows = win.nw if win else 0
+    win = None
     del circuits
 
     # e2e: host netlist text -> compile/upload -> run -> accepted points on
@@ -475,14 +486,62 @@ def engine_arm(args, texts, wdesc, rank, world) -> dict | None:
                                     f" the first {args.e2e_window}"},
             "batched_vs_plain": value / plain,
             "batched_vs_plain_e2e": e2e["value"] / plain_e2e}
+    if mc and args.predictors:
+        # the batched form with a Newton predictor on every instance, over
+        # the same windows: 3 = the quadratic polynomial guess, 2 = that
+        # plus the learned network's correction (trained here on the GPU on
+        # plain trajectories of seeded random-logic circuits, untimed)
+        forms = out_extra.setdefault("forms", {})
+        for kind in [int(k) for k in args.predictors.split(",") if k.strip()]:
+            params, train_info = None, None
+            if kind == 2:
+                from ngspice_gb300 import netlists, predictor
+                tt = time.perf_counter()
+                train = [netlists.random_logic(n_transistors=150 + 15 * s, seed=500 + s,
+                                               tstop="150p") for s in range(args.learn_circuits)]
+                data = predictor.collect(train)
+                params, losses = predictor.train(data, steps=args.learn_steps, lr=args.learn_lr)
+                train_info = {"circuits": args.learn_circuits, "steps": args.learn_steps,
+                              "seconds": time.perf_counter() - tt,
+                              "loss_first": float(losses[0]), "loss_last": float(losses[-1])}
+                progress(f"network trained in {train_info['seconds']:.1f} s")
+            cs = open_all(texts)
+            for c in cs:
+                c.set_predictor(kind, params)
+            pw = Windows(E, cs, dt, tstop)
+            for _ in range(first_timed_window):
+                pw.step()
+            k_sec = k_acc = k_it = 0
+            for _ in range(args.steps):
+                flush_l2()
+                sec, g = pw.step()
+                k_sec += sec
+                k_acc += sum(x[0] for x in g)
+                k_it += sum(x[1] for x in g)
+            guesses = sum(int(c.results()[E.R_GUESSES]) for c in cs)
+            first = sum(int(c.results()[E.R_GUESS1]) for c in cs)
+            pw = None
+            del cs
+            name = {3: "batched_quadratic_guess", 2: "batched_learned"}.get(kind, f"batched_k{kind}")
+            forms[name] = {"value": k_acc / k_sec, "newton_iterations_per_accepted_step":
+                           k_it / max(k_acc, 1), "accepted_on_first_iteration": first,
+                           "steps_from_a_guess": guesses}
+            if train_info:
+                forms[name]["training"] = train_info
+            if "plain_gpu" in forms:
+                forms[name + "_vs_plain"] = (k_acc / k_sec) / forms["plain_gpu"]["value"]
+            progress(f"{name}: {k_acc / k_sec:.1f} accepted steps/s,"
+                     f" {k_it / max(k_acc, 1):.3f} Newton iterations per step")
     if tuned:
         out_extra["refactor_shape"] = {"blocks": tuned["blocks"],
                                        "one_block_levels_up_to": tuned["small_work"]}
+    if failed:
+        out_extra["failed_instances"] = {str(i): st for i, st in failed.items()}
     if mc:
         out_extra["windows"] = {
             "window": args.window, "transient": args.tstop or DEFAULT_WINDOW[args.workload],
             "timed": f"windows {first_timed_window}..{first_timed_window + args.steps - 1}"
-                     f" (cycling over {win.nw} windows of the transient; the window after the"
+                     f" (cycling over {n_windows} windows of the transient; the window after the"
                      " last one starts fresh runs)"}
 
     pk = peaks()
@@ -640,6 +699,12 @@ def main():
                          " its transient")
     ap.add_argument("--e2e-window", default="200p",
                     help="Monte Carlo workloads: transient span of the end-to-end pass")
+    ap.add_argument("--predictors", default="3,2",
+                    help="Monte Carlo workloads: Newton predictors also timed on the batch"
+                         " (3 quadratic guess, 2 with the learned network; empty: none)")
+    ap.add_argument("--learn-circuits", type=int, default=24)
+    ap.add_argument("--learn-steps", type=int, default=3000)
+    ap.add_argument("--learn-lr", type=float, default=1e-3)
     ap.add_argument("--plain-sample", type=int, default=4,
                     help="instances of a Monte Carlo workload timed through the plain drop-in")
     ap.add_argument("--instances", type=int, default=0,

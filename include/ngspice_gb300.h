@@ -198,6 +198,29 @@ NGSF_API int ngsf_node_graph(const ngsf_handle *h, int *nv, int *nedges, int *vn
  * a = |d1| + |d2| (quiet nodes keep the quadratic extrapolation). */
 NGSF_API int ngsf_set_predictor(ngsf_handle *h, int kind, const float *params);
 
+/* Synchronised runs: the step hand-over of the reference's shared library
+ * (GetSyncData through sharedsync, src/sharedspice.c:2437-2490, called
+ * from src/spicelib/analysis/dctran.c:598-601 and :937-960).  With sync on,
+ * ngsf_run_window also stops (status -3) at every point where the
+ * reference calls sharedsync; ngsf_sync_point reports the stop and
+ * ngsf_sync_reply hands back the caller's delta and return value before
+ * the next ngsf_run_window continues the run.  A stop costs a kernel exit
+ * and relaunch, so synchronised runs suit single circuits driven step by
+ * step; a batch keeps sync off. */
+NGSF_API int ngsf_set_sync(ngsf_handle *h, int on);
+/* 1 when h is stopped at a sync point, else 0.  *loc: 0 before a step
+ * (after the breakpoint adjustment of delta), 1 after the step's Newton
+ * and truncation-error verdict; *redostep: 1 when the engine rejected the
+ * step (its time is then already moved back); *time, *delta: CKTtime and
+ * CKTdelta; *olddelta: the step just tried (0 at loc 0).  Any pointer may
+ * be NULL. */
+NGSF_API int ngsf_sync_point(const ngsf_handle *h, int *loc, int *redostep, double *time,
+                             double *delta, double *olddelta);
+/* The caller's answer: the delta of the next step (> 0) and 1 to redo the
+ * step (at loc 1 an accepted step is then discarded and counted as
+ * rejected; at loc 0 the reference only counts a rejection). */
+NGSF_API int ngsf_sync_reply(ngsf_handle *h, double delta, int redo);
+
 /* Whether the circuit runs over the whole grid when it is alone or in a
  * batch of at most four (wide), and with how many blocks. */
 NGSF_API int ngsf_wide_info(const ngsf_handle *h, int *wide, int *blocks);
@@ -254,7 +277,7 @@ typedef struct {
     double time;            /* CKTtime */
     double delta;           /* CKTdelta */
     double deltaOld[3];     /* CKTdeltaOld[0..2] */
-    double ag[2];           /* CKTag[0..1] (NIcomCof) */
+    double ag[3];           /* CKTag[0..2] (NIcomCof; ag[2]: Gear order 2) */
     double gmin;            /* CKTgmin (junction gmin of the devices) */
     double srcFact;         /* CKTsrcFact (source stepping) */
     double diagGmin;        /* CKTdiagGmin (added to the diagonal when factoring) */

@@ -87,8 +87,14 @@ typedef int(GetSyncData)(double, double *, double, int, int, int, void *);
 IMPEXP int ngSpice_Init(SendChar *printfcn, SendStat *statfcn, ControlledExit *ngexit,
                         SendData *sdata, SendInitData *sinitdata, BGThreadRunning *bgtrun,
                         void *userData);
-/* sharedspice.h:398; the engine advances time on the GPU without per-step
- * host synchronisation, so GetSyncData is recorded but not called. */
+/* sharedspice.h:398; with syncdat set, a transient stops at the two
+ * points where the reference calls sharedsync (before each step, and after
+ * each step's verdict) and calls syncdat there with the reference's
+ * arguments and meaning (sharedspice.c:2437-2490): the callback may change
+ * the next delta and, by returning 1, redo the step; delta is kept short of
+ * the final time as the reference keeps it.  Each stop is a kernel exit and
+ * relaunch.  The external-source callbacks (vsrcdat, isrcdat) are recorded
+ * but not called: netlists with EXTERNAL sources are refused. */
 IMPEXP int ngSpice_Init_Sync(GetVSRCData *vsrcdat, GetISRCData *isrcdat,
                              GetSyncData *syncdat, int *ident, void *userData);
 /* sharedspice.h:403; a transient runs on the GPU in 64 windows of its

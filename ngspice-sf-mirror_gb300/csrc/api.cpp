@@ -13,6 +13,7 @@
  */
 #include <algorithm>
 #include <atomic>
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -390,6 +391,53 @@ NGSF_API int ngsf_set_predictor(ngsf_handle *h, int kind, const float *params)
     return 0;
 }
 
+NGSF_API int ngsf_set_sync(ngsf_handle *h, int on)
+{
+    if (!h || !h->p.dev)
+        return fail("ngsf_set_sync: null or host-only handle");
+    try {
+        h->p.dev->set_sync(on != 0);
+    } catch (const std::exception &e) {
+        return fail(e.what());
+    }
+    return 0;
+}
+
+NGSF_API int ngsf_sync_point(const ngsf_handle *h, int *loc, int *redostep, double *time,
+                             double *delta, double *olddelta)
+{
+    if (!h || h->p.ires.size() < NGSF_R_ALL || h->p.fres.size() < NGSF_F_ALL)
+        return 0;
+    const int at = h->p.ires[NGSF_R_SYNCLOC];
+    if (h->p.ires[NGSF_R_STATUS] != NGSF_HELD || at == 0)
+        return 0;
+    if (loc)
+        *loc = at - 1;
+    if (redostep)
+        *redostep = h->p.ires[NGSF_R_SYNCREDO];
+    if (time)
+        *time = h->p.fres[NGSF_F_TIME];
+    if (delta)
+        *delta = h->p.fres[NGSF_F_DELTA];
+    if (olddelta)
+        *olddelta = at == 1 ? 0.0 : h->p.fres[NGSF_F_OLDDELTA];
+    return 1;
+}
+
+NGSF_API int ngsf_sync_reply(ngsf_handle *h, double delta, int redo)
+{
+    if (!ngsf_sync_point(h, nullptr, nullptr, nullptr, nullptr, nullptr))
+        return fail("ngsf_sync_reply: the circuit is not stopped at a sync point");
+    if (!(delta > 0.0) || !std::isfinite(delta))
+        return fail("ngsf_sync_reply: delta must be positive and finite");
+    try {
+        h->p.dev->sync_reply(delta, redo ? 1 : 0);
+    } catch (const std::exception &e) {
+        return fail(e.what());
+    }
+    return 0;
+}
+
 }  // extern "C"
 
 /* ====================================================================== */
@@ -416,6 +464,7 @@ struct Shared {
     SendData *datfcn = nullptr;
     SendInitData *initfcn = nullptr;
     BGThreadRunning *bgfcn = nullptr;
+    GetSyncData *syncfcn = nullptr;
     void *user = nullptr;
     int ident = 0;
     std::string deck;                 /* current circuit text */
@@ -529,7 +578,8 @@ int continue_tran(bool *halted)
         vv[i].is_complex = false;
         pv[i] = &vv[i];
     }
-    for (; S.activeWindow < kStreamWindows; S.activeWindow++) {
+    const double delmin = h->p.img.opt.delmin;
+    while (S.activeWindow < kStreamWindows) {
         const int k = S.activeWindow;
         const double until = k + 1 == kStreamWindows ? 2 * tstop : tstop * (k + 1) / kStreamWindows;
         if (ngsf_run_window(&h, 1, until, 0, nullptr)) {
@@ -575,8 +625,34 @@ int continue_tran(bool *halted)
             finish_tran(1);
             return 1;
         }
-        if (S.haltReq.load()) {
+        int loc = 0, redo = 0;
+        double time = 0, delta = 0, olddelta = 0;
+        const bool atSync = ngsf_sync_point(h, &loc, &redo, &time, &delta, &olddelta) != 0;
+        if (atSync) {
+            /* sharedsync (sharedspice.c:2437-2490): the caller may change
+             * delta and ask for the step again; delta stays short of the
+             * final time */
+            int ret = 0;
+            if (S.syncfcn)
+                ret = S.syncfcn(time, &delta, olddelta, redo, S.ident, loc, S.user);
+            if (redo) {
+                if (time + delta > tstop)
+                    delta = tstop - time - 1.1 * delmin;
+            } else if (time + delta > tstop) {
+                double nd = tstop - time - 1.1 * delmin;
+                if (nd <= 0.0)
+                    nd = tstop - time;
+                delta = nd;
+            }
+            if (ngsf_sync_reply(h, delta, ret)) {
+                say("stderr Error: %s", ngsf_last_error());
+                finish_tran(1);
+                return 1;
+            }
+        } else {
             S.activeWindow++;
+        }
+        if (S.haltReq.load()) {
             *halted = true;
             return 0;
         }
@@ -650,6 +726,11 @@ int do_tran(const std::string &tranArgs)
         S.activePlot = plot.get();
         S.plots.push_back(std::move(plot));
         S.cur = (int)S.plots.size() - 1;
+    }
+    if (S.syncfcn && ngsf_set_sync(h, 1)) {
+        say("stderr Error: %s", ngsf_last_error());
+        ngsf_close(h);
+        return 1;
     }
     S.active = h;
     S.activeWindow = 0;
@@ -798,8 +879,8 @@ IMPEXP int ngSpice_Init_Sync(GetVSRCData *vsrcdat, GetISRCData *isrcdat, GetSync
 {
     (void)vsrcdat;
     (void)isrcdat;
-    (void)syncdat;
     std::lock_guard<std::recursive_mutex> g(S.mu);
+    S.syncfcn = syncdat;
     if (ident)
         S.ident = *ident;
     if (userData)

@@ -1510,9 +1510,9 @@ NGSF_HD inline int bsim4_eval(const B4Ctx &x, const double *P, size_t ps, double
             st1[B4S_QG] = st0[B4S_QG];
             st1[B4S_QD] = st0[B4S_QD];
         }
-        dev_integrate(x, st0, st1, B4S_QB);
-        dev_integrate(x, st0, st1, B4S_QG);
-        dev_integrate(x, st0, st1, B4S_QD);
+        dev_integrate(x, st0, st1, st2, B4S_QB);
+        dev_integrate(x, st0, st1, st2, B4S_QG);
+        dev_integrate(x, st0, st1, st2, B4S_QD);
         ceqqg = st0[B4S_CQG] - gcggb * vgb + gcgdb * vbd + gcgsb * vbs;
         ceqqd = st0[B4S_CQD] - gcdgb * vgb + gcddb * vbd + gcdsb * vbs;
         ceqqb = st0[B4S_CQB] - gcbgb * vgb + gcbdb * vbd + gcbsb * vbs;

@@ -288,12 +288,16 @@ int mk_internal(Circuit &c, const std::string &name, bool voltage)
 void compile(Circuit &c, Image &img)
 {
     const Options &o = c.opt;
-    if (o.method != 0)
-        throw NetlistError("only the trapezoidal integration method is implemented");
+    if (o.method != 0 && o.method != 1)
+        throw NetlistError("unknown integration method");
     if (c.uic)
         throw NetlistError(".tran uic is not supported by this engine");
+    /* the engine keeps CKTstate0..3 (maxord + 2 vectors): trapezoidal
+     * orders 1-2 and Gear orders 1-2; Gear above order 2 would need up to
+     * eight */
     if (o.maxord < 1 || o.maxord > 2)
-        throw NetlistError("maxord must be 1 or 2 for the trapezoidal method");
+        throw NetlistError(o.method == 1 ? "maxord must be 1 or 2 (Gear orders 3-6 are not built)"
+                                         : "maxord must be 1 or 2 for the trapezoidal method");
 
     /* ---------------- setup: internal nodes, branches, states -------- */
     std::vector<std::array<double, M1P_COUNT>> m1p;

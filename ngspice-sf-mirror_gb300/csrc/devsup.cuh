@@ -115,26 +115,45 @@ NGSF_HD inline double dev_fetlim(double vnew, double vold, double vto)
 /* DEVqmeyer: Meyer gate capacitances (devsup.c:674-736) */
 
 /* Iteration context a device load reads besides its own instance:
- * CKTmode, CKTorder, CKTgmin, CKTdelta, CKTdeltaOld[1], CKTag[0..1],
- * CKTrhsOld and the state vectors CKTstate0..2. */
+ * CKTmode, CKTorder, CKTintegrateMethod (gear), CKTgmin, CKTdelta,
+ * CKTdeltaOld[1], CKTag[0..2], CKTrhsOld and the state vectors
+ * CKTstate0..2. */
 struct DevCtx {
     int mode;
     int order;
-    double gmin, delta, deltaOld1, ag0, ag1;
+    int gear;
+    double gmin, delta, deltaOld1, ag0, ag1, ag2;
     const double *rhsOld;
     double *st0;
     double *st1;
     const double *st2;
 };
 
-/* NIintegrate, trapezoidal (src/maths/ni/niinteg.c:18-80) for a charge at
- * state offset q whose current lives at q+1 */
-NGSF_HD inline void dev_integrate(const DevCtx &x, double *st0, const double *st1, int q)
+/* NIintegrate (src/maths/ni/niinteg.c:18-80) for a charge at state offset
+ * q whose current lives at q+1 (st0..st2: this instance's CKTstate0..2).
+ * Trapezoidal orders 1 and 2; Gear sums ag[order]*q_order down to
+ * ag[0]*q_0 from zero, in that order. */
+NGSF_HD inline double ni_integ_current(int gear, int order, double ag0, double ag1, double ag2,
+                                       const double *st0, const double *st1,
+                                       const double *st2, int q)
 {
-    if (x.order == 1)
-        st0[q + 1] = x.ag0 * st0[q] + x.ag1 * st1[q];
-    else
-        st0[q + 1] = -st1[q + 1] * x.ag1 + x.ag0 * (st0[q] - st1[q]);
+    if (gear) {
+        double c = 0;
+        if (order >= 2)
+            c += ag2 * st2[q];
+        c += ag1 * st1[q];
+        c += ag0 * st0[q];
+        return c;
+    }
+    if (order == 1)
+        return ag0 * st0[q] + ag1 * st1[q];
+    return -st1[q + 1] * ag1 + ag0 * (st0[q] - st1[q]);
+}
+
+NGSF_HD inline void dev_integrate(const DevCtx &x, double *st0, const double *st1,
+                                  const double *st2, int q)
+{
+    st0[q + 1] = ni_integ_current(x.gear, x.order, x.ag0, x.ag1, x.ag2, st0, st1, st2, q);
 }
 
 /* DEVpred (src/spicelib/devices/devsup.c:815-827): linear extrapolation of

@@ -148,7 +148,7 @@ NGSF_HD inline int dio_eval(const DevCtx &x, const double *P, size_t ps, const i
         st0[DIS_SRCAPCHARGE] = 0;
         if (mode & NGSF_MODEINITTRAN)
             st1[DIS_CAPCHARGE] = st0[DIS_CAPCHARGE];
-        dev_integrate(x, st0, st1, DIS_CAPCHARGE);
+        dev_integrate(x, st0, st1, st2, DIS_CAPCHARGE);
         gd = gd + x.ag0 * capd;
         cd = cd + st0[DIS_CAPCURRENT];
         if (mode & NGSF_MODEINITTRAN)

@@ -30,6 +30,7 @@
 #include <float.h>
 #include <math.h>
 #include <string.h>
+#include <stddef.h>
 #include <stdint.h>
 
 #include "../../include/ngspice_gb300.h"
@@ -70,6 +71,10 @@ struct Ctl {
     /* CKTop fallbacks: gmin stepping and source stepping (cktop.c) */
     int opPhase, gi, itersBefore;
     double gmin, diagGmin, srcFact, factor, oldGmin, gtarget, startgmin, convFact, raise;
+    /* synchronised runs: the sharedsync point the run stopped at (0 none,
+     * 1 + the reference's loc), redostep as set by the time loop, and the
+     * caller's answer (1: redo the step) */
+    int syncLoc, syncRedo, syncReply;
 };
 
 /* Per-phase clock record (C.prof, optional): thread 0 of the circuit's
@@ -181,15 +186,14 @@ __device__ void dev_qmeyer(double vgs, double vgd, double von, double vdsat,
     }
 }
 
-/* NIintegrate, trapezoidal (src/maths/ni/niinteg.c:18-80) */
-__device__ void ni_integrate(const Ctl &s, double *st0, const double *st1,
-                             double *geq, double *ceq, double cap, int qcap)
+/* NIintegrate (src/maths/ni/niinteg.c:18-80), trapezoidal or Gear; st0..st2
+ * are the instance's CKTstate0..2 */
+__device__ void ni_integrate(const ngsf_ckt_t &C, const Ctl &s, double *st0, const double *st1,
+                             const double *st2, double *geq, double *ceq, double cap, int qcap)
 {
     int ccap = qcap + 1;
-    if (s.order == 1)
-        st0[ccap] = s.ag[0] * st0[qcap] + s.ag[1] * st1[qcap];
-    else
-        st0[ccap] = -st1[ccap] * s.ag[1] + s.ag[0] * (st0[qcap] - st1[qcap]);
+    st0[ccap] = ni_integ_current(C.opt.method, s.order, s.ag[0], s.ag[1], s.ag[2], st0, st1, st2,
+                                 qcap);
     *ceq = st0[ccap] - s.ag[0] * st0[qcap];
     *geq = s.ag[0] * cap;
 }
@@ -333,7 +337,7 @@ __device__ void cap_load(const ngsf_ckt_t &C, const Ctl &s, const Iter &it, int 
                     it.st1[st] = it.st0[st];
             }
             double geq, ceq;
-            ni_integrate(s, it.st0, it.st1, &geq, &ceq, cap, st);
+            ni_integrate(C, s, it.st0, it.st1, it.st2, &geq, &ceq, cap, st);
             if (mode & NGSF_MODEINITTRAN)
                 it.st1[st + 1] = it.st0[st + 1];
             g = m * geq;
@@ -626,11 +630,11 @@ __device__ int mos1_load_one(const ngsf_ckt_t &C, const Ctl &s, const Iter &it, 
         if ((mode & NGSF_MODETRAN) ||
             ((mode & NGSF_MODEINITTRAN) && !(mode & NGSF_MODEUIC))) {
             double geq, ceq;
-            ni_integrate(s, st0, st1, &geq, &ceq, capbd, M1S_QBD);
+            ni_integrate(C, s, st0, st1, st2, &geq, &ceq, capbd, M1S_QBD);
             gbd += geq;
             cbd += st0[M1S_CQBD];
             cd -= st0[M1S_CQBD];
-            ni_integrate(s, st0, st1, &geq, &ceq, capbs, M1S_QBS);
+            ni_integrate(C, s, st0, st1, st2, &geq, &ceq, capbs, M1S_QBS);
             gbs += geq;
             cbs += st0[M1S_CQBS];
         }
@@ -696,9 +700,9 @@ __device__ int mos1_load_one(const ngsf_ckt_t &C, const Ctl &s, const Iter &it, 
             st0[M1S_CQGD] = 0;
         if (capgb == 0)
             st0[M1S_CQGB] = 0;
-        ni_integrate(s, st0, st1, &gcgs, &ceqgs, capgs, M1S_QGS);
-        ni_integrate(s, st0, st1, &gcgd, &ceqgd, capgd, M1S_QGD);
-        ni_integrate(s, st0, st1, &gcgb, &ceqgb, capgb, M1S_QGB);
+        ni_integrate(C, s, st0, st1, st2, &gcgs, &ceqgs, capgs, M1S_QGS);
+        ni_integrate(C, s, st0, st1, st2, &gcgd, &ceqgd, capgd, M1S_QGD);
+        ni_integrate(C, s, st0, st1, st2, &gcgb, &ceqgb, capgb, M1S_QGB);
         ceqgs = ceqgs - gcgs * vgs + s.ag[0] * st0[M1S_QGS];
         ceqgd = ceqgd - gcgd * vgd + s.ag[0] * st0[M1S_QGD];
         ceqgb = ceqgb - gcgb * vgb + s.ag[0] * st0[M1S_QGB];
@@ -813,8 +817,10 @@ __device__ int dio_load_one(const ngsf_ckt_t &C, const Ctl &s, const Iter &it, i
     x.gmin = s.gmin;
     x.delta = s.delta;
     x.deltaOld1 = s.deltaOld[1];
+    x.gear = C.opt.method;
     x.ag0 = s.ag[0];
     x.ag1 = s.ag[1];
+    x.ag2 = s.ag[2];
     x.rhsOld = it.rhsOld;
     x.st0 = it.st0;
     x.st1 = const_cast<double *>(it.st1);
@@ -835,8 +841,10 @@ __device__ int bsim4_load_one(const ngsf_ckt_t &C, const Ctl &s, const Iter &it,
     x.gmin = s.gmin;
     x.delta = s.delta;
     x.deltaOld1 = s.deltaOld[1];
+    x.gear = C.opt.method;
     x.ag0 = s.ag[0];
     x.ag1 = s.ag[1];
+    x.ag2 = s.ag[2];
     x.rhsOld = it.rhsOld;
     x.st0 = it.st0;
     x.st1 = const_cast<double *>(it.st1);
@@ -1093,30 +1101,40 @@ __device__ int ckt_load(const ngsf_ckt_t &C, Ctl &s, const Iter &it)
  * finite: the host then chooses new pivots from this matrix (the reference
  * re-factors with pivoting when refactoring fails,
  * src/maths/ni/niiter.c:161-195; klu_refactor fails on a zero pivot only,
- * src/maths/KLU/klusmp.c:591-602).  In the operating point (gmin and
+ * src/maths/KLU/klusmp.c:591-602).  An L entry above a growth limit also
+ * asks for new pivots: in the operating point always NGSF_GROWTH (gmin and
  * source stepping move the matrix far from the one the pivots were chosen
- * on) an L entry above NGSF_GROWTH also asks for new pivots; the transient
- * refactors on its pivots like the reference. */
+ * on), in the transient C.tran_growth (0: none).  The pivots are chosen
+ * with the threshold 1e-3 that bounds |L| by 1e3 on the matrix they were
+ * chosen on; KLU's ordering keeps later matrices near that bound, the
+ * Markowitz plan occasionally does not (L entries past 1e6 in 4 of the
+ * 4096 Monte Carlo instances, whose Newton then fails where the
+ * reference's converges), and a re-pivot there restores it. */
 #define NGSF_GROWTH 1e6
-__device__ __forceinline__ double growth_limit(const Ctl &s)
+__device__ __forceinline__ double growth_limit(const ngsf_ckt_t &C, const Ctl &s)
 {
-    return (s.mode & (NGSF_MODEDCOP | NGSF_MODETRANOP)) ? NGSF_GROWTH : DBL_MAX;
+    if (s.mode & (NGSF_MODEDCOP | NGSF_MODETRANOP))
+        return NGSF_GROWTH;
+    return C.tran_growth > 0.0 ? C.tran_growth : DBL_MAX;
 }
 
 /* Right-looking refactorization on the fixed pivot sequence, level by
  * level of the column dependency graph.  Level l first checks its pivots
- * and scales the L entries of its pivot columns by the pivots' inverses,
- * then every later entry receives the products L(i,k) * U(k,j) of the
- * level's pivots, one thread per destination, products in a fixed order.
- * FP64 is scarce on GB300 (a warp's division is about ten dependent
- * fused multiply-adds), so a pivot is inverted once -- by the thread that
- * writes its last update, or at the start when nothing updates it -- and
- * the L entries and the backward solve multiply by the inverse; the
- * products are fused multiply-adds.  The packed descriptors (sc_pk,
- * ud_pk) carry every index an entry needs in one load, and each thread
- * keeps NGSF_RL_ILP entries' loads in flight before it stores: within a
- * level no destination is read by another entry of the level, so the
- * reordering changes no value. */
+ * and divides the L entries of its pivot columns by their pivots, then
+ * every later entry receives the products L(i,k) * U(k,j) of the level's
+ * pivots, one thread per destination, products in a fixed order.  The
+ * arithmetic is klu_refactor's (src/maths/KLU/klu_refactor.c): a quotient
+ * per L entry and an unfused multiply and subtract per product.  Pivot
+ * inverses in the L scaling and fused products were tried: on a few
+ * matrices whose pivots grow by more than 1e6 in the transient that
+ * rounding let Newton fail where klu's arithmetic converges, so the
+ * inverse (one per pivot, by the thread that writes the pivot's last
+ * update, or at the start when nothing updates it) serves only the
+ * backward solve.  The packed descriptors (sc_pk, ud_pk) carry every
+ * index an entry needs in one load, and each thread keeps NGSF_RL_ILP
+ * entries' loads in flight before it stores: within a level no
+ * destination is read by another entry of the level, so the reordering
+ * changes no value. */
 #define NGSF_RL_SMALL 1024
 #define NGSF_RL_ILP 4
 __device__ __forceinline__ int rl_level_work(const ngsf_ckt_t &C, int l)
@@ -1124,7 +1142,7 @@ __device__ __forceinline__ int rl_level_work(const ngsf_ckt_t &C, int l)
     return C.ud_ptr[l + 1] - C.ud_ptr[l] + C.sc_ptr[l + 1] - C.sc_ptr[l];
 }
 
-/* level l, first half (threads t of T): pivot checks, L(:,k) *= 1/U(k,k) */
+/* level l, first half (threads t of T): pivot checks, L(:,k) /= U(k,k) */
 __device__ __forceinline__ int rl_scale(const ngsf_ckt_t &C, int l, int t, int T, double growth)
 {
     int bad = 0;
@@ -1146,12 +1164,12 @@ __device__ __forceinline__ int rl_scale(const ngsf_ckt_t &C, int l, int t, int T
         for (int j = 0; j < NGSF_RL_ILP; j++)
             if (q[j].x >= 0) {
                 x[j] = C.lux[q[j].x];
-                v[j] = C.uinv[q[j].y];
+                v[j] = C.lux[q[j].y];
             }
 #pragma unroll
         for (int j = 0; j < NGSF_RL_ILP; j++)
             if (q[j].x >= 0) {
-                const double l_ik = x[j] * v[j];
+                const double l_ik = x[j] / v[j];
                 C.lux[q[j].x] = l_ik;
                 if (!(fabs(l_ik) <= growth))
                     bad = 1;
@@ -1186,11 +1204,11 @@ __device__ __forceinline__ void rl_update(const ngsf_ckt_t &C, int l, int t, int
 #pragma unroll
         for (int j = 0; j < NGSF_RL_ILP; j++)
             if (d + j * T < d1) {
-                double acc = fma(-x[j], y[j], a[j]);
+                double acc = __dsub_rn(a[j], __dmul_rn(x[j], y[j]));
                 if (q[j].x < 0) {
                     const int dj = d + j * T;
                     for (int c = C.ud_cptr[dj] + 1; c < C.ud_cptr[dj + 1]; c++)
-                        acc = fma(-C.lux[C.ud_l[c]], C.lux[C.ud_u[c]], acc);
+                        acc = __dsub_rn(acc, __dmul_rn(C.lux[C.ud_l[c]], C.lux[C.ud_u[c]]));
                 }
                 C.lux[dst[j]] = acc;
                 if (q[j].w >= 0)
@@ -1225,7 +1243,7 @@ __device__ void solve_pack(const ngsf_ckt_t &C, int t, int T)
 __device__ int lu_factor_rl(const ngsf_ckt_t &C, Ctl &s, int b, int nbAll)
 {
     int bad = 0;
-    const double growth = growth_limit(s);
+    const double growth = growth_limit(C, s);
     if (nbAll <= 1) {
         for (int q = threadIdx.x; q < C.nlu; q += blockDim.x)
             C.lux[q] = 0.0;
@@ -1325,7 +1343,7 @@ __device__ int lu_factor(const ngsf_ckt_t &C, Ctl &s)
         __syncthreads();
     }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nwarps = blockDim.x >> 5;
-    const double growth = growth_limit(s);
+    const double growth = growth_limit(C, s);
     int bad = 0;
     for (int l = 0; l < C.nlevels; l++) {
         for (int c = C.lvl_ptr[l] + warp; c < C.lvl_ptr[l + 1]; c += nwarps) {
@@ -1419,10 +1437,63 @@ __device__ __forceinline__ void solve_apply(const SolveRow &p, double *w, const 
     w[p.row] = back ? acc * p.piv : acc;
 }
 
+/* A warp's long row of a solve level (more than 32 terms): each lane's
+ * first NGSF_SOLVE_HPF terms of its lane-strided share, fetched before the
+ * barrier like SolveRow. */
+#define NGSF_SOLVE_HPF 4
+struct SolveHeavy {
+    int k, q0, q1;
+    double v[NGSF_SOLVE_HPF];
+    int c[NGSF_SOLVE_HPF];
+};
+
+__device__ __forceinline__ void heavy_fetch(SolveHeavy &h, const int *hrow, int hh, int hEnd,
+                                            const int *rptr, const double *val,
+                                            const int *col, int lane)
+{
+    h.k = -1;
+    if (hh < hEnd) {
+        h.k = hrow[hh];
+        h.q0 = rptr[h.k];
+        h.q1 = rptr[h.k + 1];
+#pragma unroll
+        for (int j = 0; j < NGSF_SOLVE_HPF; j++) {
+            const int q = h.q0 + lane + 32 * j;
+            if (q < h.q1) {
+                h.v[j] = val[q];
+                h.c[j] = col[q];
+            }
+        }
+    }
+}
+
+/* the warp's row: lane-strided partial sums in term order, a fixed
+ * butterfly, then w[k] -= sum (x 1/pivot) by lane 0 */
+__device__ __forceinline__ void heavy_apply(const ngsf_ckt_t &C, const SolveHeavy &h, double *w,
+                                            const double *val, const int *col, int lane,
+                                            bool back)
+{
+    double acc = 0.0;
+#pragma unroll
+    for (int j = 0; j < NGSF_SOLVE_HPF; j++) {
+        const int q = h.q0 + lane + 32 * j;
+        if (q < h.q1)
+            acc = fma(h.v[j], w[h.c[j]], acc);
+    }
+    for (int q = h.q0 + lane + 32 * NGSF_SOLVE_HPF; q < h.q1; q += 32)
+        acc = fma(val[q], w[col[q]], acc);
+    for (int o = 16; o > 0; o >>= 1)
+        acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (lane == 0)
+        w[h.k] = back ? (w[h.k] - acc) * C.uinv[h.k] : w[h.k] - acc;
+}
+
 /* One sweep (forward over L, or backward over U with the division by the
  * pivot): per level, rows of up to 32 terms by one thread each, terms in
  * order; longer rows (listed per level in hptr/hrow) by a warp, with
- * lane-strided partial sums and a fixed butterfly. */
+ * lane-strided partial sums and a fixed butterfly.  Each thread's first
+ * row and each warp's first long row of the next level are fetched before
+ * the barrier. */
 __device__ __forceinline__ void solve_sweep(const ngsf_ckt_t &C, double *w, int nlev, const int *lptr,
                             const int4 *desc, const double *val, const int *col,
                             const int *rptr, const int *hptr, const int *hrow, bool back)
@@ -1430,9 +1501,13 @@ __device__ __forceinline__ void solve_sweep(const ngsf_ckt_t &C, double *w, int 
     const int t = threadIdx.x, T = blockDim.x;
     const int warp = t >> 5, lane = t & 31, nwarps = T >> 5;
     SolveRow p;
+    SolveHeavy hv;
     p.row = -1;
-    if (nlev > 0)
+    hv.k = -1;
+    if (nlev > 0) {
         solve_fetch(p, desc, lptr[0] + t, lptr[1], val, col, C.uinv, back);
+        heavy_fetch(hv, hrow, hptr[0] + warp, hptr[1], rptr, val, col, lane);
+    }
     for (int l = 0; l < nlev; l++) {
         const int r1 = lptr[l + 1];
         solve_apply(p, w, val, col, back);
@@ -1441,18 +1516,17 @@ __device__ __forceinline__ void solve_sweep(const ngsf_ckt_t &C, double *w, int 
             solve_fetch(q, desc, r, r1, val, col, C.uinv, back);
             solve_apply(q, w, val, col, back);
         }
-        for (int h = hptr[l] + warp; h < hptr[l + 1]; h += nwarps) {
-            const int k = hrow[h];
-            double acc = 0.0;
-            for (int q = rptr[k] + lane; q < rptr[k + 1]; q += 32)
-                acc = fma(val[q], w[col[q]], acc);
-            for (int o = 16; o > 0; o >>= 1)
-                acc += __shfl_xor_sync(0xffffffffu, acc, o);
-            if (lane == 0)
-                w[k] = back ? (w[k] - acc) * C.uinv[k] : w[k] - acc;
+        if (hv.k >= 0)
+            heavy_apply(C, hv, w, val, col, lane, back);
+        for (int h = hptr[l] + warp + nwarps; h < hptr[l + 1]; h += nwarps) {
+            SolveHeavy q;
+            heavy_fetch(q, hrow, h, hptr[l + 1], rptr, val, col, lane);
+            heavy_apply(C, q, w, val, col, lane, back);
         }
-        if (l + 1 < nlev)
+        if (l + 1 < nlev) {
             solve_fetch(p, desc, r1 + t, lptr[l + 2], val, col, C.uinv, back);
+            heavy_fetch(hv, hrow, hptr[l + 1] + warp, hptr[l + 2], rptr, val, col, lane);
+        }
         __syncthreads();
     }
 }
@@ -1501,7 +1575,7 @@ __device__ int conv_test(const ngsf_ckt_t &C, Ctl &s, const Iter &it, bool volta
     return block_or(s, bad);
 }
 
-/* CKTterr (src/spicelib/analysis/cktterr.c:13-79), trapezoidal */
+/* CKTterr (src/spicelib/analysis/cktterr.c:13-79), trapezoidal or Gear */
 __device__ double ckt_terr(const ngsf_ckt_t &C, const Ctl &s, int qcap, double timeStep)
 {
     const ngsf_opts_t &o = C.opt;
@@ -1526,8 +1600,10 @@ __device__ double ckt_terr(const ngsf_ckt_t &C, const Ctl &s, int qcap, double t
         for (int i = 0; i <= j; i++)
             deltmp[i] = deltmp[i + 1] + s.deltaOld[i];
     }
+    /* error constants of the methods by order (cktterr.c:28-39) */
     const double trapCoeff[2] = {.5, .08333333333};
-    double factor = trapCoeff[s.order - 1];
+    const double gearCoeff[2] = {.5, .2222222222};
+    double factor = C.opt.method ? gearCoeff[s.order - 1] : trapCoeff[s.order - 1];
     double del = o.trtol * tol / NG_MAX(o.abstol, factor * fabs(diff[0]));
     if (s.order == 2)
         del = sqrt(del);
@@ -1710,7 +1786,8 @@ __device__ int src_accept(const ngsf_ckt_t &C, Ctl &s, const ngsf_src_t &K)
 /* ---------------------------------------------------------------- */
 /* NIiter                                                            */
 /* ---------------------------------------------------------------- */
-enum { PH_OP = 1, PH_NEXTTIME = 2, PH_STEP = 3, PH_STEP_NIITER = 4, PH_HELD = 5 };
+enum { PH_OP = 1, PH_NEXTTIME = 2, PH_STEP = 3, PH_STEP_NIITER = 4, PH_HELD = 5,
+       PH_SYNC0 = 6, PH_SYNC1 = 7 };
 
 __device__ void capture(const ngsf_ckt_t &C, Ctl &s, const Iter &it)
 {
@@ -1879,9 +1956,54 @@ __device__ int ni_iter(const ngsf_ckt_t &C, Ctl &s, int maxIter, bool resume)
     }
 }
 
-/* NIcomCof, trapezoidal (src/maths/ni/nicomcof.c:17-47) */
+/* NIcomCof (src/maths/ni/nicomcof.c:17-130).  Gear, orders 1 and 2 (the
+ * engine keeps four state vectors): ag solves the corrector system whose
+ * row j holds the j-th powers of (t_n - t_{n-i}) / delta, i = 0..order,
+ * with right-hand side (0, -1/delta, 0, ..); the first column is
+ * (1, 0, ..), so the elimination starts at row and column 1. */
+__device__ void ni_comcof_gear(Ctl &s)
+{
+    const int q = s.order;
+    double mat[3][3];
+    for (int i = 0; i < 7; i++)
+        s.ag[i] = 0;
+    s.ag[1] = -1 / s.delta;
+    double arg = 0;
+    for (int i = 0; i <= q; i++)
+        mat[0][i] = 1;
+    for (int i = 1; i <= q; i++)
+        mat[i][0] = 0;
+    for (int i = 1; i <= q; i++) {
+        arg += s.deltaOld[i - 1];
+        double arg1 = 1;
+        for (int j = 1; j <= q; j++) {
+            arg1 *= arg / s.delta;
+            mat[j][i] = arg1;
+        }
+    }
+    for (int i = 1; i <= q; i++)
+        for (int j = i + 1; j <= q; j++) {
+            mat[j][i] /= mat[i][i];
+            for (int k = i + 1; k <= q; k++)
+                mat[j][k] -= mat[j][i] * mat[i][k];
+        }
+    for (int i = 1; i <= q; i++)
+        for (int j = i + 1; j <= q; j++)
+            s.ag[j] = s.ag[j] - mat[j][i] * s.ag[i];
+    s.ag[q] /= mat[q][q];
+    for (int i = q - 1; i >= 0; i--) {
+        for (int j = i + 1; j <= q; j++)
+            s.ag[i] = s.ag[i] - mat[i][j] * s.ag[j];
+        s.ag[i] /= mat[i][i];
+    }
+}
+
 __device__ void ni_comcof(const ngsf_ckt_t &C, Ctl &s)
 {
+    if (C.opt.method) {
+        ni_comcof_gear(s);
+        return;
+    }
     if (s.order == 1) {
         s.ag[0] = 1 / s.delta;
         s.ag[1] = -1 / s.delta;
@@ -2188,6 +2310,23 @@ __device__ int op_run(const ngsf_ckt_t &C, Ctl &s, bool resume)
  * held circuit stays held; the host releases the batch once no circuit
  * still waits for new pivots, so those early pauses cost short launches
  * instead of one long launch each. */
+/* A synchronised run stops at sharedsync, loc 1 (dctran.c:937-960), after
+ * the step's verdict: redostep 0 (accepted; the phase is already nextTime)
+ * or 1 (rejected; the time is already moved back and delta cut).  The host
+ * hands time, delta and olddelta to the caller and resumes in PH_SYNC1. */
+__device__ int sync_stop(Ctl &s, int redostep)
+{
+    __syncthreads();   /* every warp has read the phase and the step state */
+    if (threadIdx.x == 0) {
+        s.phase = PH_SYNC1;
+        s.syncLoc = 2;
+        s.syncRedo = redostep;
+        s.syncReply = 0;
+    }
+    __syncthreads();
+    return NGSF_HELD;
+}
+
 __device__ int dc_tran(const ngsf_ckt_t &C, Ctl &s, long long maxSteps, bool resume, bool hold)
 {
     const ngsf_opts_t &o = C.opt;
@@ -2298,6 +2437,25 @@ __device__ int dc_tran(const ngsf_ckt_t &C, Ctl &s, long long maxSteps, bool res
                     s.saveDelta = s.delta;
                     s.delta = (b[0] - s.time) / 2.;
                 }
+                s.phase = PH_SYNC0;
+                s.syncLoc = C.sync ? 1 : 0;
+                s.syncRedo = 0;
+            }
+            __syncthreads();
+            /* sharedsync, loc 0 (dctran.c:598-601): a synchronised run
+             * stops here; the caller may change delta */
+            if (C.sync)
+                return NGSF_HELD;
+        }
+        if (s.phase == PH_SYNC0) {
+            resume = false;
+            __syncthreads();   /* every warp has read the phase */
+            if (threadIdx.x == 0) {
+                /* a caller's 1 here only counts a rejection (the time moves
+                 * back by an olddelta of 0; dctran ignores the value) */
+                if (s.syncLoc && s.syncReply)
+                    s.rejected++;
+                s.syncLoc = s.syncReply = 0;
                 for (int i = 5; i >= 0; i--)
                     s.deltaOld[i + 1] = s.deltaOld[i];
                 s.deltaOld[0] = s.delta;
@@ -2308,6 +2466,33 @@ __device__ int dc_tran(const ngsf_ckt_t &C, Ctl &s, long long maxSteps, bool res
                 s.phase = PH_STEP;
             }
             __syncthreads();
+        }
+        if (s.phase == PH_SYNC1) {
+            /* the caller's answer at sharedsync loc 1: an accepted step
+             * goes on to nextTime unless the caller asks to redo it (the
+             * time then moves back by olddelta and the step counts as
+             * rejected, sharedspice.c sharedsync); a rejected step is
+             * tried again with the delta in force */
+            resume = false;
+            __syncthreads();   /* every warp has read the phase */
+            if (threadIdx.x == 0) {
+                const bool redo = s.syncRedo || s.syncReply;
+                if (!s.syncRedo && s.syncReply) {
+                    s.time -= s.olddelta;
+                    s.rejected++;
+                }
+                s.syncLoc = s.syncReply = s.syncRedo = 0;
+                if (redo) {
+                    s.steps++;
+                    s.phase = PH_STEP;
+                } else {
+                    s.phase = PH_NEXTTIME;
+                }
+            }
+            __syncthreads();
+            if (s.phase == PH_STEP && s.steps > maxSteps)
+                return NGSF_E_WATCHDOG;
+            continue;
         }
         if (s.phase == PH_STEP) {
             __syncthreads();   /* every warp has read the phase */
@@ -2376,6 +2561,8 @@ __device__ int dc_tran(const ngsf_ckt_t &C, Ctl &s, long long maxSteps, bool res
                     s.phase = PH_NEXTTIME;
                 }
                 __syncthreads();
+                if (C.sync)
+                    return sync_stop(s, 0);
                 continue;
             }
             const long long tt = prof_t(C);
@@ -2397,6 +2584,8 @@ __device__ int dc_tran(const ngsf_ckt_t &C, Ctl &s, long long maxSteps, bool res
                     s.phase = PH_NEXTTIME;
                 }
                 __syncthreads();
+                if (C.sync)
+                    return sync_stop(s, 0);
                 continue;
             } else {
                 __syncthreads();   /* every warp has compared against delta */
@@ -2417,6 +2606,8 @@ __device__ int dc_tran(const ngsf_ckt_t &C, Ctl &s, long long maxSteps, bool res
                 return NGSF_E_TIMESTEP;
             }
         }
+        if (C.sync)
+            return sync_stop(s, 1);
         if (threadIdx.x == 0) {
             s.steps++;
             s.phase = PH_STEP;
@@ -2545,6 +2736,7 @@ __device__ void run_circuit(const ngsf_ckt_t &C, Ctl &s, int runMode, long long 
             s.diagGmin = 0.0;
             s.srcFact = 1.0;
             s.opPhase = 0;
+            s.syncLoc = s.syncRedo = s.syncReply = 0;
             for (int i = 0; i < 7; i++) {
                 s.ag[i] = 0;
                 s.deltaOld[i] = 0;
@@ -2607,6 +2799,9 @@ __device__ void run_circuit(const ngsf_ckt_t &C, Ctl &s, int runMode, long long 
         C.fresult[NGSF_F_TIME] = s.time;
         C.fresult[NGSF_F_DELTA] = s.delta;
         C.fresult[NGSF_F_DIAGGMIN] = s.diagGmin;
+        C.result[NGSF_R_SYNCLOC] = status == NGSF_HELD ? s.syncLoc : 0;
+        C.result[NGSF_R_SYNCREDO] = s.syncRedo;
+        C.fresult[NGSF_F_OLDDELTA] = s.olddelta;
     }
     prof_add(C, NGSF_P_TOTAL, tRun);
 }
@@ -2648,7 +2843,7 @@ __global__ void __launch_bounds__(NGSF_THREADS) stamp_static_kernel(ngsf_ckt_t C
 /* ---------------------------------------------------------------- */
 struct OpArgs {
     int op, mode, order, types;
-    double time, delta, deltaOld[3], ag0, ag1, gmin, srcFact, diagGmin;
+    double time, delta, deltaOld[3], ag0, ag1, ag2, gmin, srcFact, diagGmin;
 };
 enum { OPK_LOAD = 1, OPK_LUFAC, OPK_SOLVE, OPK_CONV, OPK_TRUNC };
 
@@ -2730,6 +2925,7 @@ op_kernel(const ngsf_ckt_t *ckt, OpArgs a, int solveCap, int *iout, double *dout
             s.deltaOld[k] = a.deltaOld[k];
         s.ag[0] = a.ag0;
         s.ag[1] = a.ag1;
+        s.ag[2] = a.ag2;
         s.order = a.order;
         s.mode = a.mode;
         s.gmin = a.gmin;
@@ -2795,6 +2991,7 @@ eval_kernel(const ngsf_ckt_t *ckt, OpArgs a, int reps)
             s.deltaOld[k] = a.deltaOld[k];
         s.ag[0] = a.ag0;
         s.ag[1] = a.ag1;
+        s.ag[2] = a.ag2;
         s.order = a.order;
         s.mode = a.mode;
         s.gmin = a.gmin;
@@ -2837,6 +3034,19 @@ __global__ void fp64_peak_kernel(double *out, int iters)
 static_assert(sizeof(Ctl) <= NGSF_WIDE_CTL_BYTES, "control block does not fit the wide hand-over");
 
 extern "C" int ngsf_ctl_bytes(void) { return (int)sizeof(Ctl); }
+
+/* The caller's answer to a sharedsync stop, written into the paused run's
+ * saved control block: the delta of the next step and the return value
+ * (1: redo the step). */
+extern "C" cudaError_t ngsf_sync_write(void *ctlsave, double delta, int reply)
+{
+    cudaError_t e = cudaMemcpy((char *)ctlsave + offsetof(Ctl, delta), &delta, sizeof(double),
+                               cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy((char *)ctlsave + offsetof(Ctl, syncReply), &reply, sizeof(int),
+                       cudaMemcpyHostToDevice);
+    return e;
+}
 
 namespace {
 cudaError_t allow_dyn_smem(const void *fn);
@@ -2906,8 +3116,8 @@ extern "C" NGSF_API int ngsf_stamp_initial_static(const ngsf_handle *h, double *
     size_t o_b4h = take((size_t)B4H_COUNT * d->bsim4.n * sizeof(double));
     size_t o_vbrk = take((size_t)d->vsrc.n * sizeof(double));
     size_t o_ibrk = take((size_t)d->isrc.n * sizeof(double));
-    size_t o_res = take(NGSF_R_COUNT * sizeof(int));
-    size_t o_fres = take(NGSF_F_COUNT * sizeof(double));
+    size_t o_res = take(NGSF_R_ALL * sizeof(int));
+    size_t o_fres = take(NGSF_F_ALL * sizeof(double));
     size_t o_hpart = take((size_t)d->nhchunk * sizeof(double));
     if (off > NGSF_STATIC_SCRATCH_BYTES) {
         std::string m = "ngsf_stamp_initial_static: the circuit needs " + std::to_string(off) +
@@ -3075,6 +3285,7 @@ OpArgs op_args(int op, const ngsf_point *pt, int types)
             a.deltaOld[k] = pt->deltaOld[k];
         a.ag0 = pt->ag[0];
         a.ag1 = pt->ag[1];
+        a.ag2 = pt->ag[2];
         a.gmin = pt->gmin;
         a.srcFact = pt->srcFact;
         a.diagGmin = pt->diagGmin;

@@ -279,7 +279,7 @@ typedef struct {
      * when it receives more than one product, the first product's L pos,
      * its U pos, the pivot k when the destination is U(k,k) and this is its
      * last update, else -1}, further products at ud_l/ud_u [ud_cptr[d] + 1
-     * ..]; per L entry to scale {pos, its column's pivot k} (16- and 8-byte
+     * ..]; per L entry to scale {pos, its pivot's lux pos} (16- and 8-byte
      * aligned groups of ints, read as int4 / int2) */
     const int *ud_pk;
     const int *sc_pk;
@@ -330,6 +330,13 @@ typedef struct {
      * launch continue the saved run instead of starting a fresh one */
     double pause_at;
     int run_resume;
+    /* synchronised runs (sharedspice GetSyncData): the time loop also
+     * stops (NGSF_HELD) at the two points where the reference calls
+     * sharedsync, so that the host can hand the step to the caller */
+    int sync;
+    /* L-entry growth past which a transient refactorization asks for new
+     * pivots (0: only zero or non-finite pivots do) */
+    double tran_growth;
 } ngsf_ckt_t;
 
 /* phases of the per-phase clock record */
@@ -347,6 +354,11 @@ enum {
 };
 /* floating results */
 enum { NGSF_F_TIME, NGSF_F_DELTA, NGSF_F_DIAGGMIN, NGSF_F_COUNT };
+/* internal results after the public ones: the sharedsync point a
+ * synchronised run stopped at (0: none, 1 + the reference's loc), its
+ * redostep, and the step's olddelta */
+enum { NGSF_R_SYNCLOC = NGSF_R_COUNT, NGSF_R_SYNCREDO, NGSF_R_ALL };
+enum { NGSF_F_OLDDELTA = NGSF_F_COUNT, NGSF_F_ALL };
 
 #ifdef __cplusplus
 }

@@ -45,6 +45,7 @@ extern "C" cudaError_t ngsf_launch_tran(const ngsf_ckt_t *d_ckts, const int *d_o
                                         int runMode, long long maxSteps, int solveCap,
                                         int gnnBytes, int threads, cudaStream_t stream);
 extern "C" int ngsf_ctl_bytes(void);
+extern "C" cudaError_t ngsf_sync_write(void *ctlsave, double delta, int reply);
 extern "C" int ngsf_tran_occupancy(int threads, int dynSmem, int *regs, int *smem);
 
 namespace ngsf {
@@ -77,7 +78,7 @@ struct DeviceCircuit::Impl {
     char *base = nullptr;
     size_t bytes = 0;
     char *lubase = nullptr;
-    size_t lubytes = 0;
+    size_t lubytes = 0, lucap = 0;
     char *predbase = nullptr;  /* Newton predictor arrays */
     size_t predbytes = 0;
     ngsf_ckt_t h{};            /* device pointers */
@@ -195,6 +196,8 @@ void DeviceCircuit::upload(const Image &img, const std::vector<int> &probes, int
     o.hch_cell = puti(hch_cell);
     o.hpart = zero((size_t)std::max<size_t>(1, hch_cell.size()) * sizeof(double));
     o.a_diag = puti(img.a_diag);
+    probes_ = probes;
+    o.probe = puti(probes_);   /* the last uploaded array: zero regions follow */
     o.opsave_rhs = zero((size_t)(n + 1) * sizeof(double));
     o.opsave_st = zero((size_t)(img.nstates + 1) * sizeof(double));
     o.work = zero((size_t)(n + 1) * sizeof(double));
@@ -203,15 +206,13 @@ void DeviceCircuit::upload(const Image &img, const std::vector<int> &probes, int
     o.rhsOld = zero((size_t)(n + 1) * sizeof(double));
     const int breakcap = 2 + 4 * (img.nvsrc + img.nisrc) + 64;
     o.breaks = zero((size_t)breakcap * sizeof(double));
-    probes_ = probes;
     o.out = zero((size_t)outcap * (1 + probes.size()) * sizeof(double));
-    o.probe = puti(probes_);
     o.cap_ax = zero((size_t)capmax * nnz * sizeof(double));
     o.cap_rhs = zero((size_t)2 * capmax * (n + 1) * sizeof(double));
     o.cap_meta = zero((size_t)4 * capmax * sizeof(double));
     o.ctlsave = zero((size_t)ngsf_ctl_bytes() + 64);
-    o.result = zero(NGSF_R_COUNT * sizeof(int));
-    o.fresult = zero(NGSF_F_COUNT * sizeof(double));
+    o.result = zero(NGSF_R_ALL * sizeof(int));
+    o.fresult = zero(NGSF_F_ALL * sizeof(double));
     o.wide = zero(sizeof(ngsf_wide_t));
     o.prof = zero(NGSF_P_COUNT * sizeof(long long));
 
@@ -220,9 +221,19 @@ void DeviceCircuit::upload(const Image &img, const std::vector<int> &probes, int
     impl->bytes = a.used;
     ck(cudaMalloc(&impl->base, a.used), "cudaMalloc(arena)");
     ck(cudaMemset(impl->base, 0, a.used), "cudaMemset(arena)");
-    for (auto &p : plans)
-        ck(cudaMemcpy(impl->base + p.off, p.src, p.bytes, cudaMemcpyHostToDevice),
-           "cudaMemcpy(upload)");
+    {
+        /* one host image of the arena up to its last uploaded array (zeros
+         * between arrays, as the memset left them) and one copy */
+        size_t hi = 0;
+        for (auto &p : plans)
+            hi = std::max(hi, p.off + p.bytes);
+        std::vector<char> stage(hi, 0);
+        for (auto &p : plans)
+            memcpy(stage.data() + p.off, p.src, p.bytes);
+        if (hi)
+            ck(cudaMemcpy(impl->base, stage.data(), hi, cudaMemcpyHostToDevice),
+               "cudaMemcpy(upload)");
+    }
 
     char *b = impl->base;
     auto I = [&](size_t off) { return (int *)(b + off); };
@@ -284,6 +295,11 @@ void DeviceCircuit::upload(const Image &img, const std::vector<int> &probes, int
     h.prof = (ph && atoi(ph) != 0) ? (long long *)(b + o.prof) : nullptr;
     h.pause_at = INFINITY;
     h.run_resume = 0;
+    /* transient re-pivot on L growth past 1e6 (NGSF_TRAN_GROWTH overrides;
+     * 0 turns it off) */
+    h.tran_growth = 1e6;
+    if (const char *g = getenv("NGSF_TRAN_GROWTH"))
+        h.tran_growth = atof(g);
     if (!impl->d_desc)
         ck(cudaMalloc(&impl->d_desc, sizeof(ngsf_ckt_t)), "cudaMalloc(desc)");
     ck(cudaMemcpy(impl->d_desc, &h, sizeof(h), cudaMemcpyHostToDevice), "cudaMemcpy(desc)");
@@ -301,6 +317,19 @@ void DeviceCircuit::set_run(double pause_at, bool resume)
     h.pause_at = pause_at;
     h.run_resume = resume ? 1 : 0;
     ck(cudaMemcpy(impl->d_desc, &h, sizeof(h), cudaMemcpyHostToDevice), "cudaMemcpy(desc)");
+}
+
+void DeviceCircuit::set_sync(bool on)
+{
+    impl->h.sync = on ? 1 : 0;
+    if (impl->d_desc)
+        ck(cudaMemcpy(impl->d_desc, &impl->h, sizeof(impl->h), cudaMemcpyHostToDevice),
+           "cudaMemcpy(desc)");
+}
+
+void DeviceCircuit::sync_reply(double delta, int redo)
+{
+    ck(ngsf_sync_write(impl->h.ctlsave, delta, redo), "sync reply");
 }
 
 void DeviceCircuit::set_factor_shape(int blocks, int small)
@@ -520,12 +549,23 @@ void DeviceCircuit::upload_lu(const Image &img)
         return off;
     };
     auto puti = [&](const std::vector<int> &v) { return put(v.data(), v.size() * sizeof(int)); };
+    /* the right-looking schedule (two barriers per level, every
+     * destination of a level in parallel) is faster than the left-looking
+     * one (a column's dependency chain per warp) at every size measured;
+     * NGSF_LU=ll selects the left-looking one.  Only the selected
+     * schedule's arrays are uploaded. */
+    bool rl = img.n > 0;
+    if (const char *e = getenv("NGSF_LU"))
+        rl = std::string(e) != "ll";
+    const std::vector<int> none;
+    const bool ll = !rl;
     size_t o_lux = put(nullptr, (size_t)img.nlu * sizeof(double));
-    size_t o_a_lupos = puti(img.a_lupos), o_lvl_ptr = puti(img.lvl_ptr),
-           o_lvl_col = puti(img.lvl_col), o_cdiag = puti(img.cdiag), o_cend = puti(img.cend),
-           o_cbeg = puti(img.cbeg), o_kptr = puti(img.kptr), o_kdep = puti(img.kdep),
-           o_kpos = puti(img.kpos), o_kseg = puti(img.kseg), o_upd_dst = puti(img.upd_dst),
-           o_upd_src = puti(img.upd_src), o_prow = puti(img.prow), o_pcol = puti(img.pcol),
+    size_t o_a_lupos = puti(img.a_lupos), o_lvl_ptr = puti(ll ? img.lvl_ptr : none),
+           o_lvl_col = puti(ll ? img.lvl_col : none), o_cdiag = puti(img.cdiag),
+           o_cend = puti(img.cend), o_cbeg = puti(img.cbeg), o_kptr = puti(ll ? img.kptr : none),
+           o_kdep = puti(ll ? img.kdep : none), o_kpos = puti(ll ? img.kpos : none),
+           o_kseg = puti(ll ? img.kseg : none), o_upd_dst = puti(ll ? img.upd_dst : none),
+           o_upd_src = puti(ll ? img.upd_src : none), o_prow = puti(img.prow), o_pcol = puti(img.pcol),
            o_fl_ptr = puti(img.fl_ptr), o_fl_row = puti(img.fl_row), o_bl_ptr = puti(img.bl_ptr),
            o_bl_row = puti(img.bl_row), o_lr_ptr = puti(img.lr_ptr), o_lr_col = puti(img.lr_col),
            o_lr_pos = puti(img.lr_pos), o_ur_ptr = puti(img.ur_ptr), o_ur_col = puti(img.ur_col),
@@ -544,20 +584,14 @@ void DeviceCircuit::upload_lu(const Image &img)
     size_t o_fdesc = puti(fdesc), o_bdesc = puti(bdesc);
     size_t o_lval = put(nullptr, std::max<size_t>(1, img.lr_col.size()) * sizeof(double));
     size_t o_uval = put(nullptr, std::max<size_t>(1, img.ur_col.size()) * sizeof(double));
-    /* the right-looking schedule (two barriers per level, every
-     * destination of a level in parallel) is faster than the left-looking
-     * one (a column's dependency chain per warp) at every size measured;
-     * NGSF_LU=ll selects the left-looking one */
-    bool rl = img.n > 0;
-    if (const char *e = getenv("NGSF_LU"))
-        rl = std::string(e) != "ll";
-    const std::vector<int> none;
+    /* the packed descriptors below replace ud_dst, ud_p, sc_pos, sc_piv on
+     * the device */
     size_t o_rl_ptr = puti(rl ? img.rl_ptr : none), o_rl_col = puti(rl ? img.rl_col : none),
-           o_sc_ptr = puti(rl ? img.sc_ptr : none), o_sc_pos = puti(rl ? img.sc_pos : none),
-           o_sc_piv = puti(rl ? img.sc_piv : none), o_ud_ptr = puti(rl ? img.ud_ptr : none),
-           o_ud_dst = puti(rl ? img.ud_dst : none), o_ud_cptr = puti(rl ? img.ud_cptr : none),
+           o_sc_ptr = puti(rl ? img.sc_ptr : none), o_sc_pos = puti(none),
+           o_sc_piv = puti(none), o_ud_ptr = puti(rl ? img.ud_ptr : none),
+           o_ud_dst = puti(none), o_ud_cptr = puti(rl ? img.ud_cptr : none),
            o_ud_l = puti(rl ? img.ud_l : none), o_ud_u = puti(rl ? img.ud_u : none),
-           o_ud_p = puti(rl ? img.ud_p : none);
+           o_ud_p = puti(none);
     /* packed form of the right-looking schedule */
     std::vector<int> ud_pk, sc_pk;
     if (rl) {
@@ -580,19 +614,27 @@ void DeviceCircuit::upload_lu(const Image &img)
         sc_pk.resize(2 * img.sc_pos.size());
         for (size_t e = 0; e < img.sc_pos.size(); e++) {
             sc_pk[2 * e] = img.sc_pos[e];
-            sc_pk[2 * e + 1] = diagcol[img.sc_piv[e]];
+            sc_pk[2 * e + 1] = img.sc_piv[e];
         }
     }
     size_t o_ud_pk = puti(ud_pk), o_sc_pk = puti(sc_pk);
     size_t o_uinv = put(nullptr, (size_t)std::max(1, img.n) * sizeof(double));
-    if (impl->lubase)
-        cudaFree(impl->lubase);
-    impl->lubase = nullptr;
-    impl->lubytes = a.used;
-    ck(cudaMalloc(&impl->lubase, a.used), "cudaMalloc(lu arena)");
+    /* one host image of the arena and one copy; the device arena is kept
+     * when the new plan fits it (a re-pivot usually changes the fill a
+     * little), so a re-plan costs no cudaFree (which synchronises) */
+    std::vector<char> stage(a.used, 0);
     for (auto &p : plans)
-        ck(cudaMemcpy(impl->lubase + p.off, p.src, p.bytes, cudaMemcpyHostToDevice),
-           "cudaMemcpy(lu upload)");
+        memcpy(stage.data() + p.off, p.src, p.bytes);
+    if (!impl->lubase || impl->lucap < a.used) {
+        if (impl->lubase)
+            cudaFree(impl->lubase);
+        impl->lubase = nullptr;
+        impl->lucap = a.used + a.used / 4;
+        ck(cudaMalloc(&impl->lubase, impl->lucap), "cudaMalloc(lu arena)");
+    }
+    impl->lubytes = a.used;
+    ck(cudaMemcpy(impl->lubase, stage.data(), a.used, cudaMemcpyHostToDevice),
+       "cudaMemcpy(lu upload)");
     char *b = impl->lubase;
     auto I = [&](size_t off) { return (int *)(b + off); };
     ngsf_ckt_t &h = impl->h;
@@ -663,11 +705,11 @@ std::vector<double> DeviceCircuit::read_ax()
 
 void DeviceCircuit::read_results(std::vector<int> &ires, std::vector<double> &fres)
 {
-    ires.resize(NGSF_R_COUNT);
-    fres.resize(NGSF_F_COUNT);
-    ck(cudaMemcpy(ires.data(), impl->h.result, NGSF_R_COUNT * sizeof(int),
+    ires.resize(NGSF_R_ALL);
+    fres.resize(NGSF_F_ALL);
+    ck(cudaMemcpy(ires.data(), impl->h.result, NGSF_R_ALL * sizeof(int),
                   cudaMemcpyDeviceToHost), "cudaMemcpy(result)");
-    ck(cudaMemcpy(fres.data(), impl->h.fresult, NGSF_F_COUNT * sizeof(double),
+    ck(cudaMemcpy(fres.data(), impl->h.fresult, NGSF_F_ALL * sizeof(double),
                   cudaMemcpyDeviceToHost), "cudaMemcpy(fresult)");
 }
 
@@ -888,11 +930,12 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
                                 ax[c->img.a_diag[j]] += dg;
                     replan.push_back(c);
                     axs.push_back(std::move(ax));
-                } else if (c->ires[NGSF_R_STATUS] == NGSF_HELD &&
+                } else if (c->ires[NGSF_R_STATUS] == NGSF_HELD && c->ires[NGSF_R_SYNCLOC] == 0 &&
                            !(c->fres[NGSF_F_TIME] >= pause_at)) {
                     next.push_back(c);   /* held after its first step */
                 } else {
-                    /* finished, failed, or stopped at the end of the window */
+                    /* finished, failed, or stopped at the end of the window
+                     * or at a sync point */
                     c->paused = c->ires[NGSF_R_STATUS] == NGSF_HELD;
                     c->dev->read_points(c->ires[NGSF_R_NPOINTS], c->points);
                 }
@@ -904,13 +947,21 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
             {
                 std::atomic<size_t> cursor{0};
                 /* 1 planned, 0 singular, -1 the planner itself failed */
+                /* each worker plans a circuit and uploads its plan (a
+                 * thread of its own: the calling thread's device made
+                 * current first) */
+                int dev = 0;
+                cudaGetDevice(&dev);
                 auto work = [&]() {
+                    cudaSetDevice(dev);
                     for (size_t i; (i = cursor.fetch_add(1)) < replan.size();) {
                         Prepared *c = replan[i];
                         std::string err;
                         try {
                             ok[i] = plan_lu(c->img.n, c->img.a_cp, c->img.a_ri, axs[i],
                                             c->img.opt.pivrel, c->img.opt.pivtol, c->img, err);
+                            if (ok[i] == 1)
+                                c->dev->upload_lu(c->img);
                         } catch (const std::exception &) {
                             ok[i] = -1;
                         }
@@ -937,14 +988,13 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
                         std::chrono::duration<double>(std::chrono::steady_clock::now() - tp).count());
             for (size_t i = 0; i < replan.size(); i++)
                 if (ok[i] < 0)
-                    throw std::runtime_error("pivot planning failed (out of host memory?)");
+                    throw std::runtime_error("pivot planning or plan upload failed");
             for (size_t i = 0; i < replan.size(); i++) {
                 Prepared *c = replan[i];
                 if (!ok[i]) {
                     c->ires[NGSF_R_STATUS] = NGSF_E_SINGULAR;
                     continue;
                 }
-                c->dev->upload_lu(c->img);
                 next.push_back(c);
             }
             pending.swap(next);

@@ -32,6 +32,10 @@ public:
     /* windowed runs: stop at the first accepted point at or after pause_at;
      * resume: continue the saved run instead of starting a fresh one */
     void set_run(double pause_at, bool resume);
+    /* synchronised runs: stop at the sharedsync points as well; the
+     * caller's answer to a stop goes into the saved control block */
+    void set_sync(bool on);
+    void sync_reply(double delta, int redo);
     const ngsf_ckt_t &desc() const;
     ngsf_ckt_t *device_desc() const;
     size_t bytes() const;

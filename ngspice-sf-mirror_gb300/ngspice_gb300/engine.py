@@ -55,7 +55,7 @@ class EngineError(RuntimeError):
 class Point(C.Structure):
     """ngsf_point: the CKTcircuit control scalars of one operation."""
     _fields_ = [("time", C.c_double), ("delta", C.c_double), ("deltaOld", C.c_double * 3),
-                ("ag", C.c_double * 2), ("gmin", C.c_double), ("srcFact", C.c_double),
+                ("ag", C.c_double * 3), ("gmin", C.c_double), ("srcFact", C.c_double),
                 ("diagGmin", C.c_double), ("mode", C.c_int), ("order", C.c_int)]
 
 
@@ -64,14 +64,15 @@ class DevInfo(C.Structure):
                 ("has_load", C.c_int), ("has_trunc", C.c_int), ("has_accept", C.c_int)]
 
 
-def make_point(time=0.0, delta=0.0, deltaOld=(0.0, 0.0, 0.0), ag=(0.0, 0.0), gmin=1e-12,
+def make_point(time=0.0, delta=0.0, deltaOld=(0.0, 0.0, 0.0), ag=(0.0, 0.0, 0.0), gmin=1e-12,
                srcFact=1.0, diagGmin=0.0, mode=0, order=1) -> Point:
     p = Point()
     p.time, p.delta, p.gmin, p.srcFact, p.diagGmin = time, delta, gmin, srcFact, diagGmin
     p.mode, p.order = int(mode), int(order)
     for k in range(3):
         p.deltaOld[k] = deltaOld[k] if k < len(deltaOld) else 0.0
-    p.ag[0], p.ag[1] = ag[0], ag[1]
+    for k in range(3):
+        p.ag[k] = ag[k] if k < len(ag) else 0.0
     return p
 
 
@@ -133,6 +134,9 @@ def lib(path: str | None = None) -> C.CDLL:
     L.ngsf_phase_cycles.argtypes = [vp, C.POINTER(C.c_longlong)]
     L.ngsf_eval_bench.argtypes = [vp, pp, C.c_int, C.c_int, C.c_int, dp]
     L.ngsf_fp64_peak.argtypes = [dp]
+    L.ngsf_set_sync.argtypes = [vp, C.c_int]
+    L.ngsf_sync_point.argtypes = [vp, ip, ip, dp, dp, dp]
+    L.ngsf_sync_reply.argtypes = [vp, C.c_double, C.c_int]
     fp = C.POINTER(C.c_float)
     if hasattr(L, "ngsf_node_graph"):
         L.ngsf_node_graph.argtypes = [vp, ip, ip, ip, ip, ip, fp]
@@ -283,6 +287,27 @@ class Circuit:
             self._pred_params = params
             p = params.ctypes.data_as(C.POINTER(C.c_float))
         if lib().ngsf_set_predictor(self._h, int(kind), p):
+            raise EngineError(last_error())
+
+    # ---- synchronised runs (sharedspice GetSyncData) ----
+    def set_sync(self, on: bool = True):
+        """Stop also at the two sharedsync points of every step."""
+        if lib().ngsf_set_sync(self._h, 1 if on else 0):
+            raise EngineError(last_error())
+
+    def sync_point(self) -> dict | None:
+        """The sharedsync stop the run is at, or None."""
+        loc, redo = C.c_int(), C.c_int()
+        t, d, od = C.c_double(), C.c_double(), C.c_double()
+        if not lib().ngsf_sync_point(self._h, C.byref(loc), C.byref(redo), C.byref(t),
+                                     C.byref(d), C.byref(od)):
+            return None
+        return {"loc": loc.value, "redostep": redo.value, "time": t.value, "delta": d.value,
+                "olddelta": od.value}
+
+    def sync_reply(self, delta: float, redo: int = 0):
+        """The caller's delta for the next step and its return value."""
+        if lib().ngsf_sync_reply(self._h, float(delta), int(redo)):
             raise EngineError(last_error())
 
     # ---- operator surface (CKTload / DEVload, CKTtrunc, NIconvTest, SMP*) ----

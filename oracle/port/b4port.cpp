@@ -58,19 +58,22 @@ extern "C" int port_b4_params(const char *mname, int polarity, int nm, const cha
 }
 
 /* One instance load; sv receives B4_NSTAMP stamp values. */
-extern "C" int port_b4_load_one(int mode, int order, double gmin, double delta,
-                                double deltaOld1, double ag0, double ag1, const double *rhsOld,
-                                double *st0, double *st1, const double *st2, const double *p,
-                                double *h, const int *node, int st, double *sv)
+extern "C" int port_b4_load_one(int mode, int order, int gear, double gmin, double delta,
+                                double deltaOld1, double ag0, double ag1, double ag2,
+                                const double *rhsOld, double *st0, double *st1,
+                                const double *st2, const double *p, double *h, const int *node,
+                                int st, double *sv)
 {
     B4Ctx x;
     x.mode = mode;
     x.order = order;
+    x.gear = gear;
     x.gmin = gmin;
     x.delta = delta;
     x.deltaOld1 = deltaOld1;
     x.ag0 = ag0;
     x.ag1 = ag1;
+    x.ag2 = ag2;
     x.rhsOld = rhsOld;
     x.st0 = st0;
     x.st1 = st1;
@@ -133,19 +136,22 @@ extern "C" int port_dio_params(const char *mname, int nm, const char **mkeys, co
     }
 }
 
-extern "C" int port_dio_load_one(int mode, int order, double gmin, double delta,
-                                 double deltaOld1, double ag0, double ag1, const double *rhsOld,
-                                 double *st0, double *st1, const double *st2, const double *p,
-                                 const int *node, int st, double *sv)
+extern "C" int port_dio_load_one(int mode, int order, int gear, double gmin, double delta,
+                                 double deltaOld1, double ag0, double ag1, double ag2,
+                                 const double *rhsOld, double *st0, double *st1,
+                                 const double *st2, const double *p, const int *node, int st,
+                                 double *sv)
 {
     DevCtx x;
     x.mode = mode;
     x.order = order;
+    x.gear = gear;
     x.gmin = gmin;
     x.delta = delta;
     x.deltaOld1 = deltaOld1;
     x.ag0 = ag0;
     x.ag1 = ag1;
+    x.ag2 = ag2;
     x.rhsOld = rhsOld;
     x.st0 = st0;
     x.st1 = st1;

@@ -10,8 +10,8 @@
  *                                              src/spicelib/analysis/cktop.c:27-654
  *   ni_iter           NIiter                   src/maths/ni/niiter.c:29-367
  *   conv_test         NIconvTest + CKTconvTest src/maths/ni/niconv.c:21-90
- *   comcof            NIcomCof (trapezoidal)   src/maths/ni/nicomcof.c:17-47
- *   integrate         NIintegrate (trap)       src/maths/ni/niinteg.c:18-80
+ *   comcof            NIcomCof (trap, Gear 1-2) src/maths/ni/nicomcof.c:17-130
+ *   integrate         NIintegrate (trap, Gear) src/maths/ni/niinteg.c:18-80
  *   terr / trunc      CKTterr / CKTtrunc       src/spicelib/analysis/cktterr.c:13-79,
  *                                              ckttrunc.c:20-57
  *   set_break/clr_break CKTsetBreak/CKTclrBreak src/spicelib/analysis/cktsetbk.c,
@@ -97,10 +97,10 @@ typedef struct {
 int port_b4_nparam(void);
 int port_b4_nstamp(void);
 void port_b4_pattern(int *rows, int *cols);
-int port_b4_load_one(int mode, int order, double gmin, double delta, double deltaOld1,
-                     double ag0, double ag1, const double *rhsOld, double *st0, double *st1,
-                     const double *st2, const double *p, double *h, const int *node, int st,
-                     double *sv);
+int port_b4_load_one(int mode, int order, int gear, double gmin, double delta,
+                     double deltaOld1, double ag0, double ag1, double ag2, const double *rhsOld,
+                     double *st0, double *st1, const double *st2, const double *p, double *h,
+                     const int *node, int st, double *sv);
 
 /* sparse mode for large circuits (sparse_port.cpp plans the pivots) */
 typedef struct {
@@ -121,9 +121,10 @@ typedef struct {
     double p[DIO_MAXPARAM];
 } dio_t;
 int port_dio_nparam(void);
-int port_dio_load_one(int mode, int order, double gmin, double delta, double deltaOld1,
-                      double ag0, double ag1, const double *rhsOld, double *st0, double *st1,
-                      const double *st2, const double *p, const int *node, int st, double *sv);
+int port_dio_load_one(int mode, int order, int gear, double gmin, double delta,
+                      double deltaOld1, double ag0, double ag1, double ag2, const double *rhsOld,
+                      double *st0, double *st1, const double *st2, const double *p,
+                      const int *node, int st, double *sv);
 
 typedef struct { int a, b; double g; } res_t;
 typedef struct { int a, b, st; double c, m, ic; } cap_t;
@@ -146,7 +147,7 @@ typedef struct {
     /* options */
     double reltol, abstol, vntol, chgtol, trtol, gmin0, pivtol, pivrel, xmu;
     double tstep, tstop, tstart, tmax, delmin, minbreak;
-    int itl1, itl4, maxord;
+    int itl1, itl4, maxord, method;   /* method: 0 trapezoidal, 1 Gear */
     /* run state */
     int sparse;              /* 1: CSC matrix + planned sparse LU */
     int recording, nrec, caprec, *rec;   /* pattern discovery (sparse) */
@@ -266,7 +267,7 @@ void port_set_options(port_t *c, const double *d, const int *i)
     c->trtol = d[4]; c->gmin0 = d[5]; c->pivtol = d[6]; c->pivrel = d[7];
     c->xmu = d[8]; c->tstep = d[9]; c->tstop = d[10]; c->tstart = d[11];
     c->tmax = d[12]; c->delmin = d[13]; c->minbreak = d[14];
-    c->itl1 = i[0]; c->itl4 = i[1]; c->maxord = i[2];
+    c->itl1 = i[0]; c->itl4 = i[1]; c->maxord = i[2]; c->method = i[3];
 }
 
 void port_add_res(port_t *c, int a, int b, double g)
@@ -496,9 +497,16 @@ static void qmeyer(double vgs, double vgd, double von, double vdsat, double *cap
 
 static void integrate(port_t *c, double *geq, double *ceq, double cap, int qcap)
 {
-    double *s0 = c->states[0], *s1 = c->states[1];
+    double *s0 = c->states[0], *s1 = c->states[1], *s2 = c->states[2];
     int ccap = qcap + 1;
-    if (c->order == 1)
+    if (c->method == 1) {
+        /* Gear: sum of ag[k] * q_k, highest k first (niinteg.c:42-67) */
+        s0[ccap] = 0;
+        if (c->order >= 2)
+            s0[ccap] += c->ag[2] * s2[qcap];
+        s0[ccap] += c->ag[1] * s1[qcap];
+        s0[ccap] += c->ag[0] * s0[qcap];
+    } else if (c->order == 1)
         s0[ccap] = c->ag[0] * s0[qcap] + c->ag[1] * s1[qcap];
     else
         s0[ccap] = -s1[ccap] * c->ag[1] + c->ag[0] * (s0[qcap] - s1[qcap]);
@@ -983,8 +991,9 @@ static int b4_load(port_t *c)
     double sv[B4_MAXSTAMP];
     for (int i = 0; i < c->nb4; i++) {
         b4_t *h = &c->b4[i];
-        nc |= port_b4_load_one(c->mode, c->order, c->gmin, c->delta, c->deltaOld[1], c->ag[0],
-                               c->ag[1], c->rhsOld, c->states[0], c->states[1], c->states[2],
+        nc |= port_b4_load_one(c->mode, c->order, c->method, c->gmin, c->delta, c->deltaOld[1],
+                               c->ag[0], c->ag[1], c->ag[2], c->rhsOld, c->states[0],
+                               c->states[1], c->states[2],
                                h->p, h->h, h->node, h->st, sv);
         for (int k = 0; k < ns; k++) {
             if (rows[k] < 0)
@@ -1048,8 +1057,9 @@ static int dio_load(port_t *c)
     double sv[9];
     for (int i = 0; i < c->ndio; i++) {
         dio_t *d = &c->dio[i];
-        nc |= port_dio_load_one(c->mode, c->order, c->gmin, c->delta, c->deltaOld[1], c->ag[0],
-                                c->ag[1], c->rhsOld, c->states[0], c->states[1], c->states[2],
+        nc |= port_dio_load_one(c->mode, c->order, c->method, c->gmin, c->delta, c->deltaOld[1],
+                                c->ag[0], c->ag[1], c->ag[2], c->rhsOld, c->states[0],
+                                c->states[1], c->states[2],
                                 d->p, d->node, d->st, sv);
         int P = d->node[0], N = d->node[1], PP = d->node[2];
         c->rhs[N] += sv[0];
@@ -1101,16 +1111,17 @@ static int ckt_load_devices(port_t *c)
 /* ------------------------------------------------------------------ */
 /* sparse refactorization on the planned pattern: left-looking, columns
  * in dependency-level order; fails (asking for new pivots) on a zero or
- * non-finite pivot or a non-finite L entry, and in the operating point
- * (MODEDCOP / MODETRANOP, where gmin and source stepping move the matrix
- * far from the one the pivots were chosen on) also on an L entry above
- * 1e6.  The transient refactors on its pivots like klu_refactor
- * (src/maths/KLU/klusmp.c:591-602: only a zero pivot fails). */
+ * non-finite pivot or a non-finite L entry, and on an L entry above 1e6
+ * (the engine's rule: klu_refactor, src/maths/KLU/klusmp.c:591-602, fails
+ * on a zero pivot only, but KLU's ordering rarely lets the pivots of a
+ * later matrix grow that far; the planner's Markowitz order sometimes
+ * does, in the operating point under gmin and source stepping and, rarely,
+ * in the transient). */
 static int sp_factor(port_t *c)
 {
     port_plan_t *P = &c->plan;
     int n = c->n;
-    const double growth = (c->mode & (MODEDCOP | MODETRANOP)) ? 1e6 : DBL_MAX;
+    const double growth = 1e6;
     double *lux = c->lux;
     memset(lux, 0, sizeof(double) * (size_t)P->nlu);
     for (int p = 0; p < c->nnz; p++)
@@ -1656,7 +1667,8 @@ static double terr(port_t *c, int qcap, double timeStep)
             deltmp[i] = deltmp[i + 1] + c->deltaOld[i];
     }
     static const double trapCoeff[] = {.5, .08333333333};
-    double factor = trapCoeff[c->order - 1];
+    static const double gearCoeff[] = {.5, .2222222222};
+    double factor = c->method == 1 ? gearCoeff[c->order - 1] : trapCoeff[c->order - 1];
     double del = c->trtol * tol / MAX(c->abstol, factor * fabs(diff[0]));
     if (c->order == 2)
         del = sqrt(del);
@@ -1683,8 +1695,52 @@ static double trunc_step(port_t *c, double timeStep)
     return MIN(2 * timeStep, t);
 }
 
+/* Gear coefficients, orders 1-2 (nicomcof.c:52-130): the corrector
+ * system's row j holds the j-th powers of the summed past steps over
+ * delta; right-hand side (0, -1/delta, 0); first column (1, 0, 0) */
+static void comcof_gear(port_t *c)
+{
+    const int q = c->order;
+    double m[3][3];
+    int i, j, k;
+    memset(c->ag, 0, sizeof c->ag);
+    c->ag[1] = -1 / c->delta;
+    double sum = 0;
+    for (i = 0; i <= q; i++)
+        m[0][i] = 1;
+    for (i = 1; i <= q; i++)
+        m[i][0] = 0;
+    for (i = 1; i <= q; i++) {
+        sum += c->deltaOld[i - 1];
+        double pw = 1;
+        for (j = 1; j <= q; j++) {
+            pw *= sum / c->delta;
+            m[j][i] = pw;
+        }
+    }
+    for (i = 1; i <= q; i++)
+        for (j = i + 1; j <= q; j++) {
+            m[j][i] /= m[i][i];
+            for (k = i + 1; k <= q; k++)
+                m[j][k] -= m[j][i] * m[i][k];
+        }
+    for (i = 1; i <= q; i++)
+        for (j = i + 1; j <= q; j++)
+            c->ag[j] = c->ag[j] - m[j][i] * c->ag[i];
+    c->ag[q] /= m[q][q];
+    for (i = q - 1; i >= 0; i--) {
+        for (j = i + 1; j <= q; j++)
+            c->ag[i] = c->ag[i] - m[i][j] * c->ag[j];
+        c->ag[i] /= m[i][i];
+    }
+}
+
 static void comcof(port_t *c)
 {
+    if (c->method == 1) {
+        comcof_gear(c);
+        return;
+    }
     if (c->order == 1) {
         c->ag[0] = 1 / c->delta;
         c->ag[1] = -1 / c->delta;

@@ -422,8 +422,16 @@ class Circuit:
                   opt("chgtol", 1e-14), opt("trtol", 7.0), opt("gmin", 1e-12),
                   opt("pivtol", 1e-13), opt("pivrel", 1e-3), 0.5, tstep, tstop, tstart,
                   tmax, delmin, 10.0 * delmin]
-            iv = [int(opt("itl1", 100)), int(opt("itl4", 10)), int(opt("maxord", 2))]
-            L.port_set_options(h, (C.c_double * len(dv))(*dv), (C.c_int * 3)(*iv))
+            # integration method (cktsopt.c OPT_METHOD): "method=gear" or
+            # the bare flags "gear" / "trap", the last one given winning
+            method = 0
+            for k, v in o.items():
+                if k == "method":
+                    method = 1 if v == "gear" else 0
+                elif k in ("gear", "trap"):
+                    method = 1 if k == "gear" else 0
+            iv = [int(opt("itl1", 100)), int(opt("itl4", 10)), int(opt("maxord", 2)), method]
+            L.port_set_options(h, (C.c_double * len(dv))(*dv), (C.c_int * 4)(*iv))
             for nodes, st, cval, p in self.dev[K_CAP]:
                 L.port_add_cap(h, nodes[0], nodes[1], st, cval, p.get("m", 1.0), p.get("ic", 0.0))
             for kk, isv in ((K_ISRC, 0), (K_VSRC, 1)):

@@ -58,6 +58,10 @@ CASES = {
 #                drop-in benchmark, first 30 ps of its transient
 #   mc_1k/2k/3k  Monte Carlo instances (device mismatch) of about 1,000,
 #                2,000 and 3,000 transistors, first 50 ps
+#   mc_c4_1314   instance 1314 of the 4096-instance Monte Carlo workload
+#                (4,714 transistors, seed 101314), first 150 ps: its L
+#                entries grow past 1e6 in the transient, so it is the
+#                batch's most rounding-sensitive refactorization
 NPROBE = 256
 
 # A tight-tolerance reference (reltol 1e-5, vntol 1e-8 V, abstol 1e-14 A)
@@ -66,6 +70,19 @@ NPROBE = 256
 # their own time points (runs whose accepted steps differ from the
 # reference's, e.g. with a Newton predictor).
 TIGHT_OPTIONS = ".options klu reltol=1e-5 vntol=1e-8 abstol=1e-14"
+
+
+# Gear integration (.options method=gear, maxord 2): the 120-transistor
+# BSIM4 deck over 400 ps and the diode/MOS1/RC decks, every unknown.
+GEAR_CASES = {
+    "gear_bsim4_logic_s3": lambda: netlists.random_logic(
+        n_transistors=120, seed=3, n_inputs=6, tstop="400p").replace(
+            ".options klu", ".options klu method=gear"),
+    "gear_mos1_mix": lambda: netlists.mos1_mix().replace(".options klu",
+                                                         ".options klu method=gear"),
+    "gear_diode_rectifier": lambda: netlists.diode_rectifier().replace(
+        ".options klu", ".options klu method=gear"),
+}
 
 
 def bsim4_logic_s3_tight() -> str:
@@ -81,6 +98,8 @@ LARGE_CASES = {
                                                mismatch=True),
     "mc_3k_50p": lambda: netlists.random_logic(n_transistors=3000, seed=103, tstop="50p",
                                                mismatch=True),
+    "mc_c4_1314": lambda: netlists.random_logic(n_transistors=4714, seed=101314, tstop="150p",
+                                                mismatch=True),
 }
 
 
@@ -225,6 +244,18 @@ def main(argv: list[str]) -> int:
             path = os.path.join(HERE, "bsim4_logic_s3_tight.npz")
             np.savez_compressed(path, **out)
             print(f"bsim4_logic_s3_tight: {len(res['times'])} points, stats={res['stats'].tolist()}"
+                  f" -> {os.path.getsize(path)} bytes")
+        for name, make in GEAR_CASES.items():
+            if only and name not in only:
+                continue
+            text = make()
+            assert "method=gear" in text
+            res = run_reference(text, 0, wd, keep_iters=False)
+            out = {k: res[k] for k in ("names", "times", "values", "stats", "cpu_seconds")}
+            out["netlist"] = np.array(text)
+            path = os.path.join(HERE, f"{name}.npz")
+            np.savez_compressed(path, **out)
+            print(f"{name}: {len(res['times'])} points, stats={res['stats'].tolist()}"
                   f" -> {os.path.getsize(path)} bytes")
         for name, make in LARGE_CASES.items():
             if only and name not in only:

@@ -91,6 +91,41 @@ def test_diode_decks_match_reference(E, name):
     assert waveform_violation(c.names(), g["times"], g["values"], t, v) < 1.0
 
 
+GEAR_CASES = ["gear_mos1_mix", "gear_diode_rectifier", "gear_bsim4_logic_s3"]
+
+
+@pytest.mark.parametrize("name", GEAR_CASES)
+def test_gear_decks_match_reference(E, name):
+    """Gear integration (.options method=gear, maxord 2): the reference's
+    Newton and step counts, time points equal to rounding, waveforms
+    within reltol=1e-3, vntol=1 uV, abstol=1 pA."""
+    g = golden(name)
+    c = run_one(E, str(g["netlist"]))
+    r = c.results()
+    ref = g["stats"]
+    assert r[E.R_STATUS] == 0
+    assert (r[E.R_NUMITER], r[E.R_TRANITER], r[E.R_ACCEPTED], r[E.R_REJECTED]) == \
+        (ref[0], ref[1], ref[3], ref[4])
+    t, v = c.points()
+    assert len(t) == len(g["times"])
+    assert np.max(np.abs(t - g["times"])) <= 1e-9 * g["times"][-1]
+    assert waveform_violation(c.names(), g["times"], g["values"], t, v) < 1.0
+
+
+def test_gear_batch_equals_single_runs(E):
+    """Gear decks in one batched launch give the bits of their single runs."""
+    texts = [str(golden(n)["netlist"]) for n in GEAR_CASES]
+    singles = [run_one(E, t) for t in texts]
+    cs = [E.Circuit(t) for t in texts]
+    E.run(cs, max_steps=1_000_000)
+    for a, b in zip(singles, cs):
+        assert list(a.results()[:7]) == list(b.results()[:7])
+        ta, va = a.points()
+        tb, vb = b.points()
+        np.testing.assert_array_equal(ta, tb)
+        np.testing.assert_array_equal(va, vb)
+
+
 @pytest.mark.parametrize("name", BSIM4_CASES)
 def test_bsim4_tran_matches_reference(E, name):
     """BSIM4 decks: the same Newton and step counts as the reference; time

@@ -4,7 +4,10 @@ Same fixtures as tests/test_oracle_port_scale.py (the reference ngspice
 compiled from its own sources): the 10,000-transistor random-logic netlist
 over its first 30 ps -- alone in its call it runs over the whole grid --
 and Monte Carlo instances of about 1,000, 2,000 and 3,000 transistors over
-50 ps, each alone and all three together in one batched launch.  The
+50 ps, each alone and all three together in one batched launch; and
+instance 1314 of the 4096-instance workload (4,714 transistors, 150 ps),
+whose L entries grow past 1e6 in the transient, over the whole grid and in
+one block.  The
 engine must reproduce the reference's Newton and step counts, and every
 recorded waveform must stay within reltol=1e-3, vntol=1 uV, abstol=1 pA at
 every reference time point (the worst error is printed)."""
@@ -39,7 +42,7 @@ def check(E, g, c, name):
     assert w < 1.0
 
 
-@pytest.mark.parametrize("name", MC + ["c1_10k_30p"])
+@pytest.mark.parametrize("name", MC + ["c1_10k_30p", "mc_c4_1314"])
 def test_engine_matches_reference_at_scale(E, name):
     g = golden(name)
     c = E.Circuit(str(g["netlist"]), probes=[str(x) for x in g["names"]], outcap=4096)
@@ -58,3 +61,15 @@ def test_batched_instances_match_reference(E, monkeypatch):
     E.run(cs)
     for n, g, c in zip(MC, gs, cs):
         check(E, g, c, n)
+
+
+def test_rounding_sensitive_instance_in_one_block(E, monkeypatch):
+    """Instance 1314 of the 4096-instance workload on the batched path (one
+    thread block; alone in its call it runs over the whole grid), against
+    the reference: the refactorization's rounding must let its transient
+    finish with the reference's counts."""
+    monkeypatch.setenv("NGSF_WIDE", "0")
+    g = golden("mc_c4_1314")
+    c = E.Circuit(str(g["netlist"]), probes=[str(x) for x in g["names"]], outcap=4096)
+    E.run([c])
+    check(E, g, c, "mc_c4_1314 (one block)")

@@ -141,3 +141,97 @@ def test_points_stream_and_halt_resume(ng):
     progress = [s for s in stats if s.startswith("tran ") and s != "tran 0.0%"]
     assert len(progress) >= 8
     assert len(set(points)) >= 8
+
+
+GetSyncData = C.CFUNCTYPE(C.c_int, C.c_double, C.POINTER(C.c_double), C.c_double, C.c_int,
+                          C.c_int, C.c_int, C.c_void_p)
+
+
+def _run_with_sync(ng, callback):
+    """One `run` of the rc_ladder deck with `callback` as GetSyncData;
+    returns the accepted times and the callback's records."""
+    calls = []
+
+    def cb(t, pdelta, olddelta, redo, ident, loc, user):
+        calls.append((loc, redo, t, pdelta[0], olddelta))
+        return callback(loc, redo, t, pdelta, olddelta, len(calls))
+
+    f = GetSyncData(cb)
+    _KEEP.append(f)
+    ng.ngSpice_Init_Sync.argtypes = [C.c_void_p, C.c_void_p, GetSyncData, C.c_void_p, C.c_void_p]
+    assert ng.ngSpice_Init_Sync(None, None, f, None, None) == 0
+    try:
+        g = golden("rc_ladder")
+        lines = [ln.encode() for ln in str(g["netlist"]).splitlines()]
+        arr = (C.c_char_p * (len(lines) + 1))(*lines, None)
+        assert ng.ngSpice_Circ(arr) == 0
+        assert ng.ngSpice_Command(b"run") == 0
+        t = ng.ngGet_Vec_Info(b"time").contents
+        tt = np.ctypeslib.as_array(t.v_realdata, shape=(t.v_length,)).copy()
+    finally:
+        assert ng.ngSpice_Init_Sync(None, None, GetSyncData(), None, None) == 0
+    return g, tt, calls
+
+
+def test_sync_callback_sees_every_step(ng):
+    """GetSyncData is called where the reference's sharedsync is: before
+    every step (loc 0, olddelta 0) and after every step's verdict (loc 1);
+    a callback that changes nothing leaves the run as it is."""
+    g, tt, calls = _run_with_sync(ng, lambda *a: 0)
+    np.testing.assert_array_equal(tt, g["times"])
+    loc0 = [c for c in calls if c[0] == 0]
+    loc1 = [c for c in calls if c[0] == 1]
+    assert len(loc0) == len(g["times"]) - 1
+    assert all(c[4] == 0.0 and c[1] == 0 for c in loc0)
+    accepted = [c[2] for c in loc1 if c[1] == 0]
+    np.testing.assert_array_equal(np.array(accepted), g["times"][1:])
+    assert len(loc1) == len(g["times"]) - 1 + int(g["stats"][4])
+    # each loc-1 call follows the loc-0 call of its step; the step tried is
+    # the delta handed out before it
+    for a, b in zip(calls, calls[1:]):
+        if b[0] == 1 and a[0] == 0:
+            assert b[4] == a[3]
+
+
+def test_sync_callback_limits_the_step(ng):
+    """A callback that caps delta at 20 ps before every step: no accepted
+    step is longer, and the run still reaches its final time."""
+    cap = 20e-12
+
+    def limit(loc, redo, t, pdelta, olddelta, k):
+        if loc == 0:
+            pdelta[0] = min(pdelta[0], cap)
+        return 0
+
+    g, tt, calls = _run_with_sync(ng, limit)
+    assert abs(tt[-1] - g["times"][-1]) <= 1e-9 * g["times"][-1]
+    assert np.max(np.diff(tt)) <= cap * (1 + 1e-9)
+    assert len(tt) > len(g["times"])
+
+
+def test_sync_callback_redoes_a_step(ng):
+    """A callback that returns 1 once after an accepted step, handing back
+    that step's own delta: the step is discarded (time moves back by
+    olddelta) and tried again, so the same time point is accepted again;
+    the points before it are those of the undisturbed run and the run
+    reaches its final time."""
+    state = {"redone": None}
+
+    def redo_once(loc, redo, t, pdelta, olddelta, k):
+        if loc == 1 and redo == 0 and state["redone"] is None and t > 1e-9:
+            state["redone"] = t
+            pdelta[0] = olddelta
+            return 1
+        return 0
+
+    g, tt, calls = _run_with_sync(ng, redo_once)
+    t0 = state["redone"]
+    assert t0 is not None
+    assert np.sum(np.isclose(tt, t0, rtol=1e-12, atol=0)) == 1
+    assert np.all(np.diff(tt) > 0)
+    before = g["times"][g["times"] < t0]
+    np.testing.assert_array_equal(tt[:len(before)], before)
+    assert abs(tt[-1] - g["times"][-1]) <= 1e-9 * g["times"][-1]
+    # the loc-1 record of the repeated step reports the same time again
+    again = [c for c in calls if c[0] == 1 and np.isclose(c[2], t0, rtol=1e-12, atol=0)]
+    assert len(again) >= 2

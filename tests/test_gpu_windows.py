@@ -79,3 +79,33 @@ def test_batch_block_sizes_give_the_same_bits(E, monkeypatch):
     for other in runs[1:]:
         for a, b in zip(runs[0], other):
             same(E, a, b)
+
+
+@pytest.mark.parametrize("wide", ["0", "1"])
+def test_passive_sync_stops_equal_one_run(E, monkeypatch, wide):
+    """A synchronised run (stops at both sharedsync points of every step)
+    answered with the engine's own delta and no redo is bit-identical to the
+    plain run, in one block and over the whole grid; every stop reports a
+    step time inside the transient and a positive delta."""
+    from ngspice_gb300 import netlists
+    monkeypatch.setenv("NGSF_WIDE", wide)
+    text = netlists.random_logic(n_transistors=1100 if wide == "1" else 200, seed=321,
+                                 tstop="12p", mismatch=True)
+    plain = E.Circuit(text)
+    E.run([plain], max_steps=1_000_000)
+    c = E.Circuit(text)
+    c.set_sync(True)
+    stops = {0: 0, 1: 0}
+    for _ in range(20000):
+        E.run_window([c], 1.0, max_steps=1_000_000)
+        sp = c.sync_point()
+        if sp is None:
+            break
+        assert 0.0 <= sp["time"] <= 12e-12 and sp["delta"] > 0
+        stops[sp["loc"]] += 1
+        c.sync_reply(sp["delta"], 0)
+    assert c.results()[E.R_STATUS] == 0
+    same(E, plain, c)
+    acc = int(plain.results()[E.R_ACCEPTED])
+    assert stops[0] == acc - 1
+    assert stops[1] >= acc - 1

@@ -50,6 +50,28 @@ def test_port_diode_decks_match_reference(name):
                               r["values"][:, idx]) < 0.1
 
 
+GEAR_CASES = ["gear_mos1_mix", "gear_diode_rectifier", "gear_bsim4_logic_s3"]
+
+
+@pytest.mark.parametrize("name", GEAR_CASES)
+def test_port_gear_decks_match_reference(name):
+    """Gear integration (.options method=gear, maxord 2) on the MOS1,
+    diode and 120-transistor BSIM4 decks: the reference's Newton and step
+    counts, time points equal to rounding, waveforms within the option
+    tolerances."""
+    g = golden(name)
+    r = port.simulate(str(g["netlist"]))
+    st, ref = r["stats"], g["stats"]
+    assert st["status"] == 0
+    assert (st["numIter"], st["tranIter"], st["accepted"], st["rejected"]) == \
+        (ref[0], ref[1], ref[3], ref[4])
+    assert np.max(np.abs(r["times"] - g["times"])) <= 1e-9 * g["times"][-1]
+    names = list(g["names"])
+    idx = [r["names"].index(x) for x in names]
+    assert waveform_violation(names, g["times"], g["values"], r["times"],
+                              r["values"][:, idx]) < 0.1
+
+
 def test_port_bsim4_logic_matches_reference():
     """Random BSIM4 logic (seed 3, ~120 transistors): identical Newton and
     step counts; the accepted time points agree to rounding (the dense LU

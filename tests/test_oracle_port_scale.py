@@ -2,8 +2,10 @@
 
 The fixtures (tests/golden/make_golden.py, LARGE_CASES) come from the
 reference ngspice compiled from its own sources: the 10,000-transistor
-random-logic netlist over its first 30 ps and Monte Carlo instances of
-about 1,000, 2,000 and 3,000 transistors (device mismatch) over 50 ps.
+random-logic netlist over its first 30 ps, Monte Carlo instances of
+about 1,000, 2,000 and 3,000 transistors (device mismatch) over 50 ps, and
+instance 1314 of the 4096-instance workload (4,714 transistors) over
+150 ps.
 They hold the reference's statistics, accepted time points and the
 waveforms of 256 unknowns spread over the equation numbering.  The port
 must reproduce the Newton and step counts and stay within the option
@@ -17,7 +19,7 @@ import port
 from conftest import golden
 from tolerances import waveform_violation
 
-CASES = ["mc_1k_50p", "mc_2k_50p", "mc_3k_50p", "c1_10k_30p"]
+CASES = ["mc_1k_50p", "mc_2k_50p", "mc_3k_50p", "c1_10k_30p", "mc_c4_1314"]
 
 
 @pytest.mark.parametrize("name", CASES)
