@@ -490,20 +490,14 @@ def engine_arm(args, texts, wdesc, rank, world) -> dict | None:
         # the batched form with a Newton predictor on every instance, over
         # the same windows: 3 = the quadratic polynomial guess, 2 = that
         # plus the learned network's correction (trained here on the GPU on
-        # plain trajectories of seeded random-logic circuits, untimed)
+        # plain trajectories of seeded random-logic circuits with device
+        # mismatch, 100-1040 transistors over 300 ps, seeds disjoint from
+        # the workload's; untimed)
         forms = out_extra.setdefault("forms", {})
         for kind in [int(k) for k in args.predictors.split(",") if k.strip()]:
             params, train_info = None, None
             if kind == 2:
-                from ngspice_gb300 import netlists, predictor
-                tt = time.perf_counter()
-                train = [netlists.random_logic(n_transistors=150 + 15 * s, seed=500 + s,
-                                               tstop="150p") for s in range(args.learn_circuits)]
-                data = predictor.collect(train)
-                params, losses = predictor.train(data, steps=args.learn_steps, lr=args.learn_lr)
-                train_info = {"circuits": args.learn_circuits, "steps": args.learn_steps,
-                              "seconds": time.perf_counter() - tt,
-                              "loss_first": float(losses[0]), "loss_last": float(losses[-1])}
+                params, train_info = train_network(args)
                 progress(f"network trained in {train_info['seconds']:.1f} s")
             cs = open_all(texts)
             for c in cs:
@@ -549,11 +543,18 @@ def engine_arm(args, texts, wdesc, rank, world) -> dict | None:
     achieved = moved / total / 1e9
     kernel = "tran_wide_kernel" if (len(texts) <= 4 and wls[0]["bsim4"] + wls[0]["mos1"] >= 1024) \
         else "tran_kernel"
-    # DRAM bytes per Newton iteration measured with ncu (dram__bytes_read +
-    # dram__bytes_write) on the C1 time-loop launch, first 3 ps: 57.2 MB
-    # over ~120 iterations; the working set stays in L2, so traffic is far
-    # below the algorithmic bytes.  Scaled by this run's iterations.
-    traffic = 57.2e6 / 120 if args.workload == "c1" else None
+    # DRAM bytes per circuit Newton iteration measured with ncu
+    # (dram__bytes_read + dram__bytes_write of one launch over the Newton
+    # iterations it ran): the C1 time-loop launch of the first 3 ps, 538 MB
+    # over about 120 iterations (the working set stays in L2); a timed
+    # window of the first 76 C2 instances, 76.65 GB over 8,637 circuit
+    # iterations, 2.21x their 4,014,764 algorithmic bytes per iteration
+    # (76 circuit arenas do not fit L2 together).  A Monte Carlo batch
+    # scales that ratio by its own algorithmic bytes per iteration.
+    per_iter = moved / max(iters, 1)
+    traffic = {"c1": 538.4e6 / 120,
+               "c2": per_iter * (76.652e9 / 8637) / 4014764,
+               "c4": per_iter * (76.652e9 / 8637) / 4014764}.get(args.workload)
     roof = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
             "frac": achieved / pk["hbm_gbs"],
             "traffic": traffic, "traffic_unit": "bytes per Newton iteration" if traffic else None,
@@ -657,6 +658,47 @@ def gnn_case(nodes: int, steps: int = 3) -> dict:
     return out
 
 
+def train_network(args) -> tuple:
+    """The bench's predictor network: trained on the GPU on plain
+    trajectories of seeded random-logic circuits with device mismatch
+    (100-1040 transistors over 300 ps, seeds disjoint from the
+    workloads')."""
+    from ngspice_gb300 import netlists, predictor
+    tt = time.perf_counter()
+    train = [netlists.random_logic(n_transistors=100 + 20 * s, seed=900000 + s, tstop="300p",
+                                   mismatch=True) for s in range(args.learn_circuits)]
+    data = predictor.collect(train)
+    params, losses = predictor.train(data, steps=args.learn_steps, lr=args.learn_lr)
+    info = {"circuits": args.learn_circuits, "steps": args.learn_steps, "lr": args.learn_lr,
+            "seconds": time.perf_counter() - tt,
+            "loss_first": float(losses[0]), "loss_last": float(losses[-1])}
+    return params, info
+
+
+def predictor_study(args) -> dict:
+    """Newton iterations per accepted step of 8 held-out instances of the
+    C2 distribution (200-2000 transistors, device mismatch, seeds 700000+,
+    300 ps) from the reference's start (0), the linear (1) and quadratic (3)
+    guesses and the quadratic guess with the trained network (2)."""
+    import numpy as np
+    from ngspice_gb300 import netlists, predictor
+    rng = np.random.default_rng(7)
+    test = [netlists.random_logic(n_transistors=int(n), seed=700000 + i, tstop="300p",
+                                  mismatch=True)
+            for i, n in enumerate(rng.integers(200, 2000, 8))]
+    params, info = train_network(args)
+    res = predictor.evaluate(test, params, kinds=(0, 1, 3, 2))
+    out = {"study": "Newton predictor", "held_out": "8 C2-distribution instances, 300 ps",
+           "training": info}
+    for k, name in ((0, "plain"), (1, "linear"), (3, "quadratic"), (2, "network")):
+        r = res[k]
+        out[name] = {"iterations_per_step": r["iterations_per_step"],
+                     "accepted_steps": r["accepted"], "status": r["status"],
+                     "accepted_on_first_iteration": r["first_iteration"],
+                     "steps_from_a_guess": r["guesses"], "plain_retries": r["fallbacks"]}
+    return out
+
+
 def phase_split(args, texts) -> None:
     """Per-phase clock split of one untimed run of the workload (circuits
     opened with NGSF_PHASES=1, so the timed runs carry no clock reads)."""
@@ -702,9 +744,9 @@ def main():
     ap.add_argument("--predictors", default="3,2",
                     help="Monte Carlo workloads: Newton predictors also timed on the batch"
                          " (3 quadratic guess, 2 with the learned network; empty: none)")
-    ap.add_argument("--learn-circuits", type=int, default=24)
-    ap.add_argument("--learn-steps", type=int, default=3000)
-    ap.add_argument("--learn-lr", type=float, default=1e-3)
+    ap.add_argument("--learn-circuits", type=int, default=48)
+    ap.add_argument("--learn-steps", type=int, default=4000)
+    ap.add_argument("--learn-lr", type=float, default=3e-3)
     ap.add_argument("--plain-sample", type=int, default=4,
                     help="instances of a Monte Carlo workload timed through the plain drop-in")
     ap.add_argument("--instances", type=int, default=0,
@@ -728,6 +770,9 @@ def main():
                     help="profiling case: this many training steps of the predictor network"
                          " on a seeded graph of --gnn-nodes nodes, then stop")
     ap.add_argument("--gnn-nodes", type=int, default=8192)
+    ap.add_argument("--predictor-study", action="store_true",
+                    help="train the bench's network and compare the Newton starts on held-out"
+                         " instances (one JSON line)")
     ap.add_argument("--device-eval-only", action="store_true",
                     help="print the device_eval JSON line and stop (profiling case)")
     ap.add_argument("--tstop", default=None,
@@ -736,6 +781,9 @@ def main():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     args.instances = args.instances or DEFAULT_INSTANCES[args.workload]
+    if args.predictor_study:
+        print(json.dumps(predictor_study(args)))
+        return
     if args.gnn_steps:
         print(json.dumps(gnn_case(args.gnn_nodes, args.gnn_steps)))
         return

@@ -1104,12 +1104,9 @@ __device__ int ckt_load(const ngsf_ckt_t &C, Ctl &s, const Iter &it)
  * src/maths/KLU/klusmp.c:591-602).  An L entry above a growth limit also
  * asks for new pivots: in the operating point always NGSF_GROWTH (gmin and
  * source stepping move the matrix far from the one the pivots were chosen
- * on), in the transient C.tran_growth (0: none).  The pivots are chosen
- * with the threshold 1e-3 that bounds |L| by 1e3 on the matrix they were
- * chosen on; KLU's ordering keeps later matrices near that bound, the
- * Markowitz plan occasionally does not (L entries past 1e6 in 4 of the
- * 4096 Monte Carlo instances, whose Newton then fails where the
- * reference's converges), and a re-pivot there restores it. */
+ * on), in the transient C.tran_growth when set (off by default: a re-pivot
+ * pauses its circuit until the batch's launch ends, and the retry rule of
+ * dc_tran catches the pivots that matter). */
 #define NGSF_GROWTH 1e6
 __device__ __forceinline__ double growth_limit(const ngsf_ckt_t &C, const Ctl &s)
 {
@@ -1143,11 +1140,12 @@ __device__ __forceinline__ int rl_level_work(const ngsf_ckt_t &C, int l)
 }
 
 /* level l, first half (threads t of T): pivot checks, L(:,k) /= U(k,k) */
-__device__ __forceinline__ int rl_scale(const ngsf_ckt_t &C, int l, int t, int T, double growth)
+__device__ __forceinline__ int rl_scale(const ngsf_ckt_t &C, double *lux, int l, int t, int T,
+                                        double growth)
 {
     int bad = 0;
     for (int c = C.rl_ptr[l] + t; c < C.rl_ptr[l + 1]; c += T) {
-        double piv = C.lux[C.cdiag[C.rl_col[c]]];
+        double piv = lux[C.cdiag[C.rl_col[c]]];
         if (!(fabs(piv) > 0.0) || !isfinite(piv))
             bad = 1;
     }
@@ -1163,14 +1161,14 @@ __device__ __forceinline__ int rl_scale(const ngsf_ckt_t &C, int l, int t, int T
 #pragma unroll
         for (int j = 0; j < NGSF_RL_ILP; j++)
             if (q[j].x >= 0) {
-                x[j] = C.lux[q[j].x];
-                v[j] = C.lux[q[j].y];
+                x[j] = lux[q[j].x];
+                v[j] = lux[q[j].y];
             }
 #pragma unroll
         for (int j = 0; j < NGSF_RL_ILP; j++)
             if (q[j].x >= 0) {
                 const double l_ik = x[j] / v[j];
-                C.lux[q[j].x] = l_ik;
+                lux[q[j].x] = l_ik;
                 if (!(fabs(l_ik) <= growth))
                     bad = 1;
             }
@@ -1180,7 +1178,7 @@ __device__ __forceinline__ int rl_scale(const ngsf_ckt_t &C, int l, int t, int T
 
 /* level l, second half: the updates (and the inverse of every pivot whose
  * last update this is) */
-__device__ __forceinline__ void rl_update(const ngsf_ckt_t &C, int l, int t, int T)
+__device__ __forceinline__ void rl_update(const ngsf_ckt_t &C, double *lux, int l, int t, int T)
 {
     const int d0 = C.ud_ptr[l], d1 = C.ud_ptr[l + 1];
     for (int d = d0 + t; d < d1; d += NGSF_RL_ILP * T) {
@@ -1196,9 +1194,9 @@ __device__ __forceinline__ void rl_update(const ngsf_ckt_t &C, int l, int t, int
         for (int j = 0; j < NGSF_RL_ILP; j++) {
             dst[j] = q[j].x >= 0 ? q[j].x : -q[j].x - 1;
             if (d + j * T < d1) {
-                a[j] = C.lux[dst[j]];
-                x[j] = C.lux[q[j].y];
-                y[j] = C.lux[q[j].z];
+                a[j] = lux[dst[j]];
+                x[j] = lux[q[j].y];
+                y[j] = lux[q[j].z];
             }
         }
 #pragma unroll
@@ -1208,9 +1206,9 @@ __device__ __forceinline__ void rl_update(const ngsf_ckt_t &C, int l, int t, int
                 if (q[j].x < 0) {
                     const int dj = d + j * T;
                     for (int c = C.ud_cptr[dj] + 1; c < C.ud_cptr[dj + 1]; c++)
-                        acc = __dsub_rn(acc, __dmul_rn(C.lux[C.ud_l[c]], C.lux[C.ud_u[c]]));
+                        acc = __dsub_rn(acc, __dmul_rn(lux[C.ud_l[c]], lux[C.ud_u[c]]));
                 }
-                C.lux[dst[j]] = acc;
+                lux[dst[j]] = acc;
                 if (q[j].w >= 0)
                     C.uinv[q[j].w] = 1.0 / acc;
             }
@@ -1218,23 +1216,30 @@ __device__ __forceinline__ void rl_update(const ngsf_ckt_t &C, int l, int t, int
 }
 
 /* One block: a whole level, two barriers. */
-__device__ __forceinline__ int rl_level_block(const ngsf_ckt_t &C, int l, double growth)
+__device__ __forceinline__ int rl_level_block(const ngsf_ckt_t &C, double *lux, int l,
+                                              double growth)
 {
-    const int bad = rl_scale(C, l, threadIdx.x, blockDim.x, growth);
+    const int bad = rl_scale(C, lux, l, threadIdx.x, blockDim.x, growth);
     __syncthreads();
-    rl_update(C, l, threadIdx.x, blockDim.x);
+    rl_update(C, lux, l, threadIdx.x, blockDim.x);
     __syncthreads();
     return bad;
 }
 
 /* The solve's copy of the factor values in term order (threads t of T). */
-__device__ void solve_pack(const ngsf_ckt_t &C, int t, int T)
+__device__ void solve_pack(const ngsf_ckt_t &C, const double *lux, int t, int T)
 {
     for (int q = t; q < C.nlterm; q += T)
-        C.lval[q] = C.lux[C.lr_pos[q]];
+        C.lval[q] = lux[C.lr_pos[q]];
     for (int q = t; q < C.nuterm; q += T)
-        C.uval[q] = C.lux[C.ur_pos[q]];
+        C.uval[q] = lux[C.ur_pos[q]];
 }
+
+/* The factor values of a batched circuit block: dynamic shared memory
+ * when the launch reserved room for them (the block path of a batch; the
+ * right-looking schedule then reads and writes shared memory instead of
+ * L2), else C.lux. */
+__shared__ double *g_lux;
 
 /* blocks of a wide launch that take part in the refactorization: enough
  * threads for the widest levels, few enough for a cheap barrier */
@@ -1245,25 +1250,26 @@ __device__ int lu_factor_rl(const ngsf_ckt_t &C, Ctl &s, int b, int nbAll)
     int bad = 0;
     const double growth = growth_limit(C, s);
     if (nbAll <= 1) {
+        double *lux = g_lux ? g_lux : C.lux;
         for (int q = threadIdx.x; q < C.nlu; q += blockDim.x)
-            C.lux[q] = 0.0;
+            lux[q] = 0.0;
         __syncthreads();
         for (int p = threadIdx.x; p < C.nnz; p += blockDim.x)
-            C.lux[C.a_lupos[p]] = C.ax[p];
+            lux[C.a_lupos[p]] = C.ax[p];
         __syncthreads();
         if (s.diagGmin != 0.0) {
             /* LoadGmin: gmin on every structural diagonal (klusmp.c:587-589) */
             for (int j = threadIdx.x; j < C.n; j += blockDim.x)
                 if (C.a_diag[j] >= 0)
-                    C.lux[C.a_lupos[C.a_diag[j]]] += s.diagGmin;
+                    lux[C.a_lupos[C.a_diag[j]]] += s.diagGmin;
             __syncthreads();
         }
         for (int k = threadIdx.x; k < C.n; k += blockDim.x)
-            C.uinv[k] = 1.0 / C.lux[C.cdiag[k]];
+            C.uinv[k] = 1.0 / lux[C.cdiag[k]];
         __syncthreads();
         for (int l = 0; l < C.rl_levels; l++)
-            bad |= rl_level_block(C, l, growth);
-        solve_pack(C, threadIdx.x, blockDim.x);
+            bad |= rl_level_block(C, lux, l, growth);
+        solve_pack(C, lux, threadIdx.x, blockDim.x);
         return block_or(s, bad);
     }
     /* wide launch: a level with little work runs in block 0 alone (two
@@ -1294,21 +1300,21 @@ __device__ int lu_factor_rl(const ngsf_ckt_t &C, Ctl &s, int b, int nbAll)
         for (int l = 0; l < C.rl_levels; l++) {
             if (rl_level_work(C, l) <= smallWork) {
                 if (b == 0)
-                    bad |= rl_level_block(C, l, growth);
+                    bad |= rl_level_block(C, C.lux, l, growth);
                 pending = true;
             } else {
                 if (pending)
                     gsync();
                 pending = false;
-                bad |= rl_scale(C, l, t, T, growth);
+                bad |= rl_scale(C, C.lux, l, t, T, growth);
                 gsync();
-                rl_update(C, l, t, T);
+                rl_update(C, C.lux, l, t, T);
                 gsync();
             }
         }
         if (pending)
             gsync();
-        solve_pack(C, t, T);
+        solve_pack(C, C.lux, t, T);
     }
     bad = block_or(s, bad);
     if (threadIdx.x == 0 && bad)
@@ -1369,7 +1375,7 @@ __device__ int lu_factor(const ngsf_ckt_t &C, Ctl &s)
     }
     for (int k = threadIdx.x; k < C.n; k += blockDim.x)
         C.uinv[k] = 1.0 / C.lux[C.cdiag[k]];
-    solve_pack(C, threadIdx.x, blockDim.x);
+    solve_pack(C, C.lux, threadIdx.x, blockDim.x);
     return block_or(s, bad);
 }
 
@@ -1377,11 +1383,15 @@ __device__ int lu_factor(const ngsf_ckt_t &C, Ctl &s)
  * memory when they fit the launch's allocation, else C.work. */
 __shared__ double *g_sw;
 
-__device__ void solve_buffers_init(const ngsf_ckt_t &C, unsigned char *dyn, int dynBytes)
+__device__ void solve_buffers_init(const ngsf_ckt_t &C, unsigned char *dyn, int dynBytes,
+                                   unsigned char *lu = nullptr, int luBytes = 0)
 {
-    if (threadIdx.x == 0)
+    if (threadIdx.x == 0) {
         g_sw = (dyn && (size_t)(C.n + 1) * sizeof(double) <= (size_t)dynBytes) ? (double *)dyn
                                                                                : nullptr;
+        g_lux = (lu && (size_t)C.nlu * sizeof(double) <= (size_t)luBytes) ? (double *)lu
+                                                                          : nullptr;
+    }
     __syncthreads();
 }
 
@@ -2551,6 +2561,13 @@ __device__ int dc_tran(const ngsf_ckt_t &C, Ctl &s, long long maxSteps, bool res
                 if (s.firsttime)
                     s.mode = NGSF_MODETRAN | NGSF_MODEINITTRAN;
                 s.order = 1;
+                /* the retry factors with pivots chosen on its own matrix
+                 * (the reference re-pivots the retry of the first step
+                 * through MODEINITTRAN; here every retry after a Newton
+                 * failure does: a failing Newton is the symptom of pivots
+                 * gone stale, and fresh ones cost one host pause) */
+                if (C.retry_repivot)
+                    s.shouldReorder = 1;
             }
             __syncthreads();
         } else {
@@ -2642,7 +2659,7 @@ __device__ void run_circuit(const ngsf_ckt_t &C, Ctl &s, int runMode, long long 
 #define NGSF_TRAN_BOUNDS __maxnreg__(NGSF_TRAN_MAXNREG)
 __global__ void NGSF_TRAN_BOUNDS
 tran_kernel(const ngsf_ckt_t *ckts, const int *order, int nckt, int runMode,
-            long long maxSteps, int solveCap, int gnnBytes)
+            long long maxSteps, int solveCap, int gnnBytes, int luCap)
 {
     extern __shared__ __align__(16) unsigned char ngsf_dyn[];
     __shared__ Ctl s;
@@ -2661,7 +2678,8 @@ tran_kernel(const ngsf_ckt_t *ckts, const int *order, int nckt, int runMode,
     if (threadIdx.x == 0)
         Cs.wide = nullptr;
     __syncthreads();
-    solve_buffers_init(Cs, ngsf_dyn, solveCap);
+    solve_buffers_init(Cs, ngsf_dyn, solveCap, luCap > 0 ? ngsf_dyn + solveCap + gnnBytes : nullptr,
+                       luCap);
     run_circuit(Cs, s, runMode, maxSteps);
     pred_block_fini();
 }
@@ -2830,6 +2848,7 @@ __global__ void __launch_bounds__(NGSF_THREADS) stamp_static_kernel(ngsf_ckt_t C
     __syncthreads();
     if (threadIdx.x == 0) {      /* RUN_PROBE stamps only: no solve buffers */
         g_sw = nullptr;
+        g_lux = nullptr;
         g_psm = nullptr;
     }
     run_circuit(Cs, s, RUN_PROBE, 0);
@@ -3246,22 +3265,43 @@ extern "C" int ngsf_tran_occupancy(int threads, int dynSmem, int *regs, int *sme
  * blocks). */
 extern "C" cudaError_t ngsf_launch_tran(const ngsf_ckt_t *d_ckts, const int *d_order, int nckt,
                                         int runMode, long long maxSteps, int solveCap,
-                                        int gnnBytes, int threads, cudaStream_t stream)
+                                        int gnnBytes, int luCap, int threads, cudaStream_t stream)
 {
     if (nckt <= 0)
         return cudaSuccess;
     if (threads != 64 && threads != 128)
         threads = NGSF_THREADS;
     /* the dynamic shared memory this launch uses, no more (a larger
-     * maximum can cost resident blocks) */
+     * maximum can cost resident blocks): solve vector, predictor staging,
+     * factor values */
+    const int dyn = solveCap + gnnBytes + luCap;
     cudaError_t e = cudaFuncSetAttribute((const void *)tran_kernel,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         solveCap + gnnBytes);
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
     if (e != cudaSuccess)
         return e;
-    tran_kernel<<<nckt, threads, (size_t)solveCap + (size_t)gnnBytes, stream>>>(
-        d_ckts, d_order, nckt, runMode, maxSteps, solveCap, gnnBytes);
+    tran_kernel<<<nckt, threads, (size_t)dyn, stream>>>(d_ckts, d_order, nckt, runMode, maxSteps,
+                                                       solveCap, gnnBytes, luCap);
     return cudaGetLastError();
+}
+
+/* Room for the factor values of a batched circuit block in dynamic shared
+ * memory: the largest circuit's nlu doubles, capped by what the block has
+ * left next to the solve vector and the predictor staging; 0 when less
+ * than 16 KB would be left (such batches keep the values in L2). */
+extern "C" int ngsf_lu_smem_bytes(int maxnlu, int otherDyn)
+{
+    int dev = 0, optin = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
+        return 0;
+    cudaFuncAttributes fa{};
+    if (cudaFuncGetAttributes(&fa, (const void *)tran_kernel) != cudaSuccess)
+        return 0;
+    long long room = (long long)optin - (long long)fa.sharedSizeBytes - otherDyn - 1024;
+    room &= ~127LL;
+    long long want = ((long long)maxnlu * (long long)sizeof(double) + 127) & ~127LL;
+    const long long cap = want < room ? want : room;
+    return cap >= 16 * 1024 ? (int)cap : 0;
 }
 
 /* ---------------------------------------------------------------- */

@@ -334,9 +334,11 @@ typedef struct {
      * stops (NGSF_HELD) at the two points where the reference calls
      * sharedsync, so that the host can hand the step to the caller */
     int sync;
-    /* L-entry growth past which a transient refactorization asks for new
-     * pivots (0: only zero or non-finite pivots do) */
+    /* transient re-pivot rules beyond the reference's zero pivot: the
+     * retry after a Newton failure factors with new pivots (retry_repivot)
+     * and, when tran_growth > 0, an L entry past it asks for new pivots */
     double tran_growth;
+    int retry_repivot;
 } ngsf_ckt_t;
 
 /* phases of the per-phase clock record */

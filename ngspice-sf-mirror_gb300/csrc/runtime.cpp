@@ -43,7 +43,8 @@ extern "C" cudaError_t ngsf_launch_tran_wide(const ngsf_ckt_t *d_ckt, int nblock
                                              cudaStream_t stream);
 extern "C" cudaError_t ngsf_launch_tran(const ngsf_ckt_t *d_ckts, const int *d_order, int nckt,
                                         int runMode, long long maxSteps, int solveCap,
-                                        int gnnBytes, int threads, cudaStream_t stream);
+                                        int gnnBytes, int luCap, int threads, cudaStream_t stream);
+extern "C" int ngsf_lu_smem_bytes(int maxnlu, int otherDyn);
 extern "C" int ngsf_ctl_bytes(void);
 extern "C" cudaError_t ngsf_sync_write(void *ctlsave, double delta, int reply);
 extern "C" int ngsf_tran_occupancy(int threads, int dynSmem, int *regs, int *smem);
@@ -295,9 +296,13 @@ void DeviceCircuit::upload(const Image &img, const std::vector<int> &probes, int
     h.prof = (ph && atoi(ph) != 0) ? (long long *)(b + o.prof) : nullptr;
     h.pause_at = INFINITY;
     h.run_resume = 0;
-    /* transient re-pivot on L growth past 1e6 (NGSF_TRAN_GROWTH overrides;
-     * 0 turns it off) */
-    h.tran_growth = 1e6;
+    /* transient re-pivot rules: the retry after a Newton failure takes new
+     * pivots (NGSF_RETRY_REPIVOT=0 turns it off); L growth past a limit
+     * (NGSF_TRAN_GROWTH, off by default) */
+    h.retry_repivot = 1;
+    if (const char *r = getenv("NGSF_RETRY_REPIVOT"))
+        h.retry_repivot = atoi(r) != 0;
+    h.tran_growth = 0.0;
     if (const char *g = getenv("NGSF_TRAN_GROWTH"))
         h.tran_growth = atof(g);
     if (!impl->d_desc)
@@ -838,13 +843,14 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
                 throw std::runtime_error("too many re-pivot rounds");
             std::vector<ngsf_ckt_t> descs;
             std::vector<Prepared *> wide;
-            int maxn = 0, learned = 0;
+            int maxn = 0, learned = 0, maxnlu = 0;
             for (auto *c : pending) {
                 if (c->wide && allowWide) {
                     wide.push_back(c);
                 } else {
                     descs.push_back(c->dev->desc());
                     maxn = std::max(maxn, c->img.n);
+                    maxnlu = std::max(maxnlu, c->dev->desc().nlu);
                     learned |= c->dev->desc().pred.kind == 2;
                 }
             }
@@ -865,6 +871,10 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
                               cudaMemcpyHostToDevice), "cudaMemcpy(order)");
                 const int solveCap = ngsf_solve_smem_bytes(maxn);
                 const int gnnBytes = ngsf_pred_smem_bytes(learned);
+                /* the factor values in shared memory (NGSF_LU_SMEM=0: in L2) */
+                int luCap = 0;
+                if (!(getenv("NGSF_LU_SMEM") && atoi(getenv("NGSF_LU_SMEM")) == 0))
+                    luCap = ngsf_lu_smem_bytes(maxnlu, solveCap + gnnBytes);
                 /* one 256-thread block per circuit (measured faster than
                  * two 128-thread or four 64-thread circuits sharing an SM:
                  * the refactorization and solves need the threads more than
@@ -876,7 +886,8 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
                     threads = atoi(bt);
                 cudaEventRecord(e0, 0);
                 ck(ngsf_launch_tran(d, d_order, (int)descs.size(), mode | (holdNow ? 4 : 0),
-                                   maxSteps, solveCap, gnnBytes, threads, 0), "launch(tran)");
+                                   maxSteps, solveCap, gnnBytes, luCap, threads, 0),
+                   "launch(tran)");
                 cudaEventRecord(e1, 0);
                 ck(cudaEventSynchronize(e1), "tran");
                 float ms = 0;
@@ -885,11 +896,13 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
                 nl++;
                 if (trace) {
                     int regs = 0, smem = 0;
-                    const int per = ngsf_tran_occupancy(threads, solveCap + gnnBytes, &regs, &smem);
+                    const int per = ngsf_tran_occupancy(threads, solveCap + gnnBytes + luCap, &regs,
+                                                        &smem);
                     fprintf(stderr, "ngsf: launch %d: %zu circuits, largest n %d, %d threads"
-                            " (%d blocks per SM; %d registers, %d + %d shared bytes),%s %.3f ms\n",
+                            " (%d blocks per SM; %d registers, %d + %d shared bytes, %d of them"
+                            " factor values),%s %.3f ms\n",
                             nl, descs.size(), maxn, threads, per, regs, smem,
-                            solveCap + gnnBytes, holdNow ? " hold," : "", ms);
+                            solveCap + gnnBytes + luCap, luCap, holdNow ? " hold," : "", ms);
                 }
             }
             for (auto *c : wide) {

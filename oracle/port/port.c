@@ -1111,17 +1111,17 @@ static int ckt_load_devices(port_t *c)
 /* ------------------------------------------------------------------ */
 /* sparse refactorization on the planned pattern: left-looking, columns
  * in dependency-level order; fails (asking for new pivots) on a zero or
- * non-finite pivot or a non-finite L entry, and on an L entry above 1e6
- * (the engine's rule: klu_refactor, src/maths/KLU/klusmp.c:591-602, fails
- * on a zero pivot only, but KLU's ordering rarely lets the pivots of a
- * later matrix grow that far; the planner's Markowitz order sometimes
- * does, in the operating point under gmin and source stepping and, rarely,
- * in the transient). */
+ * non-finite pivot or a non-finite L entry, and in the operating point
+ * (MODEDCOP / MODETRANOP, where gmin and source stepping move the matrix
+ * far from the one the pivots were chosen on) also on an L entry above
+ * 1e6.  The transient refactors on its pivots like klu_refactor
+ * (src/maths/KLU/klusmp.c:591-602: only a zero pivot fails); the retry
+ * after a Newton failure re-pivots (port_run). */
 static int sp_factor(port_t *c)
 {
     port_plan_t *P = &c->plan;
     int n = c->n;
-    const double growth = 1e6;
+    const double growth = (c->mode & (MODEDCOP | MODETRANOP)) ? 1e6 : DBL_MAX;
     double *lux = c->lux;
     memset(lux, 0, sizeof(double) * (size_t)P->nlu);
     for (int p = 0; p < c->nnz; p++)
@@ -1863,6 +1863,9 @@ int port_run(port_t *c, long *stats, long maxSteps)
                 if (firsttime)
                     c->mode = MODETRAN | MODEINITTRAN;
                 c->order = 1;
+                /* the engine's rule: the retry after a Newton failure
+                 * factors with pivots chosen on its own matrix */
+                c->shouldReorder = 1;
             } else {
                 if (firsttime) {
                     firsttime = 0;

