@@ -54,8 +54,8 @@ BYTES_SRC = 120
 BYTES_BSIM4 = 2296
 BYTES_DIO = 748
 
-DEFAULT_INSTANCES = {"c0": 1216, "c1": 1, "c2": 1024, "c4": 4096}
-DEFAULT_WINDOW = {"c0": "20n", "c1": "500p", "c2": "2n", "c4": "2n"}
+DEFAULT_INSTANCES = {"c0": 1216, "c1": 1, "c2": 1024, "c3": 1, "c4": 4096}
+DEFAULT_WINDOW = {"c0": "20n", "c1": "500p", "c2": "2n", "c3": "50p", "c4": "2n"}
 # transistor-count range of the Monte Carlo instances
 MC_RANGE = {"c2": (100, 3000), "c4": (100, 5000)}
 
@@ -88,6 +88,12 @@ def workload_texts(name: str, tstop: str | None, instances: int) -> tuple[list[s
             "circuit": "seeded random CMOS logic, 10,000 BSIM4 (level 54) transistors, gate mix"
                        " INV/NAND2/NOR2 40/35/25 %, RC pi nets, 64 PULSE inputs, VDD 1.0 V",
             "tran": f".tran 1p {tstop} (the first {tstop} of the 5n transient)"}
+    if name == "c3":
+        return [netlists.logic_with_rings(n_transistors=50000, seed=3, rings=16, stages=31,
+                                          tstop=tstop)] * instances, {
+            "circuit": "seeded random CMOS logic, 50,000 BSIM4 transistors, with 16 embedded"
+                       " 31-stage ring oscillators (RC-loaded stages, a 0.2 mA kick each)",
+            "tran": f".tran 1p {tstop} (the first {tstop} of the 10n transient)"}
     if name in ("c2", "c4"):
         sizes = mc_sizes(name, instances)
         base = 0 if name == "c2" else 100000
@@ -203,12 +209,13 @@ def cpu_pool(texts: list[str], procs: int) -> tuple[int, float]:
 def cpu_measure(args) -> dict:
     """One bounded CPU sample of the workload on the host cores.
 
-    c0/c2: independent instances, one port process per core over a sample
-    of the instances (throughput = accepted steps / makespan).  c1: one
-    circuit; the port is single-threaded, so one core; the rate is the
-    marginal one between a 20p and a 50p window of the same netlist
-    (accepted steps and seconds of the difference), which leaves out the
-    operating point and favours the CPU."""
+    c0/c2/c4: independent instances, one port process per core over a
+    sample of the instances (throughput = accepted steps / makespan).
+    c1/c3: one circuit; the port is single-threaded, so one core; the rate
+    is the marginal one between two windows of the same netlist (20p and
+    50p; 3p and 8p for the 50,000-transistor c3), accepted steps and
+    seconds of the difference, which leaves out the operating point and
+    favours the CPU."""
     sys.path.insert(0, os.path.join(ROOT, "oracle", "port"))
     import port
     port.build()
@@ -222,6 +229,16 @@ def cpu_measure(args) -> dict:
         return {"value": (a2 - a1) / max(t2 - t1, 1e-9), "cores": 1, "seconds": t1 + t2,
                 "sample": f"C1 netlist on 1 core (single-threaded port): accepted steps between the"
                           f" 20p and 50p windows ({a2 - a1} steps in {t2 - t1:.1f} s; operating"
+                          f" point excluded)"}
+    if args.workload == "c3":
+        from ngspice_gb300 import netlists
+        short = netlists.logic_with_rings(n_transistors=50000, seed=3, tstop="3p")
+        long_ = netlists.logic_with_rings(n_transistors=50000, seed=3, tstop="8p")
+        a1, t1 = _cpu_one(short)
+        a2, t2 = _cpu_one(long_)
+        return {"value": (a2 - a1) / max(t2 - t1, 1e-9), "cores": 1, "seconds": t1 + t2,
+                "sample": f"C3 netlist on 1 core (single-threaded port): accepted steps between the"
+                          f" 3p and 8p windows ({a2 - a1} steps in {t2 - t1:.1f} s; operating"
                           f" point excluded)"}
     if args.workload == "c0":
         texts, _ = workload_texts(args.workload, args.tstop, args.instances)
@@ -330,8 +347,9 @@ def engine_arm(args, texts, wdesc, rank, world) -> dict | None:
     mc = args.workload in ("c2", "c4")
     # one observed node per instance for the batches (c0: the chain's
     # output, c2/c4: the first gate output); every unknown for the single c1
-    probes = {"c0": ["n32"], "c1": None, "c2": ["y0"], "c4": ["y0"]}[args.workload]
-    outcap = 8192 if args.workload == "c1" else (4096 if mc else 1024)
+    probes = {"c0": ["n32"], "c1": None, "c2": ["y0"], "c3": ["ro0_0", "ro15_0", "y0"],
+              "c4": ["y0"]}[args.workload]
+    outcap = 8192 if args.workload in ("c1", "c3") else (4096 if mc else 1024)
     if mc:
         # Monte Carlo batch: instances stop after their first accepted step
         # until no instance still pauses for new pivots (operating point,
@@ -526,6 +544,37 @@ def engine_arm(args, texts, wdesc, rank, world) -> dict | None:
                 forms[name + "_vs_plain"] = (k_acc / k_sec) / forms["plain_gpu"]["value"]
             progress(f"{name}: {k_acc / k_sec:.1f} accepted steps/s,"
                      f" {k_it / max(k_acc, 1):.3f} Newton iterations per step")
+    if args.workload == "c3" and args.predictors:
+        # the single large circuit with the Newton predictors: the same run
+        # from the quadratic guess (3) and with the learned correction (2),
+        # against the plain start timed above
+        forms = out_extra.setdefault("forms", {})
+        forms["plain"] = {"value": value, "newton_iterations_per_accepted_step":
+                          iters / max(accepted, 1)}
+        for kind in [int(k) for k in args.predictors.split(",") if k.strip()]:
+            params, train_info = None, None
+            if kind == 2:
+                params, train_info = train_network(args)
+                progress(f"network trained in {train_info['seconds']:.1f} s")
+            c = open_all(texts)[0]
+            if tuned:
+                c.set_factor_shape(tuned["blocks"], tuned["small_work"])
+            c.set_predictor(kind, params)
+            k_sec = E.run([c])
+            r = c.results()
+            name = {3: "quadratic_guess", 2: "learned"}.get(kind, f"k{kind}")
+            forms[name] = {"value": int(r[E.R_ACCEPTED]) / k_sec, "status": int(r[E.R_STATUS]),
+                           "newton_iterations_per_accepted_step":
+                               int(r[E.R_TRANITER]) / max(int(r[E.R_ACCEPTED]), 1),
+                           "accepted_on_first_iteration": int(r[E.R_GUESS1]),
+                           "steps_from_a_guess": int(r[E.R_GUESSES])}
+            if train_info:
+                forms[name]["training"] = train_info
+            forms[name + "_vs_plain"] = forms[name]["value"] / value
+            progress(f"{name}: {forms[name]['value']:.1f} accepted steps/s,"
+                     f" {forms[name]['newton_iterations_per_accepted_step']:.3f} Newton"
+                     " iterations per step")
+            c.close()
     if tuned:
         out_extra["refactor_shape"] = {"blocks": tuned["blocks"],
                                        "one_block_levels_up_to": tuned["small_work"]}
@@ -735,7 +784,7 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="engine", choices=["engine", "reference"])
-    ap.add_argument("--workload", default="c2", choices=["c0", "c1", "c2", "c4"])
+    ap.add_argument("--workload", default="c2", choices=["c0", "c1", "c2", "c3", "c4"])
     ap.add_argument("--window", default="25p",
                     help="Monte Carlo workloads: a step advances every instance by this much of"
                          " its transient")

@@ -315,6 +315,16 @@ NGSF_API int ngsf_ni_convtest(ngsf_handle *h, const double *rhs, const double *r
  * KLU's Ax): set them, or read them back after a load. */
 NGSF_API int ngsf_smp_set_matrix(ngsf_handle *h, const double *ax);
 NGSF_API int ngsf_smp_get_matrix(const ngsf_handle *h, double *ax);
+/* SMPpreOrder's symbolic analysis (klu_analyze with btf = TRUE,
+ * src/maths/KLU/klusmp.c SMPpreOrder): the block upper triangular form of
+ * the pattern from a maximum transversal and the strongly connected
+ * components of the matched graph; *nblocks diagonal blocks, the largest
+ * *largest_block unknowns.  Works on host-only handles.  The engine's
+ * pivot planner does not use the blocks by default: its Markowitz
+ * elimination with singleton rows first already reaches KLU's fill;
+ * NGSF_ORDER=klu makes it factor in the BTF order, each block in a
+ * minimum degree order, with KLU's diagonal-preferring threshold pivots. */
+NGSF_API int ngsf_smp_preorder(const ngsf_handle *h, int *nblocks, int *largest_block);
 /* SMPreorder: new pivots from the device matrix (threshold pivoting with
  * pivrel and pivtol, diag_gmin added to every structural diagonal), then
  * the device factorization on them.  Returns 0, NGSF_E_SINGULAR (102), or

@@ -1034,6 +1034,20 @@ NGSF_API int ngsf_smp_reorder(ngsf_handle *h, double pivtol, double pivrel, doub
     return ngsf_internal_lufac(h, diag_gmin);
 }
 
+NGSF_API int ngsf_smp_preorder(const ngsf_handle *h, int *nblocks, int *largest_block)
+{
+    if (!h)
+        return fail("ngsf_smp_preorder: null handle");
+    int nb = 0, big = 0;
+    if (!btf_analyze(h->p.img.n, h->p.img.a_cp, h->p.img.a_ri, nb, big))
+        return fail("ngsf_smp_preorder: structurally singular matrix");
+    if (nblocks)
+        *nblocks = nb;
+    if (largest_block)
+        *largest_block = big;
+    return 0;
+}
+
 NGSF_API int ngsf_phase_cycles(const ngsf_handle *h, long long *cycles)
 {
     const ngsf_ckt_t *d = ngsf_internal_desc(h);

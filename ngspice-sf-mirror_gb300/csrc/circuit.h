@@ -152,6 +152,7 @@ struct Image {
     std::vector<int> rl_ptr, rl_col, sc_ptr, sc_pos, sc_piv;
     std::vector<int> ud_ptr, ud_dst, ud_cptr, ud_l, ud_u, ud_p;
     double lu_flops = 0;   /* multiply-adds of one refactorization */
+    int btf_blocks = 0;    /* diagonal blocks of the KLU order (NGSF_ORDER=klu) */
     std::vector<std::string> names;  /* equation names 1..n */
 };
 

@@ -1235,11 +1235,6 @@ __device__ void solve_pack(const ngsf_ckt_t &C, const double *lux, int t, int T)
         C.uval[q] = lux[C.ur_pos[q]];
 }
 
-/* The factor values of a batched circuit block: dynamic shared memory
- * when the launch reserved room for them (the block path of a batch; the
- * right-looking schedule then reads and writes shared memory instead of
- * L2), else C.lux. */
-__shared__ double *g_lux;
 
 /* blocks of a wide launch that take part in the refactorization: enough
  * threads for the widest levels, few enough for a cheap barrier */
@@ -1250,7 +1245,7 @@ __device__ int lu_factor_rl(const ngsf_ckt_t &C, Ctl &s, int b, int nbAll)
     int bad = 0;
     const double growth = growth_limit(C, s);
     if (nbAll <= 1) {
-        double *lux = g_lux ? g_lux : C.lux;
+        double *lux = C.lux;
         for (int q = threadIdx.x; q < C.nlu; q += blockDim.x)
             lux[q] = 0.0;
         __syncthreads();
@@ -1383,15 +1378,11 @@ __device__ int lu_factor(const ngsf_ckt_t &C, Ctl &s)
  * memory when they fit the launch's allocation, else C.work. */
 __shared__ double *g_sw;
 
-__device__ void solve_buffers_init(const ngsf_ckt_t &C, unsigned char *dyn, int dynBytes,
-                                   unsigned char *lu = nullptr, int luBytes = 0)
+__device__ void solve_buffers_init(const ngsf_ckt_t &C, unsigned char *dyn, int dynBytes)
 {
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0)
         g_sw = (dyn && (size_t)(C.n + 1) * sizeof(double) <= (size_t)dynBytes) ? (double *)dyn
                                                                                : nullptr;
-        g_lux = (lu && (size_t)C.nlu * sizeof(double) <= (size_t)luBytes) ? (double *)lu
-                                                                          : nullptr;
-    }
     __syncthreads();
 }
 
@@ -2659,7 +2650,7 @@ __device__ void run_circuit(const ngsf_ckt_t &C, Ctl &s, int runMode, long long 
 #define NGSF_TRAN_BOUNDS __maxnreg__(NGSF_TRAN_MAXNREG)
 __global__ void NGSF_TRAN_BOUNDS
 tran_kernel(const ngsf_ckt_t *ckts, const int *order, int nckt, int runMode,
-            long long maxSteps, int solveCap, int gnnBytes, int luCap)
+            long long maxSteps, int solveCap, int gnnBytes)
 {
     extern __shared__ __align__(16) unsigned char ngsf_dyn[];
     __shared__ Ctl s;
@@ -2678,8 +2669,7 @@ tran_kernel(const ngsf_ckt_t *ckts, const int *order, int nckt, int runMode,
     if (threadIdx.x == 0)
         Cs.wide = nullptr;
     __syncthreads();
-    solve_buffers_init(Cs, ngsf_dyn, solveCap, luCap > 0 ? ngsf_dyn + solveCap + gnnBytes : nullptr,
-                       luCap);
+    solve_buffers_init(Cs, ngsf_dyn, solveCap);
     run_circuit(Cs, s, runMode, maxSteps);
     pred_block_fini();
 }
@@ -2848,7 +2838,6 @@ __global__ void __launch_bounds__(NGSF_THREADS) stamp_static_kernel(ngsf_ckt_t C
     __syncthreads();
     if (threadIdx.x == 0) {      /* RUN_PROBE stamps only: no solve buffers */
         g_sw = nullptr;
-        g_lux = nullptr;
         g_psm = nullptr;
     }
     run_circuit(Cs, s, RUN_PROBE, 0);
@@ -3265,43 +3254,24 @@ extern "C" int ngsf_tran_occupancy(int threads, int dynSmem, int *regs, int *sme
  * blocks). */
 extern "C" cudaError_t ngsf_launch_tran(const ngsf_ckt_t *d_ckts, const int *d_order, int nckt,
                                         int runMode, long long maxSteps, int solveCap,
-                                        int gnnBytes, int luCap, int threads, cudaStream_t stream)
+                                        int gnnBytes, int threads, cudaStream_t stream)
 {
     if (nckt <= 0)
         return cudaSuccess;
     if (threads != 64 && threads != 128)
         threads = NGSF_THREADS;
-    /* the dynamic shared memory this launch uses, no more (a larger
-     * maximum can cost resident blocks): solve vector, predictor staging,
-     * factor values */
-    const int dyn = solveCap + gnnBytes + luCap;
+    /* the dynamic shared memory this launch uses, no more: a larger
+     * reservation takes its room from the L1 cache, which the
+     * refactorization's and solves' loads hit (factor values staged in
+     * 209 KB of shared memory per block instead ran 6 % slower) */
     cudaError_t e = cudaFuncSetAttribute((const void *)tran_kernel,
-                                         cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
+                                         cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         solveCap + gnnBytes);
     if (e != cudaSuccess)
         return e;
-    tran_kernel<<<nckt, threads, (size_t)dyn, stream>>>(d_ckts, d_order, nckt, runMode, maxSteps,
-                                                       solveCap, gnnBytes, luCap);
+    tran_kernel<<<nckt, threads, (size_t)solveCap + (size_t)gnnBytes, stream>>>(
+        d_ckts, d_order, nckt, runMode, maxSteps, solveCap, gnnBytes);
     return cudaGetLastError();
-}
-
-/* Room for the factor values of a batched circuit block in dynamic shared
- * memory: the largest circuit's nlu doubles, capped by what the block has
- * left next to the solve vector and the predictor staging; 0 when less
- * than 16 KB would be left (such batches keep the values in L2). */
-extern "C" int ngsf_lu_smem_bytes(int maxnlu, int otherDyn)
-{
-    int dev = 0, optin = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess ||
-        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) != cudaSuccess)
-        return 0;
-    cudaFuncAttributes fa{};
-    if (cudaFuncGetAttributes(&fa, (const void *)tran_kernel) != cudaSuccess)
-        return 0;
-    long long room = (long long)optin - (long long)fa.sharedSizeBytes - otherDyn - 1024;
-    room &= ~127LL;
-    long long want = ((long long)maxnlu * (long long)sizeof(double) + 127) & ~127LL;
-    const long long cap = want < room ? want : room;
-    return cap >= 16 * 1024 ? (int)cap : 0;
 }
 
 /* ---------------------------------------------------------------- */

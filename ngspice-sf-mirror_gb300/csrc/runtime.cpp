@@ -43,8 +43,7 @@ extern "C" cudaError_t ngsf_launch_tran_wide(const ngsf_ckt_t *d_ckt, int nblock
                                              cudaStream_t stream);
 extern "C" cudaError_t ngsf_launch_tran(const ngsf_ckt_t *d_ckts, const int *d_order, int nckt,
                                         int runMode, long long maxSteps, int solveCap,
-                                        int gnnBytes, int luCap, int threads, cudaStream_t stream);
-extern "C" int ngsf_lu_smem_bytes(int maxnlu, int otherDyn);
+                                        int gnnBytes, int threads, cudaStream_t stream);
 extern "C" int ngsf_ctl_bytes(void);
 extern "C" cudaError_t ngsf_sync_write(void *ctlsave, double delta, int reply);
 extern "C" int ngsf_tran_occupancy(int threads, int dynSmem, int *regs, int *smem);
@@ -843,14 +842,13 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
                 throw std::runtime_error("too many re-pivot rounds");
             std::vector<ngsf_ckt_t> descs;
             std::vector<Prepared *> wide;
-            int maxn = 0, learned = 0, maxnlu = 0;
+            int maxn = 0, learned = 0;
             for (auto *c : pending) {
                 if (c->wide && allowWide) {
                     wide.push_back(c);
                 } else {
                     descs.push_back(c->dev->desc());
                     maxn = std::max(maxn, c->img.n);
-                    maxnlu = std::max(maxnlu, c->dev->desc().nlu);
                     learned |= c->dev->desc().pred.kind == 2;
                 }
             }
@@ -871,10 +869,6 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
                               cudaMemcpyHostToDevice), "cudaMemcpy(order)");
                 const int solveCap = ngsf_solve_smem_bytes(maxn);
                 const int gnnBytes = ngsf_pred_smem_bytes(learned);
-                /* the factor values in shared memory (NGSF_LU_SMEM=0: in L2) */
-                int luCap = 0;
-                if (!(getenv("NGSF_LU_SMEM") && atoi(getenv("NGSF_LU_SMEM")) == 0))
-                    luCap = ngsf_lu_smem_bytes(maxnlu, solveCap + gnnBytes);
                 /* one 256-thread block per circuit (measured faster than
                  * two 128-thread or four 64-thread circuits sharing an SM:
                  * the refactorization and solves need the threads more than
@@ -886,8 +880,7 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
                     threads = atoi(bt);
                 cudaEventRecord(e0, 0);
                 ck(ngsf_launch_tran(d, d_order, (int)descs.size(), mode | (holdNow ? 4 : 0),
-                                   maxSteps, solveCap, gnnBytes, luCap, threads, 0),
-                   "launch(tran)");
+                                   maxSteps, solveCap, gnnBytes, threads, 0), "launch(tran)");
                 cudaEventRecord(e1, 0);
                 ck(cudaEventSynchronize(e1), "tran");
                 float ms = 0;
@@ -896,13 +889,11 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
                 nl++;
                 if (trace) {
                     int regs = 0, smem = 0;
-                    const int per = ngsf_tran_occupancy(threads, solveCap + gnnBytes + luCap, &regs,
-                                                        &smem);
+                    const int per = ngsf_tran_occupancy(threads, solveCap + gnnBytes, &regs, &smem);
                     fprintf(stderr, "ngsf: launch %d: %zu circuits, largest n %d, %d threads"
-                            " (%d blocks per SM; %d registers, %d + %d shared bytes, %d of them"
-                            " factor values),%s %.3f ms\n",
+                            " (%d blocks per SM; %d registers, %d + %d shared bytes),%s %.3f ms\n",
                             nl, descs.size(), maxn, threads, per, regs, smem,
-                            solveCap + gnnBytes + luCap, luCap, holdNow ? " hold," : "", ms);
+                            solveCap + gnnBytes, holdNow ? " hold," : "", ms);
                 }
             }
             for (auto *c : wide) {

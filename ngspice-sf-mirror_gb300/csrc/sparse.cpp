@@ -16,6 +16,7 @@
  */
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <array>
 #include <map>
 #include <set>
@@ -25,10 +26,267 @@
 
 namespace ngsf {
 
+namespace {
+
+/* Maximum transversal (the zero-free diagonal btf_maxtrans looks for,
+ * BTF/Source/btf_maxtrans.c): colRow[j] = the row matched to column j.
+ * Cheap passes take each column's own diagonal entry where the pattern has
+ * one, then the first free row; every column left unmatched searches
+ * depth first for an augmenting path (Duff's MC21).  Keeping the natural
+ * diagonal makes the matched entries the MNA diagonal wherever it exists,
+ * so the symmetric ordering of each block sees the circuit's own graph
+ * (the blocks themselves do not depend on which maximum matching is
+ * taken).  Returns false when the matrix is structurally singular. */
+bool max_transversal(int n, const std::vector<int> &cp, const std::vector<int> &ri,
+                     std::vector<int> &colRow)
+{
+    std::vector<int> rowCol(n, -1);
+    colRow.assign(n, -1);
+    for (int j = 0; j < n; j++)
+        for (int p = cp[j]; p < cp[j + 1]; p++)
+            if (ri[p] == j) {
+                rowCol[j] = j;
+                colRow[j] = j;
+                break;
+            }
+    for (int j = 0; j < n; j++)
+        if (colRow[j] < 0)
+            for (int p = cp[j]; p < cp[j + 1]; p++)
+                if (rowCol[ri[p]] < 0) {
+                    rowCol[ri[p]] = j;
+                    colRow[j] = ri[p];
+                    break;
+                }
+    std::vector<int> visited(n, -1);
+    std::vector<int> stCol, stPtr, viaRow;   /* viaRow[t]: row leading to stCol[t + 1] */
+    for (int j0 = 0; j0 < n; j0++) {
+        if (colRow[j0] >= 0)
+            continue;
+        stCol.assign(1, j0);
+        stPtr.assign(1, cp[j0]);
+        viaRow.clear();
+        visited[j0] = j0;
+        int found = -1;
+        while (!stCol.empty() && found < 0) {
+            const int t = (int)stCol.size() - 1, j = stCol[t];
+            bool pushed = false;
+            while (stPtr[t] < cp[j + 1]) {
+                const int i = ri[stPtr[t]++];
+                if (rowCol[i] < 0) {
+                    found = i;
+                    break;
+                }
+                const int j2 = rowCol[i];
+                if (visited[j2] != j0) {
+                    visited[j2] = j0;
+                    stCol.push_back(j2);
+                    stPtr.push_back(cp[j2]);
+                    viaRow.push_back(i);
+                    pushed = true;
+                    break;
+                }
+            }
+            if (found < 0 && !pushed) {
+                stCol.pop_back();
+                stPtr.pop_back();
+                if (!viaRow.empty())
+                    viaRow.pop_back();
+            }
+        }
+        if (found < 0)
+            return false;
+        /* the last column takes the free row, each earlier one the row
+         * through which the path left it */
+        for (int t = (int)stCol.size() - 1; t >= 0; t--) {
+            const int i = t == (int)stCol.size() - 1 ? found : viaRow[t];
+            colRow[stCol[t]] = i;
+            rowCol[i] = stCol[t];
+        }
+    }
+    return true;
+}
+
+/* Column order of KLU's analysis (klu_analyze.c:451 with btf = TRUE,
+ * ordering = AMD): the block upper triangular form from the maximum
+ * transversal and the strongly connected components of the matched graph
+ * (btf_strongcomp, Tarjan), blocks in topological order; within a block a
+ * minimum degree order of the block's symmetrised pattern (AMD's
+ * criterion, with exact degrees on the elimination graph; ties by column
+ * index).  Q: columns in elimination order; colRow: each column's matched
+ * ("diagonal") row; nblocks: the number of diagonal blocks. */
+bool btf_md_order(int n, const std::vector<int> &cp, const std::vector<int> &ri,
+                  std::vector<int> &Q, std::vector<int> &colRow, int &nblocks,
+                  int *largest = nullptr)
+{
+    if (!max_transversal(n, cp, ri, colRow))
+        return false;
+    /* rows as lists of columns */
+    std::vector<int> rp(n + 1, 0), rc(cp[n]);
+    for (int p = 0; p < cp[n]; p++)
+        rp[ri[p] + 1]++;
+    for (int i = 0; i < n; i++)
+        rp[i + 1] += rp[i];
+    {
+        std::vector<int> fill(rp.begin(), rp.end() - 1);
+        for (int j = 0; j < n; j++)
+            for (int p = cp[j]; p < cp[j + 1]; p++)
+                rc[fill[ri[p]]++] = j;
+    }
+    /* node j = column j with its matched row; edge j -> k for every entry
+     * (colRow[j], k), k != j.  Iterative Tarjan. */
+    std::vector<int> index(n, -1), low(n, 0), comp(n, -1), stack;
+    std::vector<char> onStack(n, 0);
+    std::vector<std::vector<int>> comps;
+    int counter = 0;
+    std::vector<std::pair<int, int>> call;   /* (node, next entry of its row) */
+    for (int s0 = 0; s0 < n; s0++) {
+        if (index[s0] >= 0)
+            continue;
+        call.push_back({s0, rp[colRow[s0]]});
+        index[s0] = low[s0] = counter++;
+        stack.push_back(s0);
+        onStack[s0] = 1;
+        while (!call.empty()) {
+            const int v = call.back().first;
+            const int row = colRow[v];
+            bool descended = false;
+            while (call.back().second < rp[row + 1]) {
+                const int w = rc[call.back().second++];
+                if (w == v)
+                    continue;
+                if (index[w] < 0) {
+                    index[w] = low[w] = counter++;
+                    stack.push_back(w);
+                    onStack[w] = 1;
+                    call.push_back({w, rp[colRow[w]]});
+                    descended = true;
+                    break;
+                }
+                if (onStack[w])
+                    low[v] = std::min(low[v], index[w]);
+            }
+            if (descended)
+                continue;
+            if (low[v] == index[v]) {
+                std::vector<int> c;
+                int w;
+                do {
+                    w = stack.back();
+                    stack.pop_back();
+                    onStack[w] = 0;
+                    comp[w] = (int)comps.size();
+                    c.push_back(w);
+                } while (w != v);
+                comps.push_back(std::move(c));
+            }
+            call.pop_back();
+            if (!call.empty())
+                low[call.back().first] = std::min(low[call.back().first], low[v]);
+        }
+    }
+    /* Tarjan emits a component after every component it reaches: the
+     * reverse emission order puts each row's entries at or right of its
+     * block (upper block triangular) */
+    nblocks = (int)comps.size();
+    if (largest) {
+        *largest = 0;
+        for (auto &c : comps)
+            *largest = std::max(*largest, (int)c.size());
+    }
+    Q.clear();
+    Q.reserve(n);
+    std::vector<int> local(n, -1);
+    for (int b = nblocks - 1; b >= 0; b--) {
+        std::vector<int> &c = comps[b];
+        std::sort(c.begin(), c.end());
+        const int m = (int)c.size();
+        if (m == 1) {
+            Q.push_back(c[0]);
+            continue;
+        }
+        for (int t = 0; t < m; t++)
+            local[c[t]] = t;
+        /* symmetrised pattern of the block */
+        std::vector<std::vector<int>> adj(m);
+        for (int t = 0; t < m; t++) {
+            const int j = c[t];
+            const int row = colRow[j];
+            for (int p = rp[row]; p < rp[row + 1]; p++) {
+                const int k = rc[p];
+                if (k != j && local[k] >= 0 && comp[k] == b) {
+                    adj[t].push_back(local[k]);
+                    adj[local[k]].push_back(t);
+                }
+            }
+        }
+        std::vector<std::set<int>> g(m);
+        for (int t = 0; t < m; t++)
+            g[t].insert(adj[t].begin(), adj[t].end());
+        std::set<std::pair<int, int>> pq;   /* (degree, local node) */
+        for (int t = 0; t < m; t++)
+            pq.insert({(int)g[t].size(), t});
+        std::vector<char> gone(m, 0);
+        while (!pq.empty()) {
+            const int v = pq.begin()->second;
+            pq.erase(pq.begin());
+            gone[v] = 1;
+            Q.push_back(c[v]);
+            std::vector<int> nb(g[v].begin(), g[v].end());
+            for (int u : nb) {
+                pq.erase({(int)g[u].size(), u});
+                g[u].erase(v);
+            }
+            for (size_t a = 0; a < nb.size(); a++)
+                for (size_t b2 = a + 1; b2 < nb.size(); b2++) {
+                    g[nb[a]].insert(nb[b2]);
+                    g[nb[b2]].insert(nb[a]);
+                }
+            for (int u : nb)
+                pq.insert({(int)g[u].size(), u});
+            g[v].clear();
+        }
+        for (int t = 0; t < m; t++)
+            local[c[t]] = -1;
+    }
+    return (int)Q.size() == n;
+}
+
+}  // namespace
+
+bool btf_analyze(int n, const std::vector<int> &cp, const std::vector<int> &ri, int &nblocks,
+                 int &largest)
+{
+    std::vector<int> Q, colRow;
+    return btf_md_order(n, cp, ri, Q, colRow, nblocks, &largest);
+}
+
 bool plan_lu(int n, const std::vector<int> &cp, const std::vector<int> &ri,
              const std::vector<double> &ax, double pivrel, double pivtol,
              Image &img, std::string &err)
 {
+    /* NGSF_ORDER=klu: KLU's pivot sequence instead of threshold Markowitz:
+     * columns in the BTF + minimum degree order of the pattern, in each
+     * column the matched ("diagonal") row when its row-scaled magnitude is
+     * at least pivrel times the column's largest (klu_kernel.c lpivot with
+     * Common->tol = PivRel and scale = 2: rows scaled by their largest
+     * entry), else the largest */
+    const char *ord = getenv("NGSF_ORDER");
+    const bool kluOrder = ord && std::string(ord) == "klu";
+    std::vector<int> Q, colRow;
+    std::vector<double> rscale;
+    if (kluOrder) {
+        int nb = 0;
+        if (!btf_md_order(n, cp, ri, Q, colRow, nb)) {
+            err = "structurally singular matrix (no zero-free diagonal)";
+            return false;
+        }
+        rscale.assign(n, 0.0);
+        for (int j = 0; j < n; j++)
+            for (int p = cp[j]; p < cp[j + 1]; p++)
+                rscale[ri[p]] = std::max(rscale[ri[p]], std::fabs(ax[p]));
+        img.btf_blocks = nb;
+    }
+
     /* ---------------- numeric Markowitz elimination ------------------ */
     /* active rows: (column, value) in no particular order; active columns:
      * row sets in ascending order (the candidate search visits rows in
@@ -74,6 +332,29 @@ bool plan_lu(int n, const std::vector<int> &cp, const std::vector<int> &ri,
         int bp = -1, bq = -1;
         double bmag = 0;
         int examined = 0;
+        if (kluOrder) {
+            const int q = Q[k];
+            double amax = 0;
+            int imax = -1;
+            for (int i : cols[q]) {
+                const double a = rscale[i] > 0 ? std::fabs(val(i, q)) / rscale[i] : 0.0;
+                if (a > amax) {
+                    amax = a;
+                    imax = i;
+                }
+            }
+            const int d = colRow[q];
+            if (imax >= 0 && cols[q].count(d) && rscale[d] > 0 &&
+                std::fabs(val(d, q)) / rscale[d] >= pivrel * amax)
+                imax = d;
+            if (imax < 0 || !(std::fabs(val(imax, q)) > pivtol)) {
+                err = "singular matrix at elimination step " + std::to_string(k);
+                return false;
+            }
+            bp = imax;
+            bq = q;
+            singles.clear();
+        }
         while (!singles.empty()) {
             int i = *singles.begin();
             singles.erase(singles.begin());

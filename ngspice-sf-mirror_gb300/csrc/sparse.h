@@ -17,6 +17,12 @@ bool plan_lu(int n, const std::vector<int> &cp, const std::vector<int> &ri,
              const std::vector<double> &ax, double pivrel, double pivtol,
              Image &img, std::string &err);
 
+/* KLU's block triangular analysis of the pattern (btf_maxtrans +
+ * btf_strongcomp): the number of diagonal blocks and the largest block's
+ * size.  Returns false when the pattern is structurally singular. */
+bool btf_analyze(int n, const std::vector<int> &cp, const std::vector<int> &ri, int &nblocks,
+                 int &largest);
+
 }  // namespace ngsf
 
 #endif

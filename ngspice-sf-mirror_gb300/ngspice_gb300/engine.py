@@ -33,7 +33,8 @@ EXPORTS = [
     "ngsf_dev_table", "ngsf_ckt_load", "ngsf_ckt_read_states", "ngsf_ckt_trunc",
     "ngsf_ni_convtest", "ngsf_smp_set_matrix", "ngsf_smp_get_matrix", "ngsf_smp_reorder",
     "ngsf_smp_lufac", "ngsf_smp_solve", "ngsf_phase_cycles", "ngsf_eval_bench",
-    "ngsf_fp64_peak",
+    "ngsf_fp64_peak", "ngsf_smp_preorder", "ngsf_set_sync", "ngsf_sync_point",
+    "ngsf_sync_reply",
     "ngSpice_Init", "ngSpice_Init_Sync", "ngSpice_Command", "ngGet_Vec_Info",
     "ngSpice_Circ", "ngSpice_CurPlot", "ngSpice_AllPlots", "ngSpice_AllVecs",
     "ngSpice_running", "ngSpice_SetBkpt", "ngSpice_nospinit", "ngSpice_nospiceinit",
@@ -134,6 +135,7 @@ def lib(path: str | None = None) -> C.CDLL:
     L.ngsf_phase_cycles.argtypes = [vp, C.POINTER(C.c_longlong)]
     L.ngsf_eval_bench.argtypes = [vp, pp, C.c_int, C.c_int, C.c_int, dp]
     L.ngsf_fp64_peak.argtypes = [dp]
+    L.ngsf_smp_preorder.argtypes = [vp, ip, ip]
     L.ngsf_set_sync.argtypes = [vp, C.c_int]
     L.ngsf_sync_point.argtypes = [vp, ip, ip, dp, dp, dp]
     L.ngsf_sync_reply.argtypes = [vp, C.c_double, C.c_int]
@@ -288,6 +290,14 @@ class Circuit:
             p = params.ctypes.data_as(C.POINTER(C.c_float))
         if lib().ngsf_set_predictor(self._h, int(kind), p):
             raise EngineError(last_error())
+
+    def smp_preorder(self) -> tuple[int, int]:
+        """SMPpreOrder's block triangular analysis: (diagonal blocks,
+        largest block)."""
+        nb, big = C.c_int(), C.c_int()
+        if lib().ngsf_smp_preorder(self._h, C.byref(nb), C.byref(big)):
+            raise EngineError(last_error())
+        return nb.value, big.value
 
     # ---- synchronised runs (sharedspice GetSyncData) ----
     def set_sync(self, on: bool = True):

@@ -180,6 +180,10 @@ def random_logic(spec: RandomLogicSpec | None = None, **kw) -> str:
         pool = [x for x in nets[-s.window:] if x[1] < s.depth and fanout_left[x[0]] > 0]
         if len(pool) < k:
             pool = [x for x in nets[-4 * s.window:] if x[1] < s.depth]
+        if len(pool) < k:
+            # every recent net is at the depth limit (circuits much larger
+            # than depth x window): restart a cone from the primary inputs
+            pool = nets[:s.n_inputs]
         chosen = []
         for _ in range(k):
             cand = rng.choice(pool)
@@ -253,3 +257,41 @@ def random_logic(spec: RandomLogicSpec | None = None, **kw) -> str:
         fanout_left[z] = rng.randint(1, 4)
     lines += [f".tran {s.tstep} {s.tstop}", ".options klu", ".end", ""]
     return "\n".join(lines)
+
+
+def logic_with_rings(n_transistors: int = 50000, seed: int = 3, rings: int = 16,
+                     stages: int = 31, tstep: str = "1p", tstop: str = "10n") -> str:
+    """The random-logic netlist of `n_transistors` BSIM4 transistors with
+    `rings` embedded ring oscillators of `stages` inverters each (odd), the
+    single large circuit of the learned-predictor workload.  Every stage
+    drives an RC pi segment like the logic's nets; each ring's first stage
+    gets a 0.2 mA, 20 ps current kick (staggered per ring) that moves it off
+    its metastable operating point, and each ring's first node also drives
+    a loaded inverter, as a tap of the ring would."""
+    base = random_logic(n_transistors=n_transistors, seed=seed, tstep=tstep, tstop=tstop)
+    rng = random.Random(seed + 7919)
+    body = base.split("\n")
+    tail = [ln for ln in body if ln.startswith(".tran") or ln.startswith(".options")
+            or ln == ".end" or ln == ""]
+    head = [ln for ln in body if ln not in tail]
+    lines = list(head)
+    for r in range(rings):
+        for k in range(stages):
+            a = f"ro{r}_{k}"
+            y = f"ro{r}_{(k + 1) % stages}"
+            wn = rng.uniform(180e-9, 360e-9)
+            wp = 2.0 * wn
+            lines.append(f"mrn{r}_{k} {y}x {a} 0 0 nch w={_fmt(wn)} l=45n")
+            lines.append(f"mrp{r}_{k} {y}x {a} vdd vdd pch w={_fmt(wp)} l=45n")
+            rval = math.exp(rng.uniform(math.log(10.0), math.log(200.0)))
+            cval = math.exp(rng.uniform(math.log(0.5e-15), math.log(4e-15)))
+            lines.append(f"rro{r}_{k} {y}x {y} {_fmt(rval)}")
+            lines.append(f"cra{r}_{k} {y}x 0 {_fmt(0.5 * cval)}")
+            lines.append(f"crb{r}_{k} {y} 0 {_fmt(0.5 * cval)}")
+        td = 5e-12 + 3e-12 * r
+        lines.append(f"iro{r} 0 ro{r}_0 pulse(0 200u {_fmt(td)} 2p 2p 20p 1)")
+        # the ring's output loads an inverter whose output joins the logic
+        lines.append(f"mron{r} rq{r} ro{r}_0 0 0 nch w=180n l=45n")
+        lines.append(f"mrop{r} rq{r} ro{r}_0 vdd vdd pch w=360n l=45n")
+        lines.append(f"crq{r} rq{r} 0 2f")
+    return "\n".join(lines + tail)

@@ -108,6 +108,8 @@ typedef struct {
     int *a_lupos, *cdiag, *cend, *kptr, *kpos, *kseg, *upd_dst, *upd_src, *prow, *pcol;
     int *lvl_ptr, *lvl_col, *fl_ptr, *fl_row, *bl_ptr, *bl_row;
     int *lr_ptr, *lr_col, *lr_pos, *ur_ptr, *ur_col, *ur_pos;
+    int nrl_levels, btf_blocks;   /* right-looking levels; KLU-order blocks */
+    double flops;                 /* multiply-adds of one refactorization */
 } port_plan_t;
 int port_plan(int n, const int *cp, const int *ri, const double *ax, double pivrel,
               double pivtol, port_plan_t *out);
@@ -1911,5 +1913,12 @@ done:
     stats[7] = c->npoints;
     stats[8] = c->reorders;
     stats[9] = c->ndump;
+    /* the last pivot plan of the sparse path: L+U entries, column levels,
+     * right-looking levels, KLU-order blocks, multiply-adds */
+    stats[10] = c->havePlan ? c->plan.nlu : 0;
+    stats[11] = c->havePlan ? c->plan.nlevels : 0;
+    stats[12] = c->havePlan ? c->plan.nrl_levels : 0;
+    stats[13] = c->havePlan ? c->plan.btf_blocks : 0;
+    stats[14] = c->havePlan ? (long)c->plan.flops : 0;
     return status;
 }

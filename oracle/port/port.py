@@ -460,7 +460,7 @@ class Circuit:
                 dmeta = np.zeros((dump, 4))
                 P = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
                 L.port_set_dump(h, P(dax), P(drhs), P(dro), P(dmeta), dump)
-            stats = (C.c_long * 10)()
+            stats = (C.c_long * 15)()
             L.port_run(h, stats, max_steps)
             st = list(stats)
             npts = min(st[7], outcap)
@@ -468,7 +468,9 @@ class Circuit:
                    "values": out[:npts, 1:].copy(),
                    "stats": {"numIter": st[0], "tranIter": st[1], "timePts": st[2],
                              "accepted": st[3], "rejected": st[4], "status": st[5],
-                             "opIter": st[6], "npoints": st[7], "reorders": st[8]}}
+                             "opIter": st[6], "npoints": st[7], "reorders": st[8]},
+                   "plan": {"nlu": st[10], "levels": st[11], "rl_levels": st[12],
+                            "btf_blocks": st[13], "multiply_adds": st[14]}}
             if dump:
                 k = st[9]
                 res.update(dump_ax=dax[:k], dump_rhs=drhs[:k], dump_rhsold=dro[:k],

@@ -22,6 +22,8 @@ typedef struct {
     int *a_lupos, *cdiag, *cend, *kptr, *kpos, *kseg, *upd_dst, *upd_src, *prow, *pcol;
     int *lvl_ptr, *lvl_col, *fl_ptr, *fl_row, *bl_ptr, *bl_row;
     int *lr_ptr, *lr_col, *lr_pos, *ur_ptr, *ur_col, *ur_pos;
+    int nrl_levels, btf_blocks;   /* right-looking levels; KLU-order blocks */
+    double flops;                 /* multiply-adds of one refactorization */
 } port_plan_t;
 
 static int *dup(const std::vector<int> &v)
@@ -66,6 +68,9 @@ int port_plan(int n, const int *cp, const int *ri, const double *ax, double pivr
     out->nlevels = (int)img.lvl_ptr.size() - 1;
     out->nflevels = (int)img.fl_ptr.size() - 1;
     out->nblevels = (int)img.bl_ptr.size() - 1;
+    out->nrl_levels = img.rl_ptr.empty() ? 0 : (int)img.rl_ptr.size() - 1;
+    out->btf_blocks = img.btf_blocks;
+    out->flops = img.lu_flops;
     out->a_lupos = dup(img.a_lupos);
     out->cdiag = dup(img.cdiag);
     out->cend = dup(img.cend);

@@ -77,3 +77,19 @@ def test_factor_shape_needs_a_device_circuit(built_lib):
         c.set_factor_shape(32, 1024)
     with pytest.raises(E.EngineError, match="host-only"):
         c.wide_info()
+
+
+@pytest.mark.parametrize("name,blocks", [("mc_1k_50p", 135), ("mc_2k_50p", 133),
+                                         ("mc_3k_50p", 137), ("c1_10k_30p", 138)])
+def test_block_triangular_analysis_matches_klu(built_lib, name, blocks):
+    """SMPpreOrder's analysis (ngsf_smp_preorder): the block upper
+    triangular form of the circuit pattern has as many diagonal blocks as
+    the reference's klu_analyze reports on the same netlist (driver with
+    ORACLE_KLU_STATS=1 on the compiled reference); the voltage sources give
+    the singleton blocks, the rest of the circuit one large block."""
+    from ngspice_gb300 import engine as E
+    g = golden(name)
+    c = E.Circuit(str(g["netlist"]), host_only=True)
+    nb, big = c.smp_preorder()
+    assert nb == blocks
+    assert big > c.n // 2
