@@ -74,6 +74,14 @@ TIGHT_OPTIONS = ".options klu reltol=1e-5 vntol=1e-8 abstol=1e-14"
 
 # Gear integration (.options method=gear, maxord 2): the 120-transistor
 # BSIM4 deck over 400 ps and the diode/MOS1/RC decks, every unknown.
+# Ring oscillators embedded in random logic (the C3 generator at a small
+# size): 300 logic transistors and two 7-stage rings over 300 ps, every
+# unknown, started off their metastable point by current kicks.
+RING_CASES = {
+    "rings_300": lambda: netlists.logic_with_rings(n_transistors=300, seed=3, rings=2, stages=7,
+                                                    tstop="300p"),
+}
+
 GEAR_CASES = {
     "gear_bsim4_logic_s3": lambda: netlists.random_logic(
         n_transistors=120, seed=3, n_inputs=6, tstop="400p").replace(
@@ -245,11 +253,10 @@ def main(argv: list[str]) -> int:
             np.savez_compressed(path, **out)
             print(f"bsim4_logic_s3_tight: {len(res['times'])} points, stats={res['stats'].tolist()}"
                   f" -> {os.path.getsize(path)} bytes")
-        for name, make in GEAR_CASES.items():
+        for name, make in list(GEAR_CASES.items()) + list(RING_CASES.items()):
             if only and name not in only:
                 continue
             text = make()
-            assert "method=gear" in text
             res = run_reference(text, 0, wd, keep_iters=False)
             out = {k: res[k] for k in ("names", "times", "values", "stats", "cpu_seconds")}
             out["netlist"] = np.array(text)

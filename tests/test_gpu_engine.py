@@ -94,11 +94,12 @@ def test_diode_decks_match_reference(E, name):
 GEAR_CASES = ["gear_mos1_mix", "gear_diode_rectifier", "gear_bsim4_logic_s3"]
 
 
-@pytest.mark.parametrize("name", GEAR_CASES)
-def test_gear_decks_match_reference(E, name):
-    """Gear integration (.options method=gear, maxord 2): the reference's
-    Newton and step counts, time points equal to rounding, waveforms
-    within reltol=1e-3, vntol=1 uV, abstol=1 pA."""
+@pytest.mark.parametrize("name", GEAR_CASES + ["rings_300"])
+def test_gear_and_ring_decks_match_reference(E, name):
+    """Gear integration (.options method=gear, maxord 2), and kicked ring
+    oscillators in random logic (the C3 generator at a small size): the
+    reference's Newton and step counts, time points equal to rounding,
+    waveforms within reltol=1e-3, vntol=1 uV, abstol=1 pA."""
     g = golden(name)
     c = run_one(E, str(g["netlist"]))
     r = c.results()

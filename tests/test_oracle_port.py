@@ -53,12 +53,13 @@ def test_port_diode_decks_match_reference(name):
 GEAR_CASES = ["gear_mos1_mix", "gear_diode_rectifier", "gear_bsim4_logic_s3"]
 
 
-@pytest.mark.parametrize("name", GEAR_CASES)
-def test_port_gear_decks_match_reference(name):
+@pytest.mark.parametrize("name", GEAR_CASES + ["rings_300"])
+def test_port_gear_and_ring_decks_match_reference(name):
     """Gear integration (.options method=gear, maxord 2) on the MOS1,
-    diode and 120-transistor BSIM4 decks: the reference's Newton and step
-    counts, time points equal to rounding, waveforms within the option
-    tolerances."""
+    diode and 120-transistor BSIM4 decks, and two kicked 7-stage ring
+    oscillators in 300-transistor logic (the C3 generator at a small size):
+    the reference's Newton and step counts, time points equal to rounding,
+    waveforms within the option tolerances."""
     g = golden(name)
     r = port.simulate(str(g["netlist"]))
     st, ref = r["stats"], g["stats"]
