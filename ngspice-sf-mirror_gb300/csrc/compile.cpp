@@ -292,12 +292,12 @@ void compile(Circuit &c, Image &img)
         throw NetlistError("unknown integration method");
     if (c.uic)
         throw NetlistError(".tran uic is not supported by this engine");
-    /* the engine keeps CKTstate0..3 (maxord + 2 vectors): trapezoidal
-     * orders 1-2 and Gear orders 1-2; Gear above order 2 would need up to
-     * eight */
-    if (o.maxord < 1 || o.maxord > 2)
-        throw NetlistError(o.method == 1 ? "maxord must be 1 or 2 (Gear orders 3-6 are not built)"
-                                         : "maxord must be 1 or 2 for the trapezoidal method");
+    /* DCtran raises the order only from 1 to 2 (dctran.c:820-830), so the
+     * order never exceeds 2 whatever maxord allows (cktsopt.c caps it at
+     * 6), and the states past CKTstate3 are never read: the engine keeps
+     * four state vectors and runs any maxord >= 2 as 2 */
+    if (o.maxord < 1)
+        throw NetlistError("maxord must be at least 1");
 
     /* ---------------- setup: internal nodes, branches, states -------- */
     std::vector<std::array<double, M1P_COUNT>> m1p;
@@ -704,7 +704,7 @@ void compile(Circuit &c, Image &img)
     op.temp = o.temp;
     op.itl1 = o.itl1;
     op.itl4 = o.itl4;
-    op.maxord = o.maxord;
+    op.maxord = std::min(o.maxord, 2);
     op.method = o.method;
     op.uic = 0;
     op.tstep = c.tstep;

@@ -430,7 +430,10 @@ class Circuit:
                     method = 1 if v == "gear" else 0
                 elif k in ("gear", "trap"):
                     method = 1 if k == "gear" else 0
-            iv = [int(opt("itl1", 100)), int(opt("itl4", 10)), int(opt("maxord", 2)), method]
+            # the order never exceeds 2 (DCtran raises it from 1 to 2 only), so
+            # maxord >= 2 runs as 2 on the port's four state vectors
+            iv = [int(opt("itl1", 100)), int(opt("itl4", 10)), min(int(opt("maxord", 2)), 2),
+                  method]
             L.port_set_options(h, (C.c_double * len(dv))(*dv), (C.c_int * 4)(*iv))
             for nodes, st, cval, p in self.dev[K_CAP]:
                 L.port_add_cap(h, nodes[0], nodes[1], st, cval, p.get("m", 1.0), p.get("ic", 0.0))

@@ -90,6 +90,11 @@ GEAR_CASES = {
                                                          ".options klu method=gear"),
     "gear_diode_rectifier": lambda: netlists.diode_rectifier().replace(
         ".options klu", ".options klu method=gear"),
+    # maxord 6 (the largest the reference accepts): DCtran still never
+    # raises the order past 2
+    "gear6_bsim4_logic_s3": lambda: netlists.random_logic(
+        n_transistors=120, seed=3, n_inputs=6, tstop="400p").replace(
+            ".options klu", ".options klu method=gear maxord=6"),
 }
 
 

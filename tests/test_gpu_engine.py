@@ -91,7 +91,8 @@ def test_diode_decks_match_reference(E, name):
     assert waveform_violation(c.names(), g["times"], g["values"], t, v) < 1.0
 
 
-GEAR_CASES = ["gear_mos1_mix", "gear_diode_rectifier", "gear_bsim4_logic_s3"]
+GEAR_CASES = ["gear_mos1_mix", "gear_diode_rectifier", "gear_bsim4_logic_s3",
+              "gear6_bsim4_logic_s3"]
 
 
 @pytest.mark.parametrize("name", GEAR_CASES + ["rings_300"])

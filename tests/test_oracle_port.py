@@ -50,7 +50,8 @@ def test_port_diode_decks_match_reference(name):
                               r["values"][:, idx]) < 0.1
 
 
-GEAR_CASES = ["gear_mos1_mix", "gear_diode_rectifier", "gear_bsim4_logic_s3"]
+GEAR_CASES = ["gear_mos1_mix", "gear_diode_rectifier", "gear_bsim4_logic_s3",
+              "gear6_bsim4_logic_s3"]
 
 
 @pytest.mark.parametrize("name", GEAR_CASES + ["rings_300"])
