@@ -62,6 +62,9 @@ CASES = {
 #                (4,714 transistors, seed 101314), first 150 ps: its L
 #                entries grow past 1e6 in the transient, so it is the
 #                batch's most rounding-sensitive refactorization
+#   mc_c4_3893   instance 3893 (3,547 transistors, seed 103893), first
+#                200 ps: on the engine's pivots its second transient step's
+#                Newton iterations fail until the retry takes new pivots
 NPROBE = 256
 
 # A tight-tolerance reference (reltol 1e-5, vntol 1e-8 V, abstol 1e-14 A)
@@ -112,6 +115,8 @@ LARGE_CASES = {
     "mc_3k_50p": lambda: netlists.random_logic(n_transistors=3000, seed=103, tstop="50p",
                                                mismatch=True),
     "mc_c4_1314": lambda: netlists.random_logic(n_transistors=4714, seed=101314, tstop="150p",
+                                                mismatch=True),
+    "mc_c4_3893": lambda: netlists.random_logic(n_transistors=3547, seed=103893, tstop="200p",
                                                 mismatch=True),
 }
 

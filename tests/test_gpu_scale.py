@@ -93,3 +93,27 @@ def test_klu_order_plan_matches_reference_transient(E, monkeypatch):
     w = waveform_violation(list(g["names"]), g["times"], g["values"], t, v)
     print(f"mc_1k_50p in KLU order: worst waveform error {w:.2e} of the tolerance")
     assert w < 1.0
+
+
+def test_newton_failure_retry_takes_new_pivots(E, monkeypatch):
+    """Instance 3893 of the 4096-instance workload in one block: on the
+    engine's pivot plan its second transient step fails Newton (the
+    reference's KLU order converges there), and with the reference's
+    behaviour (NGSF_RETRY_REPIVOT=0) the run ends in "timestep too small".
+    By default the retry factors with pivots chosen on its own matrix: the
+    run completes, one step more rejected than the reference's and the
+    accepted steps within 2 % of its count, every reference waveform point
+    within the tolerance."""
+    monkeypatch.setenv("NGSF_WIDE", "0")
+    g = golden("mc_c4_3893")
+    c = E.Circuit(str(g["netlist"]), probes=[str(x) for x in g["names"]], outcap=4096)
+    E.run([c])
+    r = c.results()
+    ref = g["stats"]
+    assert r[E.R_STATUS] == 0
+    assert r[E.R_REJECTED] <= ref[4] + 2
+    assert abs(int(r[E.R_ACCEPTED]) - int(ref[3])) <= 0.02 * ref[3]
+    t, v = c.points()
+    w = waveform_violation(list(g["names"]), g["times"], g["values"], t, v)
+    print(f"mc_c4_3893: worst waveform error {w:.2e} of the tolerance")
+    assert w < 1.0
