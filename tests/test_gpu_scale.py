@@ -75,26 +75,6 @@ def test_rounding_sensitive_instance_in_one_block(E, monkeypatch):
     check(E, g, c, "mc_c4_1314 (one block)")
 
 
-def test_klu_order_plan_matches_reference_transient(E, monkeypatch):
-    """The planner in KLU's block triangular order (NGSF_ORDER=klu: BTF
-    blocks, a minimum degree order within each, KLU's diagonal-preferring
-    threshold pivots on max-scaled rows) on the 1,000-transistor instance:
-    the reference's transient Newton and step counts and its waveforms
-    within the tolerance (the operating point's re-pivots may differ)."""
-    monkeypatch.setenv("NGSF_ORDER", "klu")
-    g = golden("mc_1k_50p")
-    c = E.Circuit(str(g["netlist"]), probes=[str(x) for x in g["names"]], outcap=4096)
-    E.run([c])
-    r = c.results()
-    ref = g["stats"]
-    assert r[E.R_STATUS] == 0
-    assert (r[E.R_TRANITER], r[E.R_ACCEPTED], r[E.R_REJECTED]) == (ref[1], ref[3], ref[4])
-    t, v = c.points()
-    w = waveform_violation(list(g["names"]), g["times"], g["values"], t, v)
-    print(f"mc_1k_50p in KLU order: worst waveform error {w:.2e} of the tolerance")
-    assert w < 1.0
-
-
 def test_newton_failure_retry_takes_new_pivots(E, monkeypatch):
     """Instance 3893 of the 4096-instance workload in one block: on the
     engine's pivot plan its second transient step fails Newton (the
