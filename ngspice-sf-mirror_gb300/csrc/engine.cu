@@ -1378,11 +1378,30 @@ __device__ int lu_factor(const ngsf_ckt_t &C, Ctl &s)
  * memory when they fit the launch's allocation, else C.work. */
 __shared__ double *g_sw;
 
+/* Row completion tags of the dependency-driven solve (n ints after the
+ * solve vector in dynamic shared memory, or null), and the tag of the
+ * sweep in progress: a row is done in this sweep when its tag equals it. */
+__shared__ int *g_sflag;
+__shared__ int g_stag;
+
+__device__ __forceinline__ size_t solve_vec_bytes(int n)
+{
+    return ((size_t)(n + 1) * sizeof(double) + 127) & ~(size_t)127;
+}
+
 __device__ void solve_buffers_init(const ngsf_ckt_t &C, unsigned char *dyn, int dynBytes)
 {
-    if (threadIdx.x == 0)
-        g_sw = (dyn && (size_t)(C.n + 1) * sizeof(double) <= (size_t)dynBytes) ? (double *)dyn
-                                                                               : nullptr;
+    const bool vec = dyn && solve_vec_bytes(C.n) <= (size_t)dynBytes;
+    const bool flags = vec && solve_vec_bytes(C.n) + (size_t)C.n * sizeof(int) <= (size_t)dynBytes;
+    if (threadIdx.x == 0) {
+        g_sw = vec ? (double *)dyn : nullptr;
+        g_sflag = flags ? (int *)(dyn + solve_vec_bytes(C.n)) : nullptr;
+        g_stag = 0;
+    }
+    __syncthreads();
+    if (flags)
+        for (int i = threadIdx.x; i < C.n; i += blockDim.x)
+            g_sflag[i] = 0;
     __syncthreads();
 }
 
@@ -1532,20 +1551,124 @@ __device__ __forceinline__ void solve_sweep(const ngsf_ckt_t &C, double *w, int 
     }
 }
 
-/* SMPsolve: x = A^-1 b, in place on rhs (row-oriented, level scheduled). */
-__device__ void lu_solve(const ngsf_ckt_t &C, Ctl &s, double *rhs)
+/* Dependency-driven sweep: the same rows, terms and arithmetic as
+ * solve_sweep (so the same bits), without the barriers between levels.
+ * Warp 0 takes the long rows (more than 32 terms) in level order, the other
+ * warps' threads the short rows, thread by thread in level order; a row
+ * waits for the rows its terms read (their tags in shared memory, acquire)
+ * and publishes its own (release).  Every worker takes its rows in level
+ * order and rows of one level do not read one another, so the earliest
+ * unfinished row can always proceed.  A wait is bounded: one that runs out
+ * (NGSF_SF_SPIN polls) flags the block and the sweep goes on without it. */
+#define NGSF_SF_SPIN (1 << 22)
+/* set when a wait of the sweep ran out: every later wait then returns at
+ * once, so one stall bounds the whole sweep */
+__shared__ int g_sf_abort;
+
+__device__ __forceinline__ bool sf_wait(int *flags, int c, int tag)
+{
+    cuda::atomic_ref<int, cuda::thread_scope_block> f(flags[c]);
+    for (int i = 0; i < NGSF_SF_SPIN; i++) {
+        if (f.load(cuda::memory_order_acquire) == tag)
+            return true;
+        if (*(volatile int *)&g_sf_abort)
+            return false;
+        if (i >= 32)
+            __nanosleep(32);   /* leave the issue slots to the rows it waits for */
+    }
+    *(volatile int *)&g_sf_abort = 1;
+    return false;
+}
+
+__device__ __forceinline__ void sf_publish(int *flags, int row, int tag)
+{
+    cuda::atomic_ref<int, cuda::thread_scope_block> f(flags[row]);
+    f.store(tag, cuda::memory_order_release);
+}
+
+__device__ int solve_sweep_sf(const ngsf_ckt_t &C, double *w, int *flags, int tag, int nlev,
+                              const int *lptr, const int4 *desc, const double *val,
+                              const int *col, const int *rptr, const int *hptr,
+                              const int *hrow, bool back)
+{
+    const int t = threadIdx.x, T = blockDim.x;
+    const int warp = t >> 5, lane = t & 31;
+    int late = 0;
+    if (warp == 0) {
+        for (int h = hptr[0]; h < hptr[nlev]; h++) {
+            const int k = hrow[h];
+            const int q0 = rptr[k], q1 = rptr[k + 1];
+            double acc = 0.0;
+            for (int q = q0 + lane; q < q1; q += 32) {
+                const int c = col[q];
+                const double v = val[q];
+                if (!sf_wait(flags, c, tag))
+                    late = 1;
+                acc = fma(v, w[c], acc);
+            }
+            for (int o = 16; o > 0; o >>= 1)
+                acc += __shfl_xor_sync(0xffffffffu, acc, o);
+            if (lane == 0) {
+                w[k] = back ? (w[k] - acc) * C.uinv[k] : w[k] - acc;
+                sf_publish(flags, k, tag);
+            }
+            __syncwarp();
+        }
+    } else {
+        for (int r = lptr[0] + t - 32; r < lptr[nlev]; r += T - 32) {
+            const int4 d = desc[r];
+            if (d.z - d.y > 32)
+                continue;
+            double acc = w[d.x];
+            for (int q = d.y; q < d.z; q++) {
+                const int c = col[q];
+                const double v = val[q];
+                if (!sf_wait(flags, c, tag))
+                    late = 1;
+                acc = fma(-v, w[c], acc);
+            }
+            w[d.x] = back ? acc * C.uinv[d.x] : acc;
+            sf_publish(flags, d.x, tag);
+        }
+    }
+    __syncthreads();
+    return late;
+}
+
+/* SMPsolve: x = A^-1 b, in place on rhs (row-oriented; dependency driven
+ * when the block has room for the row tags and C.solve_sf is set, else
+ * level by level).  Returns nonzero when a bounded wait ran out. */
+__device__ int lu_solve(const ngsf_ckt_t &C, Ctl &s, double *rhs)
 {
     double *w = g_sw ? g_sw : C.work;
     for (int k = threadIdx.x; k < C.n; k += blockDim.x)
         w[k] = rhs[C.prow[k]];
     __syncthreads();
-    solve_sweep(C, w, C.nflevels, C.fl_ptr, (const int4 *)C.fdesc, C.lval, C.lr_col, C.lr_ptr,
-                C.fh_ptr, C.fh_row, false);
-    solve_sweep(C, w, C.nblevels, C.bl_ptr, (const int4 *)C.bdesc, C.uval, C.ur_col, C.ur_ptr,
-                C.bh_ptr, C.bh_row, true);
+    int late = 0;
+    if (g_sflag && C.solve_sf && blockDim.x > 32) {
+        __shared__ int tag;
+        if (threadIdx.x == 0) {
+            tag = (g_stag += 2);
+            g_sf_abort = 0;
+        }
+        __syncthreads();
+        const int tg = tag;
+        late |= solve_sweep_sf(C, w, g_sflag, tg - 1, C.nflevels, C.fl_ptr,
+                               (const int4 *)C.fdesc, C.lval, C.lr_col, C.lr_ptr, C.fh_ptr,
+                               C.fh_row, false);
+        late |= solve_sweep_sf(C, w, g_sflag, tg, C.nblevels, C.bl_ptr, (const int4 *)C.bdesc,
+                               C.uval, C.ur_col, C.ur_ptr, C.bh_ptr, C.bh_row, true);
+        late = block_or(s, late);
+    } else {
+        solve_sweep(C, w, C.nflevels, C.fl_ptr, (const int4 *)C.fdesc, C.lval, C.lr_col,
+                    C.lr_ptr, C.fh_ptr, C.fh_row, false);
+        solve_sweep(C, w, C.nblevels, C.bl_ptr, (const int4 *)C.bdesc, C.uval, C.ur_col,
+                    C.ur_ptr, C.bh_ptr, C.bh_row, true);
+    }
     for (int k = threadIdx.x; k < C.n; k += blockDim.x)
         rhs[C.pcol[k]] = w[k];
     __syncthreads();
+    return late;
 }
 
 /* NIconvTest (src/maths/ni/niconv.c:21-90).
@@ -1880,7 +2003,13 @@ __device__ int ni_iter(const ngsf_ckt_t &C, Ctl &s, int maxIter, bool resume)
         }
         resume = false;
         tp = prof_t(C);
-        lu_solve(C, s, it.rhs);
+        if (lu_solve(C, s, it.rhs)) {
+            /* a solve wait ran out: stop with the step-budget status */
+            if (threadIdx.x == 0)
+                s.numIter += iterno;
+            __syncthreads();
+            return NGSF_E_WATCHDOG;
+        }
         if (threadIdx.x == 0) {
             it.rhs[0] = 0;
             it.rhsOld[0] = 0;
@@ -2838,6 +2967,7 @@ __global__ void __launch_bounds__(NGSF_THREADS) stamp_static_kernel(ngsf_ckt_t C
     __syncthreads();
     if (threadIdx.x == 0) {      /* RUN_PROBE stamps only: no solve buffers */
         g_sw = nullptr;
+        g_sflag = nullptr;
         g_psm = nullptr;
     }
     run_circuit(Cs, s, RUN_PROBE, 0);
@@ -2956,7 +3086,7 @@ op_kernel(const ngsf_ckt_t *ckt, OpArgs a, int solveCap, int *iout, double *dout
         r = lu_factor(Cs, s);
         break;
     case OPK_SOLVE:
-        lu_solve(Cs, s, it.rhs);
+        r = lu_solve(Cs, s, it.rhs);
         break;
     case OPK_CONV:
         r = conv_test(Cs, s, it);
@@ -3179,9 +3309,12 @@ extern "C" NGSF_API int ngsf_stamp_initial_static(const ngsf_handle *h, double *
  * NGSF_SOLVE_SMEM_MAX (the solve then works in global memory). */
 extern "C" int ngsf_solve_smem_bytes(int n)
 {
-    size_t b = (size_t)(n + 1) * sizeof(double);
-    b = (b + 127) & ~(size_t)127;
-    return b <= (size_t)NGSF_SOLVE_SMEM_MAX ? (int)b : 0;
+    /* the solve vector, then the row tags of the dependency-driven solve */
+    size_t v = ((size_t)(n + 1) * sizeof(double) + 127) & ~(size_t)127;
+    size_t b = (v + (size_t)n * sizeof(int) + 127) & ~(size_t)127;
+    if (b <= (size_t)NGSF_SOLVE_SMEM_MAX)
+        return (int)b;
+    return v <= (size_t)NGSF_SOLVE_SMEM_MAX ? (int)v : 0;
 }
 
 /* staging of the predictor's network tiles (0 when no circuit has one) */
@@ -3514,8 +3647,13 @@ extern "C" NGSF_API int ngsf_smp_solve(ngsf_handle *h, double *rhs)
     const size_t b = ((size_t)d->n + 1) * sizeof(double);
     if (put(d->rhs, rhs, b, who))
         return -1;
-    if (launch_op(h, op_args(OPK_SOLVE, nullptr, 0), nullptr, nullptr, who))
+    int late = 0;
+    if (launch_op(h, op_args(OPK_SOLVE, nullptr, 0), &late, nullptr, who))
         return -1;
+    if (late) {
+        ngsf_internal_set_error("ngsf_smp_solve: a bounded wait of the solve ran out");
+        return -1;
+    }
     if (get(rhs, d->rhs, b, who))
         return -1;
     rhs[0] = 0.0;

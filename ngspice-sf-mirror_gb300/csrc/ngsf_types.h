@@ -339,6 +339,9 @@ typedef struct {
      * and, when tran_growth > 0, an L entry past it asks for new pivots */
     double tran_growth;
     int retry_repivot;
+    /* triangular solves driven by row dependencies instead of level
+     * barriers (same bits); 0 (default): level by level */
+    int solve_sf;
 } ngsf_ckt_t;
 
 /* phases of the per-phase clock record */

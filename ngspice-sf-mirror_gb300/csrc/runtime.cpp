@@ -304,6 +304,13 @@ void DeviceCircuit::upload(const Image &img, const std::vector<int> &probes, int
     h.tran_growth = 0.0;
     if (const char *g = getenv("NGSF_TRAN_GROWTH"))
         h.tran_growth = atof(g);
+    /* triangular solves level by level; NGSF_SOLVE=sf: dependency driven
+     * (the same bits, measured slower: every row waits term by term on
+     * the rows it reads, where a level's rows are fetched ahead of the
+     * barrier) */
+    h.solve_sf = 0;
+    if (const char *sv = getenv("NGSF_SOLVE"))
+        h.solve_sf = std::string(sv) == "sf";
     if (!impl->d_desc)
         ck(cudaMalloc(&impl->d_desc, sizeof(ngsf_ckt_t)), "cudaMalloc(desc)");
     ck(cudaMemcpy(impl->d_desc, &h, sizeof(h), cudaMemcpyHostToDevice), "cudaMemcpy(desc)");
