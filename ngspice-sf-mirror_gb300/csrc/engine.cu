@@ -3307,12 +3307,13 @@ extern "C" NGSF_API int ngsf_stamp_initial_static(const ngsf_handle *h, double *
 /* Dynamic shared memory for the solve workspace of circuits with n
  * unknowns: (n+1) doubles rounded to 128 bytes, or 0 when that exceeds
  * NGSF_SOLVE_SMEM_MAX (the solve then works in global memory). */
-extern "C" int ngsf_solve_smem_bytes(int n)
+extern "C" int ngsf_solve_smem_bytes(int n, int tags)
 {
-    /* the solve vector, then the row tags of the dependency-driven solve */
+    /* the solve vector, then (dependency-driven solves only) the row tags;
+     * no more than that, since the reservation shrinks the L1 cache */
     size_t v = ((size_t)(n + 1) * sizeof(double) + 127) & ~(size_t)127;
     size_t b = (v + (size_t)n * sizeof(int) + 127) & ~(size_t)127;
-    if (b <= (size_t)NGSF_SOLVE_SMEM_MAX)
+    if (tags && b <= (size_t)NGSF_SOLVE_SMEM_MAX)
         return (int)b;
     return v <= (size_t)NGSF_SOLVE_SMEM_MAX ? (int)v : 0;
 }
@@ -3448,7 +3449,7 @@ int launch_op(const ngsf_handle *h, const OpArgs &a, int *r, double *dv, const c
     cudaError_t e = cudaMalloc(&d_i, 16);
     if (e == cudaSuccess)
         e = allow_dyn_smem((const void *)op_kernel);
-    const int solveCap = ngsf_solve_smem_bytes(hd->n);
+    const int solveCap = ngsf_solve_smem_bytes(hd->n, hd->solve_sf);
     if (e == cudaSuccess) {
         op_kernel<<<1, NGSF_THREADS, (size_t)solveCap>>>(dd, a, solveCap, d_i,
                                                           (double *)(d_i + 2));

@@ -36,7 +36,7 @@
 #include "sparse.h"
 
 extern "C" int ngsf_wide_blocks(void);
-extern "C" int ngsf_solve_smem_bytes(int n);
+extern "C" int ngsf_solve_smem_bytes(int n, int tags);
 extern "C" int ngsf_pred_smem_bytes(int any);
 extern "C" cudaError_t ngsf_launch_tran_wide(const ngsf_ckt_t *d_ckt, int nblocks, int runMode,
                                              long long maxSteps, int solveCap, int gnnBytes,
@@ -849,7 +849,7 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
                 throw std::runtime_error("too many re-pivot rounds");
             std::vector<ngsf_ckt_t> descs;
             std::vector<Prepared *> wide;
-            int maxn = 0, learned = 0;
+            int maxn = 0, learned = 0, tags = 0;
             for (auto *c : pending) {
                 if (c->wide && allowWide) {
                     wide.push_back(c);
@@ -857,6 +857,7 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
                     descs.push_back(c->dev->desc());
                     maxn = std::max(maxn, c->img.n);
                     learned |= c->dev->desc().pred.kind == 2;
+                    tags |= c->dev->desc().solve_sf;
                 }
             }
             if (!descs.empty()) {
@@ -874,7 +875,7 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
                 });
                 ck(cudaMemcpy(d_order, order.data(), order.size() * sizeof(int),
                               cudaMemcpyHostToDevice), "cudaMemcpy(order)");
-                const int solveCap = ngsf_solve_smem_bytes(maxn);
+                const int solveCap = ngsf_solve_smem_bytes(maxn, tags);
                 const int gnnBytes = ngsf_pred_smem_bytes(learned);
                 /* one 256-thread block per circuit (measured faster than
                  * two 128-thread or four 64-thread circuits sharing an SM:
@@ -909,7 +910,7 @@ int run_batch(const std::vector<Prepared *> &cs, long long maxSteps, double *sec
                 int nb = c->wide_blocks;
                 cudaEventRecord(e0, 0);
                 ck(ngsf_launch_tran_wide(c->dev->device_desc(), nb, mode, maxSteps,
-                                        ngsf_solve_smem_bytes(c->img.n),
+                                        ngsf_solve_smem_bytes(c->img.n, c->dev->desc().solve_sf),
                                         ngsf_pred_smem_bytes(c->dev->desc().pred.kind == 2), 0),
                    "launch(tran wide)");
                 cudaEventRecord(e1, 0);
