@@ -342,6 +342,22 @@ def seconds_of(t: str) -> float:
     return float(t)
 
 
+def replica_totals(seconds: float, accepted: float, world: int, device: str) -> tuple:
+    """Whole-job figures of N replicas (one per rank, the same workload
+    each): the slowest rank's device time and the accepted steps of all
+    ranks (an all-reduce over the process group; a single process returns
+    its own)."""
+    if world <= 1:
+        return seconds, accepted
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    a = torch.tensor([float(accepted)], dtype=torch.float64, device=device)
+    dist.all_reduce(a, op=dist.ReduceOp.SUM)
+    return float(t.item()), float(a.item())
+
+
 def engine_arm(args, texts, wdesc, rank, world) -> dict | None:
     from ngspice_gb300 import engine as E
     mc = args.workload in ("c2", "c4")
@@ -415,16 +431,7 @@ def engine_arm(args, texts, wdesc, rank, world) -> dict | None:
     iters = sum(iters_of)
     moved = sum(bytes_per_iteration(w) * k for w, k in zip(wls, iters_of))
     total = sum(dev_times)
-    if world > 1:
-        import torch
-        import torch.distributed as dist
-        t = torch.tensor([total], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        a = torch.tensor([accepted], dtype=torch.float64, device="cuda")
-        dist.all_reduce(a, op=dist.ReduceOp.SUM)
-        total, accepted_all = float(t.item()), float(a.item())
-    else:
-        accepted_all = accepted
+    total, accepted_all = replica_totals(total, accepted, world, "cuda")
     value = accepted_all / total
     lu_madds = [c.lu_flops() for c in circuits]
     # free the timed batch (device memory and host images) before the
