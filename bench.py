@@ -601,14 +601,14 @@ def engine_arm(args, texts, wdesc, rank, world) -> dict | None:
         else "tran_kernel"
     # DRAM bytes per circuit Newton iteration measured with ncu
     # (dram__bytes_read + dram__bytes_write of one launch over the Newton
-    # iterations it ran): the C1 time-loop launch of the first 3 ps, 538 MB
+    # iterations it ran): the C1 time-loop launch of the first 3 ps, 66.3 MB
     # over about 120 iterations (the working set stays in L2); a timed
     # window of the first 76 C2 instances, 76.65 GB over 8,637 circuit
     # iterations, 2.21x their 4,014,764 algorithmic bytes per iteration
     # (76 circuit arenas do not fit L2 together).  A Monte Carlo batch
     # scales that ratio by its own algorithmic bytes per iteration.
     per_iter = moved / max(iters, 1)
-    traffic = {"c1": 538.4e6 / 120,
+    traffic = {"c1": 66.3e6 / 120,
                "c2": per_iter * (76.652e9 / 8637) / 4014764,
                "c4": per_iter * (76.652e9 / 8637) / 4014764}.get(args.workload)
     roof = {"bound": "hbm", "achieved": achieved, "peak": pk["hbm_gbs"], "unit": "GB/s",
