@@ -93,3 +93,21 @@ def test_block_triangular_analysis_matches_klu(built_lib, name, blocks):
     nb, big = c.smp_preorder()
     assert nb == blocks
     assert big > c.n // 2
+
+
+def test_block_triangular_analysis_of_small_decks(built_lib):
+    """The analysis on decks whose zero-free diagonal needs augmenting
+    paths (voltage-source branches have no diagonal entry): every source's
+    node and branch become singleton blocks, the resistive network between
+    them one block."""
+    from ngspice_gb300 import engine as E
+    deck = ("t\nv1 a 0 1\nv2 b a 2\nr1 b c 1k\nr2 c 0 1k\nr3 c d 1k\nc1 d 0 1p\n"
+            ".tran 1n 10n\n.end\n")
+    c = E.Circuit(deck, host_only=True)
+    nb, big = c.smp_preorder()
+    # unknowns a, b, c, d, v1#branch, v2#branch: the sources' nodes and
+    # branches are singletons, c and d one block
+    assert c.n == 6
+    assert (nb, big) == (5, 2)
+    rc = E.Circuit("t\nv1 a 0 1\nr1 a b 1k\nr2 b 0 1k\n.tran 1n 10n\n.end\n", host_only=True)
+    assert rc.smp_preorder() == (3, 1)
