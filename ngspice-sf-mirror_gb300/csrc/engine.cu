@@ -44,6 +44,21 @@
 /* largest dynamic shared memory a launch asks for (solve buffers) */
 #define NGSF_SOLVE_SMEM_MAX (160 * 1024)
 
+/* This file is compiled in parts, three translation units built in
+ * parallel (ptxas takes about a minute on each transient kernel):
+ * NGSF_PART 1 the batched transient kernel and its host launchers, 2 the
+ * wide (whole-grid) launch, 3 the operator surface, the allocation-free
+ * stamps and the probes; without NGSF_PART (0) everything at once.  The
+ * device functions are shared by all parts; each part compiles the
+ * kernels it defines. */
+#ifndef NGSF_PART
+#define NGSF_PART 0
+#endif
+#define NGSF_IN(p) (NGSF_PART == 0 || NGSF_PART == (p))
+/* defined in part 1, used by every part */
+extern "C" int ngsf_solve_smem_bytes(int n, int tags);
+extern "C" int ngsf_pred_smem_bytes(int any);
+
 namespace {
 
 struct Ctl {
@@ -2777,6 +2792,7 @@ __device__ void run_circuit(const ngsf_ckt_t &C, Ctl &s, int runMode, long long 
 #define NGSF_TRAN_MAXNREG 255
 #endif
 #define NGSF_TRAN_BOUNDS __maxnreg__(NGSF_TRAN_MAXNREG)
+#if NGSF_IN(1)
 __global__ void NGSF_TRAN_BOUNDS
 tran_kernel(const ngsf_ckt_t *ckts, const int *order, int nckt, int runMode,
             long long maxSteps, int solveCap, int gnnBytes)
@@ -2803,6 +2819,8 @@ tran_kernel(const ngsf_ckt_t *ckts, const int *order, int nckt, int runMode,
     pred_block_fini();
 }
 
+#endif  /* NGSF_IN(1) */
+#if NGSF_IN(2)
 /* One circuit over the whole (cooperative) grid: block 0 runs the
  * transient, the other blocks evaluate transistors on its command. */
 __global__ void NGSF_TRAN_BOUNDS
@@ -2833,6 +2851,7 @@ tran_wide_kernel(const ngsf_ckt_t *ckt, int runMode, long long maxSteps, int sol
         wide_issue(Cs, s, NGSF_WIDE_EXIT);
 }
 
+#endif  /* NGSF_IN(2) */
 __device__ void run_circuit(const ngsf_ckt_t &C, Ctl &s, int runMode, long long maxSteps)
 {
     const bool hold = (runMode & RUN_HOLD) != 0;
@@ -2945,6 +2964,7 @@ __device__ void run_circuit(const ngsf_ckt_t &C, Ctl &s, int runMode, long long 
 
 }  // namespace
 
+#if NGSF_IN(3)
 /* ---------------------------------------------------------------- */
 /* First-iteration stamps without allocation                          */
 /* ---------------------------------------------------------------- */
@@ -3169,8 +3189,10 @@ __global__ void fp64_peak_kernel(double *out, int iters)
         out[blockIdx.x] = r;
 }
 
+#endif  /* NGSF_IN(3) */
 static_assert(sizeof(Ctl) <= NGSF_WIDE_CTL_BYTES, "control block does not fit the wide hand-over");
 
+#if NGSF_IN(1)
 extern "C" int ngsf_ctl_bytes(void) { return (int)sizeof(Ctl); }
 
 /* The caller's answer to a sharedsync stop, written into the paused run's
@@ -3186,6 +3208,8 @@ extern "C" cudaError_t ngsf_sync_write(void *ctlsave, double delta, int reply)
     return e;
 }
 
+#endif  /* NGSF_IN(1) */
+#if NGSF_IN(2)
 namespace {
 cudaError_t allow_dyn_smem(const void *fn);
 }
@@ -3208,9 +3232,11 @@ extern "C" int ngsf_wide_blocks(void)
     return sms * per;
 }
 
+#endif  /* NGSF_IN(2) */
 extern "C" const ngsf_ckt_t *ngsf_internal_desc(const ngsf_handle *h);
 extern "C" void ngsf_internal_set_error(const char *msg);
 
+#if NGSF_IN(3)
 namespace {
 
 /* Device address of g_static_scratch on the current device, looked up on
@@ -3307,6 +3333,8 @@ extern "C" NGSF_API int ngsf_stamp_initial_static(const ngsf_handle *h, double *
 /* Dynamic shared memory for the solve workspace of circuits with n
  * unknowns: (n+1) doubles rounded to 128 bytes, or 0 when that exceeds
  * NGSF_SOLVE_SMEM_MAX (the solve then works in global memory). */
+#endif  /* NGSF_IN(3) */
+#if NGSF_IN(1)
 extern "C" int ngsf_solve_smem_bytes(int n, int tags)
 {
     /* the solve vector, then (dependency-driven solves only) the row tags;
@@ -3321,6 +3349,8 @@ extern "C" int ngsf_solve_smem_bytes(int n, int tags)
 /* staging of the predictor's network tiles (0 when no circuit has one) */
 extern "C" int ngsf_pred_smem_bytes(int any) { return any ? PRED_STAGE_BYTES : 0; }
 
+#endif  /* NGSF_IN(1) */
+#if NGSF_IN(2) || NGSF_IN(3)
 namespace {
 cudaError_t allow_dyn_smem(const void *fn)
 {
@@ -3346,6 +3376,8 @@ cudaError_t allow_dyn_smem(const void *fn)
 }
 }  // namespace
 
+#endif  /* NGSF_IN(2) || NGSF_IN(3) */
+#if NGSF_IN(2)
 extern "C" cudaError_t ngsf_launch_tran_wide(const ngsf_ckt_t *d_ckt, int nblocks, int runMode,
                                              long long maxSteps, int solveCap, int gnnBytes,
                                              cudaStream_t stream)
@@ -3360,6 +3392,8 @@ extern "C" cudaError_t ngsf_launch_tran_wide(const ngsf_ckt_t *d_ckt, int nblock
                                        (size_t)solveCap + (size_t)gnnBytes, stream);
 }
 
+#endif  /* NGSF_IN(2) */
+#if NGSF_IN(1)
 /* circuit blocks of the batched launch one SM holds at once; *regs and
  * *smem (may be NULL) receive the kernel's registers per thread and static
  * shared bytes */
@@ -3408,6 +3442,8 @@ extern "C" cudaError_t ngsf_launch_tran(const ngsf_ckt_t *d_ckts, const int *d_o
     return cudaGetLastError();
 }
 
+#endif  /* NGSF_IN(1) */
+#if NGSF_IN(3)
 /* ---------------------------------------------------------------- */
 /* Operator surface, host side (declared in ngspice_gb300.h)          */
 /* ---------------------------------------------------------------- */
@@ -3754,4 +3790,4 @@ extern "C" NGSF_API int ngsf_fp64_peak(double *flops_per_second)
         *flops_per_second = 2.0 * 8.0 * (double)iters * blocks * threads / (best * 1e-3);
     return 0;
 }
-
+#endif  /* NGSF_IN(3) */

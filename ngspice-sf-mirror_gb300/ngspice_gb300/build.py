@@ -36,18 +36,36 @@ def nvcc() -> str:
     raise RuntimeError("nvcc not found")
 
 
-def sources() -> list[str]:
-    return sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC)
-                  if f.endswith((".cu", ".cpp")))
+# engine.cu is compiled in three parts (NGSF_PART 1-3: the batched
+# transient kernel, the wide launch, the operator surface and probes), in
+# parallel with the other translation units: ptxas spends about a minute on
+# each transient kernel
+ENGINE_PARTS = 3
 
 
-def _compile(src: str) -> str:
-    obj = os.path.join(BUILD, os.path.basename(src) + ".o")
+def sources() -> list[tuple[str, int]]:
+    out = []
+    for f in sorted(os.listdir(CSRC)):
+        if not f.endswith((".cu", ".cpp")):
+            continue
+        path = os.path.join(CSRC, f)
+        if f == "engine.cu":
+            out += [(path, k) for k in range(1, ENGINE_PARTS + 1)]
+        else:
+            out.append((path, 0))
+    return out
+
+
+def _compile(item: tuple[str, int]) -> str:
+    src, part = item
+    obj = os.path.join(BUILD, os.path.basename(src) + (f".{part}" if part else "") + ".o")
     deps = [src] + [os.path.join(CSRC, h) for h in os.listdir(CSRC) if h.endswith((".h", ".cuh", ".def"))]
     deps += [os.path.join(INCLUDE, h) for h in os.listdir(INCLUDE) if h.endswith((".h", ".cuh", ".def"))]
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(d) for d in deps):
         return obj
     cmd = [nvcc()] + ARCH + COMMON + ["-c", src, "-o", obj]
+    if part:
+        cmd.append(f"-DNGSF_PART={part}")
     if src.endswith(".cu") and os.environ.get("NGSF_TRAN_MAXNREG"):
         cmd.append(f"-DNGSF_TRAN_MAXNREG={int(os.environ['NGSF_TRAN_MAXNREG'])}")
     if src.endswith(".cu"):
