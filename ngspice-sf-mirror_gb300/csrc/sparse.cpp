@@ -16,6 +16,7 @@
  */
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstdlib>
 #include <array>
 #include <map>
@@ -707,6 +708,9 @@ bool plan_lu(int n, const std::vector<int> &cp, const std::vector<int> &ri,
          * position, each group in generation order (a stable counting
          * sort; cnt and start are indexed by LU position) */
         std::vector<int> cnt(img.nlu, 0), start(img.nlu, 0), touched;
+        /* destinations touched in the level, one bit per LU position:
+         * enumerating the set bits gives them in ascending order */
+        std::vector<uint64_t> mark((size_t)img.nlu / 64 + 1, 0);
         std::vector<int> colrow(img.nlu);   /* row of each LU position */
         for (int j = 0; j < n; j++) {
             for (size_t t = 0; t < ucol[j].size(); t++)
@@ -730,10 +734,16 @@ bool plan_lu(int n, const std::vector<int> &cp, const std::vector<int> &ri,
                  * by position); within a destination the products keep
                  * the pivot order, whatever the walk order */
                 const std::vector<int> &lk = lcol[k];
+                if (lk.empty())
+                    continue;
                 for (auto &e : urow[k]) {
                     const int j = e.first, upos = e.second;
-                    int q = img.cbeg[j];
                     const int qe = img.cend[j];
+                    /* column j's rows ascend with the position: start the
+                     * walk at the first row not below L column k's first */
+                    int q = (int)(std::lower_bound(colrow.begin() + img.cbeg[j],
+                                                   colrow.begin() + qe, lk[0]) -
+                                  colrow.begin());
                     for (size_t s2 = 0; s2 < lk.size(); s2++) {
                         const int i = lk[s2];
                         while (q < qe && colrow[q] < i)
@@ -743,20 +753,32 @@ bool plan_lu(int n, const std::vector<int> &cp, const std::vector<int> &ri,
                             return false;
                         }
                         const int d = q;
-                        if (cnt[d]++ == 0)
+                        if (cnt[d]++ == 0) {
                             touched.push_back(d);
+                            mark[(size_t)d >> 6] |= 1ull << (d & 63);
+                        }
                         prod.push_back({d, img.cdiag[k] + 1 + (int)s2, upos, img.cdiag[k]});
                     }
                 }
             }
-            if (touched.size() * 16 > (size_t)img.nlu) {
-                /* a dense level: scanning the counts is cheaper than a sort */
+            if (!touched.empty()) {
+                /* ascending destinations from the bit marks (cleared on the
+                 * way), between the smallest and largest touched word */
+                size_t w0 = (size_t)-1, w1 = 0;
+                for (int d : touched) {
+                    w0 = std::min(w0, (size_t)d >> 6);
+                    w1 = std::max(w1, (size_t)d >> 6);
+                }
                 touched.clear();
-                for (int d = 0; d < img.nlu; d++)
-                    if (cnt[d])
-                        touched.push_back(d);
-            } else {
-                std::sort(touched.begin(), touched.end());
+                for (size_t w = w0; w <= w1; w++) {
+                    uint64_t m = mark[w];
+                    mark[w] = 0;
+                    while (m) {
+                        const int b = __builtin_ctzll(m);
+                        touched.push_back((int)(w * 64 + (size_t)b));
+                        m &= m - 1;
+                    }
+                }
             }
             const int base = (int)img.ud_l.size();
             int off = base;
