@@ -40,7 +40,8 @@ enum { B4N_D, B4N_G, B4N_S, B4N_B, B4N_DP, B4N_SP, B4N_COUNT };
     X(czbd) X(czbs) X(czbdsw) X(czbdswg) X(czbssw) X(czbsswg)                    \
     X(MJS) X(MJSWS) X(MJSWGS) X(MJD) X(MJSWD) X(MJSWGD)                          \
     X(PhiBS) X(PhiBSWS) X(PhiBSWGS) X(PhiBD) X(PhiBSWD) X(PhiBSWGD)              \
-    X(drainConductance) X(sourceConductance) X(m) X(mult_i) X(mult_q)
+    X(drainConductance) X(sourceConductance) X(m) X(mult_i) X(mult_q)           \
+    X(version47)
 
 #define B4P_ENUM(f) B4P_##f,
 enum { B4P_LIST(B4P_ENUM) B4P_COUNT };

@@ -1582,37 +1582,71 @@ NGSF_HD inline int bsim4_eval(const B4Ctx &x, const double *P, size_t ps, double
     const double mult_i = Q(mult_i), mult_q = Q(mult_q);
     const double gjbd = gbd, gjbs = gbs;
     const double gdpr = Q(drainConductance), gspr = Q(sourceConductance);
-    /* right-hand side: d', g', b', s' */
-    sv[0 * svs] = (mult_i * (ceqjd - ceqbd - ceqdrn) - mult_q * ceqqd);
-    sv[1 * svs] = -(mult_q * ceqqg);
-    sv[2 * svs] = (mult_i * (ceqbd + ceqbs - ceqjd - ceqjs) - mult_q * ceqqb);
-    sv[3 * svs] = (mult_i * (ceqdrn - ceqbs + ceqjs) + mult_q * (ceqqg + ceqqb + ceqqd));
-    /* gate row (BSIM4_34..37) */
-    sv[4 * svs] = mult_q * gcggb;
-    sv[5 * svs] = mult_q * gcgdb;
-    sv[6 * svs] = mult_q * gcgsb;
-    sv[7 * svs] = mult_q * gcgbb;
-    /* drain-prime row (BSIM4_44..50) */
-    sv[8 * svs] = mult_i * (gdpr + gds + gbd + RevSum + gbdpdp) + mult_q * gcddb;
-    sv[9 * svs] = -(mult_i * gdpr);
-    sv[10 * svs] = mult_i * (Gmx + gbdpg) + mult_q * gcdgb;
-    sv[11 * svs] = -(mult_i * (gds + FwdSum - gbdpsp) - mult_q * gcdsb);
-    sv[12 * svs] = -(mult_i * (gjbd - Gmbsx - gbdpb) - mult_q * gcdbb);
-    sv[13 * svs] = -(mult_i * gdpr);
-    sv[14 * svs] = mult_i * gdpr;
-    /* source-prime row (BSIM4_51..57) */
-    sv[15 * svs] = -(mult_i * (gds + RevSum - gbspdp) - mult_q * gcsdb);
-    sv[16 * svs] = mult_q * gcsgb + mult_i * (gbspg - Gmx);
-    sv[17 * svs] = mult_i * (gspr + gds + gbs + FwdSum + gbspsp) + mult_q * gcssb;
-    sv[18 * svs] = -(mult_i * gspr);
-    sv[19 * svs] = -(mult_i * (gjbs + Gmbsx - gbspb) - mult_q * gcsbb);
-    sv[20 * svs] = -(mult_i * gspr);
-    sv[21 * svs] = mult_i * gspr;
-    /* bulk-prime row (BSIM4_58..61) */
-    sv[22 * svs] = mult_q * gcbdb - mult_i * (gjbd - gbbdp);
-    sv[23 * svs] = mult_q * gcbgb - mult_i * gbgs;
-    sv[24 * svs] = mult_q * gcbsb - mult_i * (gjbs - gbbsp);
-    sv[25 * svs] = mult_i * (gjbd + gjbs - gbbs) + mult_q * gcbbb;
+    if (Q(version47) == 0.0) {
+        /* right-hand side: d', g', b', s' */
+        sv[0 * svs] = (mult_i * (ceqjd - ceqbd - ceqdrn) - mult_q * ceqqd);
+        sv[1 * svs] = -(mult_q * ceqqg);
+        sv[2 * svs] = (mult_i * (ceqbd + ceqbs - ceqjd - ceqjs) - mult_q * ceqqb);
+        sv[3 * svs] = (mult_i * (ceqdrn - ceqbs + ceqjs) + mult_q * (ceqqg + ceqqb + ceqqd));
+        /* gate row (BSIM4_34..37) */
+        sv[4 * svs] = mult_q * gcggb;
+        sv[5 * svs] = mult_q * gcgdb;
+        sv[6 * svs] = mult_q * gcgsb;
+        sv[7 * svs] = mult_q * gcgbb;
+        /* drain-prime row (BSIM4_44..50) */
+        sv[8 * svs] = mult_i * (gdpr + gds + gbd + RevSum + gbdpdp) + mult_q * gcddb;
+        sv[9 * svs] = -(mult_i * gdpr);
+        sv[10 * svs] = mult_i * (Gmx + gbdpg) + mult_q * gcdgb;
+        sv[11 * svs] = -(mult_i * (gds + FwdSum - gbdpsp) - mult_q * gcdsb);
+        sv[12 * svs] = -(mult_i * (gjbd - Gmbsx - gbdpb) - mult_q * gcdbb);
+        sv[13 * svs] = -(mult_i * gdpr);
+        sv[14 * svs] = mult_i * gdpr;
+        /* source-prime row (BSIM4_51..57) */
+        sv[15 * svs] = -(mult_i * (gds + RevSum - gbspdp) - mult_q * gcsdb);
+        sv[16 * svs] = mult_q * gcsgb + mult_i * (gbspg - Gmx);
+        sv[17 * svs] = mult_i * (gspr + gds + gbs + FwdSum + gbspsp) + mult_q * gcssb;
+        sv[18 * svs] = -(mult_i * gspr);
+        sv[19 * svs] = -(mult_i * (gjbs + Gmbsx - gbspb) - mult_q * gcsbb);
+        sv[20 * svs] = -(mult_i * gspr);
+        sv[21 * svs] = mult_i * gspr;
+        /* bulk-prime row (BSIM4_58..61) */
+        sv[22 * svs] = mult_q * gcbdb - mult_i * (gjbd - gbbdp);
+        sv[23 * svs] = mult_q * gcbgb - mult_i * gbgs;
+        sv[24 * svs] = mult_q * gcbsb - mult_i * (gjbs - gbbsp);
+        sv[25 * svs] = mult_i * (gjbd + gjbs - gbbs) + mult_q * gcbbb;
+    } else {
+        /* BSIM4v7 scales each stamp's whole sum by m and adds its terms in
+         * the order of b4v7ld.c:4909-4928 and 4994-5066 (the terms of the
+         * selectors this load rejects are zero and left out); a 4.7
+         * instance has mult_i = mult_q = m */
+        const double m = mult_i;
+        sv[0 * svs] = m * (((ceqjd - ceqbd) - ceqdrn) - ceqqd);
+        sv[1 * svs] = -(m * ceqqg);
+        sv[2 * svs] = m * ((((ceqbd + ceqbs) - ceqjd) - ceqjs) - ceqqb);
+        sv[3 * svs] = m * (((((ceqdrn - ceqbs) + ceqjs) + ceqqg) + ceqqb) + ceqqd);
+        sv[4 * svs] = m * gcggb;
+        sv[5 * svs] = m * gcgdb;
+        sv[6 * svs] = m * gcgsb;
+        sv[7 * svs] = m * gcgbb;
+        sv[8 * svs] = m * (((((gdpr + gds) + gbd) + RevSum) + gcddb) + gbdpdp);
+        sv[9 * svs] = -(m * gdpr);
+        sv[10 * svs] = m * ((Gmx + gcdgb) + gbdpg);
+        sv[11 * svs] = -(m * (((gds + FwdSum) - gcdsb) - gbdpsp));
+        sv[12 * svs] = -(m * (((gjbd - Gmbsx) - gcdbb) - gbdpb));
+        sv[13 * svs] = -(m * gdpr);
+        sv[14 * svs] = m * gdpr;
+        sv[15 * svs] = -(m * (((gds + RevSum) - gcsdb) - gbspdp));
+        sv[16 * svs] = m * ((gcsgb - Gmx) + gbspg);
+        sv[17 * svs] = m * (((((gspr + gds) + gbs) + FwdSum) + gcssb) + gbspsp);
+        sv[18 * svs] = -(m * gspr);
+        sv[19 * svs] = -(m * (((gjbs + Gmbsx) - gcsbb) - gbspb));
+        sv[20 * svs] = -(m * gspr);
+        sv[21 * svs] = m * gspr;
+        sv[22 * svs] = m * ((gcbdb - gjbd) + gbbdp);
+        sv[23 * svs] = m * (gcbgb - gbgs);
+        sv[24 * svs] = m * ((gcbsb - gjbs) + gbbsp);
+        sv[25 * svs] = m * (((gjbd + gjbs) + gcbbb) - gbbs);
+    }
     /* GIDL (BSIM4_62..69) */
     sv[26 * svs] = mult_i * Ggidld;
     sv[27 * svs] = mult_i * Ggidlg;

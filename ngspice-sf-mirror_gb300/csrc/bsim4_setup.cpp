@@ -90,6 +90,7 @@ struct B4Model {
     double DunitLengthSidewallTempJctCap, SunitLengthGateSidewallTempJctCap;
     double DunitLengthGateSidewallTempJctCap;
     double PhiBS, PhiBD, PhiBSWS, PhiBSWD, PhiBSWGS, PhiBSWGD;
+    bool v47;   /* version 4.7.x: the reference's BSIM4v7 device */
 };
 
 #define M(f) (bm.v[MF_##f])
@@ -157,6 +158,10 @@ void model_temp(B4Model &bm, double Temp)
     if (M(DsidewallJctPotential) < 0.1) M(DsidewallJctPotential) = 0.1;
     if (M(DGatesidewallJctPotential) < 0.1) M(DGatesidewallJctPotential) = 0.1;
 
+    /* BSIM4v7 defaults cf in setup, before the thickness consistency below
+     * can change toxe (b4v7set.c:1908-1911); 4.8 defaults it after
+     * (b4temp.c:173-175) */
+    const double toxe_setup = M(toxe);
     /* mtrlMod 0 oxide thickness consistency */
     {
         double chktol = fabs(M(toxe));
@@ -178,7 +183,7 @@ void model_temp(B4Model &bm, double Temp)
     bm.epssub = kEPSSI;
     const double epsrox = bm.epsrox, toxe = bm.toxe, epssub = bm.epssub;
     if (!G(cf))
-        M(cf) = 2.0 * epsrox * kEPS0 / kPI * log(1.0 + 0.4e-6 / toxe);
+        M(cf) = 2.0 * epsrox * kEPS0 / kPI * log(1.0 + 0.4e-6 / (bm.v47 ? toxe_setup : toxe));
     bm.coxe = epsrox * kEPS0 / toxe;
 
     bm.coxp = M(epsrox) * kEPS0 / M(toxp);
@@ -367,16 +372,37 @@ const B4Model &resolve_model(const Model &m, double temp, double tnom_opt)
     std::memset(&bm, 0, sizeof bm);
     M(type) = m.polarity;
     G(type) = true;
+    bm.v47 = m.bsim4_v47();
+    /* model parameters the BSIM4v7 device does not have (bsim4v7/b4v7.c):
+     * its parser ignores them (parser/inpgmod.c:189) */
+    static const char *kNotIn47[] = {"gidlclamp", "idovvdsc", "ketac", "lketac", "wketac",
+                                     "pketac"};
     for (const auto &kv : m.p.v) {
         const std::string &k = kv.first;
         if (k == "level")
             continue;
         if (k == "version") {
-            if (kv.second < 4.8 - 1e-9 || kv.second >= 4.9)
+            if (!bm.v47 && (kv.second < 4.8 - 1e-9 || kv.second >= 4.9))
                 throw NetlistError("BSIM4 model " + m.name +
-                                   ": only version 4.8.x is implemented (other versions select "
-                                   "another device in the reference)");
+                                   ": only versions 4.7.x and 4.8.x are implemented (other "
+                                   "versions select another device in the reference)");
             continue;
+        }
+        if (bm.v47) {
+            bool skip = false;
+            for (const char *x : kNotIn47)
+                if (k == x)
+                    skip = true;
+            if (skip)
+                continue;
+            /* BSIM4v7 also has a model-level rgeomod (b4v7.c:137) */
+            if (k == "rgeomod") {
+                if (kv.second != 0.0)
+                    throw NetlistError("BSIM4 model " + m.name +
+                                       ": rgeomod=" + std::to_string((int)kv.second) +
+                                       " is not supported by the GPU load (rgeomod=0 only)");
+                continue;
+            }
         }
         int field = -1;
         for (const auto &ne : kNames)
@@ -433,6 +459,11 @@ void bsim4_params(const Circuit &c, const Model &m, const Instance &in, double *
         if (!ok)
             throw NetlistError("BSIM4 instance " + in.name + ": parameter '" + kv.first +
                                "' is not supported");
+        /* the BSIM4v7 instance table has no current/charge multipliers
+         * (bsim4v7/b4v7.c): its parser rejects them (parser/inpdpar.c:130) */
+        if (bm.v47 && (kv.first == "mult_i" || kv.first == "mult_q"))
+            throw NetlistError("BSIM4 instance " + in.name + ": unknown parameter (" +
+                               kv.first + ") for a version 4.7 model");
     }
     const double scale = 1.0;
     const double L = ip.has("l") ? ip.get("l", 0) * scale : 5.0e-6;
@@ -542,6 +573,10 @@ void bsim4_params(const Circuit &c, const Model &m, const Instance &in, double *
     PP(vfbsdoff) = PP(vfbsdoff) * (1.0 + PP(tvfbsdoff) * delTemp);
     PP(voff) = PP(voff) * (1.0 + PP(tvoff) * delTemp);
     PP(nfactor) = PP(nfactor) + PP(tnfactor) * delTemp / Tnom;
+    /* BSIM4v7 never bins tvoffcv, so its size-dependent copy stays 0
+     * (b4v7temp.c:1267; 4.8 bins it at b4temp.c:868-871) */
+    if (bm.v47)
+        PP(tvoffcv) = 0.0;
     PP(voffcv) = PP(voffcv) * (1.0 + PP(tvoffcv) * delTemp);
     PP(eta0) = PP(eta0) + PP(teta0) * delTemp / Tnom;
 
@@ -976,6 +1011,7 @@ void bsim4_params(const Circuit &c, const Model &m, const Instance &in, double *
     SET(m, mm);
     SET(mult_i, mult_i * mm);
     SET(mult_q, mult_q * mm);
+    SET(version47, bm.v47 ? 1.0 : 0.0);
 #undef SET
 #undef PP
     (void)kKb;

@@ -48,6 +48,15 @@ struct Model {
     int level = 1;
     Params p;
     std::vector<int> instances; /* indices into Circuit::inst, creation order */
+    /* A BSIM4 card whose version starts with 4.7 selects the reference's
+     * separate BSIM4v7 device (parser/inpdomod.c:297-313); 4.8, "default" or
+     * no version select BSIM4 4.8.3. */
+    bool bsim4_v47() const {
+        if (kind != K_BSIM4 || !p.has("version"))
+            return false;
+        const double v = p.get("version", 4.8);
+        return v >= 4.7 - 1e-9 && v < 4.8 - 1e-9;
+    }
 };
 
 struct Waveform {

@@ -522,11 +522,15 @@ std::unique_ptr<Circuit> parse_netlist(const std::string &text)
             defaultInst[in.kind].push_back((int)i);
         }
     }
+    /* BSIM4v7 follows BSIM4 in the device table (devices/dev.c:154-157), so
+     * every 4.7 model loads after every 4.8 model */
+    const int kV47Last = 1 << 30;
     for (int kk = 0; kk < K_COUNT; kk++) {
         std::vector<std::pair<int, std::vector<int>>> g;
         for (auto &mr : modelRank)
             if (c->models[mr.first].kind == kk)
-                g.push_back({mr.second, c->models[mr.first].instances});
+                g.push_back({mr.second - (c->models[mr.first].bsim4_v47() ? kV47Last : 0),
+                             c->models[mr.first].instances});
         if (defaultModelRank.count(kk))
             g.push_back({defaultModelRank[kk], defaultInst[kk]});
         std::sort(g.begin(), g.end(), [](auto &a, auto &b) { return a.first > b.first; });

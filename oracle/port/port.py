@@ -316,9 +316,17 @@ class Circuit:
         for idx, e in enumerate(inst):
             key = ("default", e[0]) if e[0] not in (K_MOS1, K_BSIM4, K_DIO) else e[3]
             groups.setdefault(key, []).append(idx)
+        def v47(key):
+            # version 4.7 cards select the BSIM4v7 device, which follows
+            # BSIM4 in the device table (devices/dev.c:154-157)
+            if not isinstance(key, str) or key not in self.models:
+                return False
+            ver = self.models[key][1].get("version")
+            return ver is not None and 4.7 - 1e-9 <= ver < 4.8 - 1e-9
+
         for kk in range(7):
             keys = [key for key in groups if (inst[groups[key][0]][0] == kk)]
-            keys.sort(key=lambda q: -model_order[q])
+            keys.sort(key=lambda q: (v47(q), -model_order[q]))
             for key in keys:
                 self.order[kk] += list(reversed(groups[key]))
         self.inst = inst

@@ -22,7 +22,8 @@
  * them; the load itself writes state 0, and state 1 in MODEINITTRAN),
  * the integration coefficients, gmin, srcFact, and each BSIM4 instance's
  * BSIM4von (kept between iterations for the gate-voltage limiting), in
- * the model / instance list order CKTload visits.  Record layout:
+ * the model / instance list order CKTload visits: 4.8 instances, then
+ * version 4.7 (BSIM4v7) ones.  Record layout:
  *   int32 iteration index (0-based, as in ITERS.bin), int32 nstates,
  *   int32 nvon, int32 0, double ag[2], deltaOld[2], gmin, srcFact,
  *   nstates x double state0, state1, state2, nvon x double von.
@@ -98,6 +99,9 @@ static void snapshot_states(CKTcircuit *ckt)
                 }
                 pre_von[nv++] = here->BSIM4von;
             }
+    /* then the version 4.7 instances: BSIM4v7 follows BSIM4 in the device
+     * table, so CKTload reaches them after every 4.8 instance */
+    nv = oracle_v47_von(ckt, &pre_von, &pre_cap_von, nv);
     pre_nvon = nv;
     pre_valid = 1;
 }

@@ -37,6 +37,7 @@
 #include "oracle_ref.h"
 
 extern SPICEdev *get_bsim4_info(void);
+extern SPICEdev *get_bsim4v7_info(void);
 extern SPICEdev *get_cap_info(void);
 extern SPICEdev *get_dio_info(void);
 extern SPICEdev *get_isrc_info(void);
@@ -48,10 +49,10 @@ extern IFsimulator SIMinfo;
 extern int spice_num_analysis(void);
 extern SPICEanalysis **spice_analysis_ptr(void);
 
-/* Same relative order as the reference table: bsim4 < cap < dio < isrc <
- * mos1 < res < vsrc. */
+/* Same relative order as the reference table: bsim4 < bsim4v7 < cap < dio <
+ * isrc < mos1 < res < vsrc. */
 static SPICEdev *(*oracle_devices[])(void) = {
-    get_bsim4_info, get_cap_info, get_dio_info, get_isrc_info,
+    get_bsim4_info, get_bsim4v7_info, get_cap_info, get_dio_info, get_isrc_info,
     get_mos1_info, get_res_info, get_vsrc_info,
 };
 #define ORACLE_NDEV ((int)(sizeof(oracle_devices) / sizeof(oracle_devices[0])))

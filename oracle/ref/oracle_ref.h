@@ -15,4 +15,9 @@ typedef struct oracle_trace {
 extern oracle_trace_t oracle_trace;
 void oracle_init(void);
 
+/* von47.c: appends every BSIM4v7 instance's von to (*buf)[nv..], growing
+ * the buffer (capacity *cap) as needed; returns the new count.  The
+ * argument is a CKTcircuit *. */
+int oracle_v47_von(void *ckt, double **buf, int *cap, int nv);
+
 #endif

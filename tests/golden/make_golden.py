@@ -36,6 +36,34 @@ from ngspice_gb300 import netlists  # noqa: E402
 
 REF_BIN = os.path.join(ROOT, "oracle", "_ref", "ngspice_ref")
 
+def bsim4_chain_v47_mixed(stages: int = 8) -> str:
+    """An inverter chain whose odd stages use version 4.7 model cards (the
+    reference's separate BSIM4v7 device) and whose even stages use 4.8
+    cards.  The 4.7 nmos card gives toxp and dtox without toxe (BSIM4v7
+    defaults cf from the set-up toxe) and a ketac that the BSIM4v7 parser
+    ignores; its instances carry m=2 (BSIM4v7 scales each stamp's whole
+    sum).  The 4.7 models are referenced first, yet load after the 4.8
+    ones."""
+    lines = ["* bsim4 inverter chain, version 4.7 and 4.8 cards",
+             ".model n47 nmos level=54 version=4.7.0 vth0=0.42 toxp=1.45e-9 dtox=0.3e-9"
+             " ketac=-0.04",
+             ".model p47 pmos level=54 version=4.7.0 vth0=-0.41 toxe=1.75e-9",
+             ".model n48 nmos level=54 version=4.8.3 vth0=0.42 toxe=1.75e-9 ketac=-0.04",
+             ".model p48 pmos level=54 vth0=-0.41 toxe=1.75e-9",
+             "vdd vdd 0 1.0",
+             "vin n0 0 pulse(0 1 20p 10p 10p 200p 500p)"]
+    for k in range(1, stages + 1):
+        if k % 2:
+            lines.append(f"mn{k} n{k} n{k-1} 0 0 n47 w=100n l=45n m=2")
+            lines.append(f"mp{k} n{k} n{k-1} vdd vdd p47 w=400n l=45n")
+        else:
+            lines.append(f"mn{k} n{k} n{k-1} 0 0 n48 w=200n l=45n")
+            lines.append(f"mp{k} n{k} n{k-1} vdd vdd p48 w=400n l=45n")
+        lines.append(f"c{k} n{k} 0 1f")
+    lines += [".tran 1p 1n", ".options klu", ".end", ""]
+    return "\n".join(lines)
+
+
 # name -> (netlist text, number of Newton iterations to capture, record the
 # linearisation point of every k-th captured iteration (0: none))
 CASES = {
@@ -49,6 +77,12 @@ CASES = {
     # one Monte Carlo instance: per-device mismatch model cards
     "bsim4_mc_s5": (netlists.random_logic(n_transistors=120, seed=5, n_inputs=6,
                                           tstop="600p", mismatch=True), 150, 5),
+    # version 4.7 model cards: the reference's BSIM4v7 device
+    "v47_logic_s3": (netlists.random_logic(n_transistors=120, seed=3, n_inputs=6,
+                                           tstop="1n").replace("level=54",
+                                                               "level=54 version=4.7.0"),
+                     200, 4),
+    "v47_chain_mixed": (bsim4_chain_v47_mixed(), 200, 1),
 }
 
 # Circuits at the sizes the benchmarks run, with no iteration capture:

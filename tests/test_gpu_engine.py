@@ -10,7 +10,7 @@ from tolerances import matrix_violation, rhs_violation, waveform_violation
 pytestmark = pytest.mark.gpu
 
 CASES = ["rc_ladder", "inverter_chain32"]
-BSIM4_CASES = ["bsim4_chain8", "bsim4_logic_s3"]
+BSIM4_CASES = ["bsim4_chain8", "bsim4_logic_s3", "v47_chain_mixed", "v47_logic_s3"]
 DIODE_CASES = ["diode_rectifier", "mos1_mix"]
 
 

@@ -17,7 +17,7 @@ from tolerances import matrix_violation, rhs_violation_rowscaled
 
 pytestmark = pytest.mark.gpu
 
-CASES = ["bsim4_chain8", "bsim4_logic_s3", "bsim4_mc_s5"]
+CASES = ["bsim4_chain8", "bsim4_logic_s3", "bsim4_mc_s5", "v47_chain_mixed", "v47_logic_s3"]
 
 
 @pytest.fixture(scope="module")

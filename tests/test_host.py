@@ -49,6 +49,34 @@ def test_unsupported_input_is_reported(built_lib):
         E.Circuit("t\nv1 a a 1\nr1 a 0 1\n.tran 1n 2n\n.end\n", host_only=True)
 
 
+def test_bsim4_version_selection(built_lib):
+    """Version 4.7 cards select the BSIM4v7 restatement, which numbers and
+    lays out the mixed 4.7/4.8 chain as the reference does; its parser
+    ignores the 4.8-only model parameters and rejects the 4.8-only instance
+    multipliers (bsim4v7/b4v7.c).  Versions before 4.7 select devices the
+    GPU load does not have."""
+    from ngspice_gb300 import engine as E
+    g = golden("v47_chain_mixed")
+    c = E.Circuit(str(g["netlist"]), host_only=True)
+    assert c.names() == list(g["names"])
+    cp, ri = c.pattern()
+    mine = {(int(ri[p]), j) for j in range(c.n) for p in range(cp[j], cp[j + 1])}
+    p0, p1 = g["it_ptr"][0], g["it_ptr"][1]
+    assert mine == set(zip(g["it_rows"][p0:p1].tolist(), g["it_cols"][p0:p1].tolist()))
+    deck = ("t\n.model nm nmos level=54 version={v} vth0=0.42 toxe=1.75e-9 {mod}\n"
+            "m1 d g 0 0 nm w=200n l=45n {inst}\nvd d 0 1\nvg g 0 1\n.tran 1p 10p\n.end\n")
+    E.Circuit(deck.format(v="4.7.0", mod="gidlclamp=-1e-5 idovvdsc=1e-9 ketac=0.1 lketac=0"
+                          " rgeomod=0", inst="m=2"), host_only=True)
+    E.Circuit(deck.format(v="4.8.3", mod="ketac=0.1", inst="mult_i=2 mult_q=0.5"),
+              host_only=True)
+    with pytest.raises(E.EngineError, match=r"unknown parameter \(mult_i\)"):
+        E.Circuit(deck.format(v="4.7.0", mod="", inst="mult_i=2"), host_only=True)
+    with pytest.raises(E.EngineError, match="rgeomod=1"):
+        E.Circuit(deck.format(v="4.7", mod="rgeomod=1", inst=""), host_only=True)
+    with pytest.raises(E.EngineError, match="versions 4.7.x and 4.8.x"):
+        E.Circuit(deck.format(v="4.6.5", mod="", inst=""), host_only=True)
+
+
 def test_run_refuses_host_only_circuit(built_lib):
     from ngspice_gb300 import engine as E
     g = golden("rc_ladder")

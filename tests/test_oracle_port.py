@@ -110,12 +110,37 @@ def test_port_bsim4_monte_carlo_instance_matches_reference():
                               r["values"][:, idx]) < 0.01
 
 
-def test_port_bsim4_newton_stamps_match_reference():
+V47_CASES = ["v47_logic_s3", "v47_chain_mixed"]
+
+
+@pytest.mark.parametrize("name", V47_CASES)
+def test_port_bsim4_v47_decks_match_reference(name):
+    """Version 4.7 model cards, which the reference runs on its separate
+    BSIM4v7 device: the 120-transistor logic deck, and an inverter chain
+    mixing 4.7 and 4.8 cards (a 4.7 nmos card with toxp and dtox but no
+    toxe, a ketac the 4.7 parser ignores, m=2 instances).  Identical Newton
+    and step counts, time points equal to rounding, waveforms within 1% of
+    the tolerance."""
+    g = golden(name)
+    r = port.simulate(str(g["netlist"]))
+    st, ref = r["stats"], g["stats"]
+    assert st["status"] == 0
+    assert (st["numIter"], st["tranIter"], st["accepted"], st["rejected"]) == \
+        (ref[0], ref[1], ref[3], ref[4])
+    assert r["names"] == list(g["names"])
+    assert np.max(np.abs(r["times"] - g["times"])) <= 1e-9 * g["times"][-1]
+    assert waveform_violation(r["names"], g["times"], g["values"], r["times"],
+                              r["values"]) < 0.01
+
+
+@pytest.mark.parametrize("name", ["bsim4_chain8", "v47_chain_mixed"])
+def test_port_bsim4_newton_stamps_match_reference(name):
     """Per-iteration stamped Jacobian and right-hand side of the first
-    200 Newton iterations of the BSIM4 inverter chain (operating point and
-    transient) within 1e-12, row-scaled, of the reference's."""
+    200 Newton iterations of the BSIM4 inverter chains (operating point and
+    transient; 4.8 cards, and 4.7 and 4.8 cards mixed) within 1e-12,
+    row-scaled, of the reference's."""
     from tolerances import matrix_violation_dense
-    g = golden("bsim4_chain8")
+    g = golden(name)
     r = port.simulate(str(g["netlist"]), dump=len(g["it_kind"]))
     assert len(r["dump_ax"]) == len(g["it_kind"])
     for it in range(len(g["it_kind"])):
