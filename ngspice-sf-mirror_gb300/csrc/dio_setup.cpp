@@ -35,7 +35,9 @@ const Alias kNames[] = {
     {"nz", "nbv"}, {"area", "area"}, {"pj", "pj"}, {"tlev", "tlev"}, {"tlevc", "tlevc"},
     {"eg", "eg"}, {"xti", "xti"}, {"kf", "kf"}, {"af", "af"}, {"fc", "fc"}, {"fcs", "fcs"},
     {"bv", "bv"}, {"vb", "bv"}, {"vrb", "bv"}, {"var", "bv"}, {"ibv", "ibv"}, {"ib", "ibv"},
-    {"tcv", "tcv"}, {"tbv1", "tcv"}, {"fv_max", "-"}, {"bv_max", "-"}, {"id_max", "-"},
+    {"tcv", "tcv"}, {"tbv1", "tcv"}, {"gap1", "gap1"}, {"gap2", "gap2"}, {"cta", "cta"},
+    {"ctc", "cta"}, {"ctp", "ctp"}, {"tpb", "tpb"}, {"tvj", "tpb"}, {"tphp", "tphp"},
+    {"fv_max", "-"}, {"bv_max", "-"}, {"id_max", "-"},
     {"te_max", "-"}, {"pd_max", "-"},
 };
 }  // namespace
@@ -61,8 +63,13 @@ void dio_params(const Circuit &c, const Model &m, const Instance &in, double *p,
     auto V = [&](const char *k, double d) { return mp.get(k, d); };
     if (G("level") && V("level", 1) != 1)
         throw NetlistError("diode model " + m.name + ": only level 1 is supported");
-    if (V("tlev", 0) != 0 || V("tlevc", 0) != 0)
-        throw NetlistError("diode model " + m.name + ": tlev/tlevc other than 0 are not supported");
+    /* temperature equation selectors (diotemp.c:59-238): tlev 0, 1, 2 and
+     * tlevc 0, 1 */
+    const int tlev = (int)V("tlev", 0), tlevc = (int)V("tlevc", 0);
+    if (tlev < 0 || tlev > 2 || tlevc < 0 || tlevc > 1)
+        throw NetlistError("diode model " + m.name + ": tlev " + std::to_string(tlev) +
+                           " / tlevc " + std::to_string(tlevc) +
+                           " are not supported (tlev 0-2, tlevc 0-1)");
 
     /* DIOsetup defaults */
     const double N = V("n", 1);
@@ -83,6 +90,11 @@ void dio_params(const Circuit &c, const Model &m, const Instance &in, double *p,
     const double eg = V("eg", 1.11);
     const double xti = V("xti", 3);
     const double tcv = V("tcv", 0.0);
+    /* DIOsetup defaults of the tlev 2 band-gap and tlevc 1 coefficients
+     * (diosetup.c:147-166) */
+    const double gap1 = V("gap1", 7.02e-4), gap2 = V("gap2", 1108.0);
+    const double cta = V("cta", 0.0), ctp = V("ctp", 0.0);
+    const double tpb = V("tpb", 0.0), tphp = V("tphp", 0.0);
     const double areaModel = V("area", 1.0), pjModel = V("pj", 0.0);
     if (satCur < 1e-28)
         satCur = 1e-28;
@@ -112,29 +124,53 @@ void dio_params(const Circuit &c, const Model &m, const Instance &in, double *p,
     const double lnTRatio = log(Temp / tnom);
     double factor = 1.0 + (gradT1 * dt) + (gradT2 * dt * dt);
     const double tGrading = grading * factor;
-    const double egfet = 1.16 - (7.02e-4 * Temp * Temp) / (Temp + 1108);
-    const double egfet1 = 1.16 - (7.02e-4 * tnom * tnom) / (tnom + 1108);
+    double egfet, egfet1;
+    if (tlev < 2) {
+        egfet = 1.16 - (7.02e-4 * Temp * Temp) / (Temp + 1108);
+        egfet1 = 1.16 - (7.02e-4 * tnom * tnom) / (tnom + 1108);
+    } else {
+        egfet = eg - (gap1 * Temp * Temp) / (Temp + gap2);
+        egfet1 = eg - (gap1 * tnom * tnom) / (tnom + gap2);
+    }
     const double fact2 = Temp / kRefTemp;
     const double arg = -egfet / (2 * kBoltz * Temp) + 1.1150877 / (kBoltz * (kRefTemp + kRefTemp));
     const double pbfact = -2 * vt * (1.5 * log(fact2) + kCharge * arg);
     const double arg1 = -egfet1 / (kBoltz * 2 * tnom) + 1.1150877 / (2 * kBoltz * kRefTemp);
     const double fact1 = tnom / kRefTemp;
     const double pbfact1 = -2 * vtnom * (1.5 * log(fact1) + kCharge * arg1);
-    const double pbo = (jctPot - pbfact1) / fact1;
-    const double gmaold = (jctPot - pbo) / pbo;
-    double tJctCap = junctionCap / (1 + tGrading * (400e-6 * (tnom - kRefTemp) - gmaold));
-    const double tJctPot = pbfact + fact2 * pbo;
-    const double gmanew = (tJctPot - pbo) / pbo;
-    tJctCap *= 1 + tGrading * (400e-6 * (Temp - kRefTemp) - gmanew);
-    const double pboSW = (jctSWPot - pbfact1) / fact1;
-    const double gmaSWold = (jctSWPot - pboSW) / pboSW;
-    double tJctSWCap = junctionSWCap / (1 + gradSW * (400e-6 * (tnom - kRefTemp) - gmaSWold));
-    const double tJctSWPot = pbfact + fact2 * pboSW;
-    const double gmaSWnew = (tJctSWPot - pboSW) / pboSW;
-    tJctSWCap *= 1 + gradSW * (400e-6 * (Temp - kRefTemp) - gmaSWnew);
-    const double a1 = ((Temp / tnom) - 1) * eg / vte;
-    const double a2 = xti / N * lnTRatio;
-    const double tSatCur = satCur * area * mm * exp(a1 + a2);
+    double tJctCap, tJctPot, tJctSWCap, tJctSWPot;
+    if (tlevc == 0) {
+        const double pbo = (jctPot - pbfact1) / fact1;
+        const double gmaold = (jctPot - pbo) / pbo;
+        tJctCap = junctionCap / (1 + tGrading * (400e-6 * (tnom - kRefTemp) - gmaold));
+        tJctPot = pbfact + fact2 * pbo;
+        const double gmanew = (tJctPot - pbo) / pbo;
+        tJctCap *= 1 + tGrading * (400e-6 * (Temp - kRefTemp) - gmanew);
+        const double pboSW = (jctSWPot - pbfact1) / fact1;
+        const double gmaSWold = (jctSWPot - pboSW) / pboSW;
+        tJctSWCap = junctionSWCap / (1 + gradSW * (400e-6 * (tnom - kRefTemp) - gmaSWold));
+        tJctSWPot = pbfact + fact2 * pboSW;
+        const double gmaSWnew = (tJctSWPot - pboSW) / pboSW;
+        tJctSWCap *= 1 + gradSW * (400e-6 * (Temp - kRefTemp) - gmaSWnew);
+    } else {
+        /* linear in the distance from the reference temperature */
+        tJctPot = jctPot - tpb * (Temp - kRefTemp);
+        tJctCap = junctionCap * (1 + cta * (Temp - kRefTemp));
+        tJctSWPot = jctSWPot - tphp * (Temp - kRefTemp);
+        tJctSWCap = junctionSWCap * (1 + ctp * (Temp - kRefTemp));
+    }
+    double tSatCur;
+    if (tlev < 2) {
+        const double a1 = ((Temp / tnom) - 1) * eg / vte;
+        const double a2 = xti / N * lnTRatio;
+        tSatCur = satCur * area * mm * exp(a1 + a2);
+    } else {
+        /* band-gap form: Eg(Tnom) / (N vt(Tnom)) - Eg(T) / (N vt(T)) */
+        const double a0 = egfet1 / (N * vtnom);
+        const double a1 = egfet / vte;
+        const double a2 = xti / N * lnTRatio;
+        tSatCur = satCur * area * mm * exp(a0 - a1 + a2);
+    }
     const double xfc = log(1 - fc);
     const double xfcs = log(1 - fcs);
     const double tF1 = tJctPot * (1 - exp((1 - tGrading) * xfc)) / (1 - tGrading);
@@ -144,7 +180,7 @@ void dio_params(const Circuit &c, const Model &m, const Instance &in, double *p,
     const double tVcrit = vte * log(vte / (kRoot2 * totalSatCur));
     double tBrkdwnV = 0.0;
     if (G("bv")) {
-        double tBV = V("bv", 0) - tcv * dt;
+        double tBV = tlev == 0 ? V("bv", 0) - tcv * dt : V("bv", 0) * (1 - tcv * dt);
         double cbv = mm * bvCur;
         double xbv;
         if (cbv < totalSatCur * tBV / vt) {

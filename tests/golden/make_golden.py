@@ -135,6 +135,25 @@ GEAR_CASES = {
 }
 
 
+# Diode temperature equations away from the nominal temperature: tlev 1
+# (scaled breakdown voltage) with tlevc 1 (linear junction potential and
+# capacitance) at 75 C; sidewall junctions with tlevc 0 at 75 C (the
+# reference stops with "timestep too small" on this deck's sidewall junction
+# under tlevc 1); tlev 2 (band-gap saturation current) at -20 C, tnom 30 C.
+_DR = ".model dr d is=2e-14 n=1.1 rs=2 cjo=2p vj=0.8 m=0.4 tt=5p"
+DIODE_TEMP_CASES = {
+    "dio_tlev1_75c": lambda: netlists.diode_rectifier().replace(
+        _DR, _DR + " bv=1.8 tcv=1e-3 tlev=1 tlevc=1 cta=1e-3 tpb=1.5e-3 ttt1=1e-3"
+        " trs1=2e-3").replace(".options klu", ".options klu temp=75"),
+    "dio_sw_75c": lambda: netlists.diode_rectifier().replace(
+        _DR, _DR + " cjsw=0.3p pj=2 vjsw=0.7 mjsw=0.3").replace(
+        ".options klu", ".options klu temp=75"),
+    "dio_tlev2_m20c": lambda: netlists.diode_rectifier().replace(
+        _DR, _DR + " tlev=2 eg=1.12 gap1=7.5e-4 gap2=1200 xti=3.2 bv=3 tcv=2e-3").replace(
+        ".options klu", ".options klu temp=-20 tnom=30"),
+}
+
+
 def bsim4_logic_s3_tight() -> str:
     text = netlists.random_logic(n_transistors=120, seed=3, n_inputs=6, tstop="400p")
     return text.replace(".options klu", TIGHT_OPTIONS)
@@ -297,7 +316,8 @@ def main(argv: list[str]) -> int:
             np.savez_compressed(path, **out)
             print(f"bsim4_logic_s3_tight: {len(res['times'])} points, stats={res['stats'].tolist()}"
                   f" -> {os.path.getsize(path)} bytes")
-        for name, make in list(GEAR_CASES.items()) + list(RING_CASES.items()):
+        for name, make in (list(GEAR_CASES.items()) + list(RING_CASES.items()) +
+                           list(DIODE_TEMP_CASES.items())):
             if only and name not in only:
                 continue
             text = make()

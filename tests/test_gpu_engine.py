@@ -11,7 +11,9 @@ pytestmark = pytest.mark.gpu
 
 CASES = ["rc_ladder", "inverter_chain32"]
 BSIM4_CASES = ["bsim4_chain8", "bsim4_logic_s3", "v47_chain_mixed", "v47_logic_s3"]
-DIODE_CASES = ["diode_rectifier", "mos1_mix"]
+# the rectifier away from the nominal temperature: tlev 1 / tlevc 1 with
+# breakdown at 75 C, sidewall junctions at 75 C, tlev 2 at -20 C
+DIODE_CASES = ["diode_rectifier", "mos1_mix", "dio_tlev1_75c", "dio_sw_75c", "dio_tlev2_m20c"]
 
 
 @pytest.fixture(scope="module")

@@ -77,6 +77,21 @@ def test_bsim4_version_selection(built_lib):
         E.Circuit(deck.format(v="4.6.5", mod="", inst=""), host_only=True)
 
 
+def test_diode_temperature_selectors(built_lib):
+    """Diode tlev 0-2 and tlevc 0-1 compile (diotemp.c); other selector
+    values are refused with a message."""
+    from ngspice_gb300 import engine as E
+    deck = ("t\n.model dd d is=1e-14 {sel}\nd1 a 0 dd\nr1 a b 1k\nv1 b 0 1\n"
+            ".tran 1n 10n\n.options temp=60\n.end\n")
+    for sel in ("tlev=1 tlevc=1 cta=1e-3 ctc=1e-3 tpb=1e-3 tvj=1e-3 ctp=1e-3 tphp=1e-3",
+                "tlev=2 gap1=7e-4 gap2=1100 eg=1.1"):
+        E.Circuit(deck.format(sel=sel), host_only=True)
+    with pytest.raises(E.EngineError, match="tlev 3"):
+        E.Circuit(deck.format(sel="tlev=3"), host_only=True)
+    with pytest.raises(E.EngineError, match="tlevc 2"):
+        E.Circuit(deck.format(sel="tlevc=2"), host_only=True)
+
+
 def test_run_refuses_host_only_circuit(built_lib):
     from ngspice_gb300 import engine as E
     g = golden("rc_ladder")
