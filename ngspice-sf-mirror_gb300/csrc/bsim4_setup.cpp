@@ -14,6 +14,7 @@
 #include <cstring>
 #include <map>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "bsim4.h"
@@ -405,11 +406,19 @@ const B4Model &resolve_model(const Model &m, double temp, double tnom_opt)
             }
         }
         int field = -1;
-        for (const auto &ne : kNames)
-            if (k == ne.name) {
-                field = ne.field;
-                break;
-            }
+        {
+            /* name -> field, first table entry winning (a Monte Carlo deck
+             * resolves one card per transistor) */
+            static const std::unordered_map<std::string, int> index = [] {
+                std::unordered_map<std::string, int> ix;
+                for (const auto &ne : kNames)
+                    ix.emplace(ne.name, ne.field);
+                return ix;
+            }();
+            auto it = index.find(k);
+            if (it != index.end())
+                field = it->second;
+        }
         if (field < 0)
             throw NetlistError("BSIM4 model " + m.name + ": unknown parameter '" + k + "'");
         double v = kv.second;
