@@ -1616,7 +1616,7 @@ NGSF_HD inline int bsim4_eval(const B4Ctx &x, const double *P, size_t ps, double
         sv[25 * svs] = mult_i * (gjbd + gjbs - gbbs) + mult_q * gcbbb;
     } else {
         /* BSIM4v7 scales each stamp's whole sum by m and adds its terms in
-         * the order of b4v7ld.c:4909-4928 and 4994-5066 (the terms of the
+         * the order of b4v7ld.c:4910-4925 and 5040-5084 (the terms of the
          * selectors this load rejects are zero and left out); a 4.7
          * instance has mult_i = mult_q = m */
         const double m = mult_i;

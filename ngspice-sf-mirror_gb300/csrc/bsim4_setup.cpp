@@ -160,7 +160,7 @@ void model_temp(B4Model &bm, double Temp)
     if (M(DGatesidewallJctPotential) < 0.1) M(DGatesidewallJctPotential) = 0.1;
 
     /* BSIM4v7 defaults cf in setup, before the thickness consistency below
-     * can change toxe (b4v7set.c:1908-1911); 4.8 defaults it after
+     * can change toxe (b4v7set.c:1908-1910); 4.8 defaults it after
      * (b4temp.c:173-175) */
     const double toxe_setup = M(toxe);
     /* mtrlMod 0 oxide thickness consistency */
