@@ -176,6 +176,27 @@ def test_planted_mistake_is_caught():
     assert waveform_violation(r["names"], g["times"], g["values"], r["times"], r["values"]) > 1
 
 
+@pytest.mark.parametrize("name,edit", [
+    # the 4.7 cards read as 4.8: ketac honoured, cf from the reconciled toxe
+    ("v47_chain_mixed", lambda t: t.replace("version=4.7.0", "version=4.8.3")),
+    # the temperature-equation selectors ignored
+    ("dio_tlev1_75c", lambda t: t.replace(" tlev=1 tlevc=1", "")),
+    ("dio_tlev2_m20c", lambda t: t.replace(" tlev=2", "")),
+])
+def test_planted_model_selection_mistakes_are_caught(name, edit):
+    """Each version 4.7 and diode temperature fixture tells its rule apart:
+    the oracle run on the deck read the wrong way leaves the reference's
+    waveforms by more than the tolerance."""
+    g = golden(name)
+    text = edit(str(g["netlist"]))
+    assert text != str(g["netlist"])
+    r = port.simulate(text)
+    names = list(g["names"])
+    idx = [r["names"].index(x) for x in names]
+    assert waveform_violation(names, g["times"], g["values"], r["times"],
+                              r["values"][:, idx]) > 1
+
+
 def test_number_evaluation_matches_reference_rules():
     ev = port.evaluate
     assert ev("2u") == 2 * 10.0 ** -6
